@@ -1,0 +1,419 @@
+#!/usr/bin/env python3
+"""Throughput of the confocal reconstruction hot path on GB300.
+
+Workload (one step): confocal full backprojection of a 256 x 256 scan x 1024
+bin capture (16 ps bins, FP32 storage) into a 256^3 FP32 volume over
+2 x 2 x 1.5 m, then the 5^3 LoG filter (sigma 1 voxel) and min-max
+normalisation.  Seeded synthetic scene (8 planar patches, r^-4 falloff,
+Poisson noise at 1e4 photons per scan point), generated on the device.
+Metric: backprojected voxel-samples/s = (voxels x scan points) per step / time.
+
+  value  device-resident inputs, CUDA-event timed over --steps steps
+  e2e    the same step through fbp_reconstruct_shape_host from pinned HOST
+         buffers (H2D of the cube, D2H of the volume inside the timed region)
+
+--impl reference times the reference algorithm's CPU form (there is no CPU
+backprojection in the reference: the oracle's FP32 restatement of its kernel,
+all host cores) on a bounded sample of the same workload.
+Multi-GPU (torchrun): each rank reconstructs its own capture (weak scaling, no
+collective on the data path); value = all ranks' samples / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_SCAN, N_BINS, DT, VRES = 256, 1024, 16e-12, (256, 256, 256)
+METRIC = "Backprojected voxel-samples/s"
+UNIT = "voxel-samples/s"
+WORKLOAD = "confocal_bp+log_256x256x1024_to_256^3"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--small", action="store_true", help="64^2 scan, 64^3 volume (plumbing check)")
+    ap.add_argument("--no-extras", action="store_true", help="skip bf16 / reference-CUDA / CPU legs")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ distributed
+
+def dist_setup(backend: str):
+    import torch.distributed as dist
+
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ------------------------------------------------------------------- peaks
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """dram read+write bytes per launch of the gather kernel from the committed
+    ncu summary (profiles/), scaled to the full workload there."""
+    p = ROOT / "profiles" / "confocal_gather_256x256x1024_to_256cube.md"
+    if not p.exists():
+        return None
+    m = re.search(r"traffic_per_launch_bytes:\s*([0-9.eE+]+)", p.read_text())
+    return float(m.group(1)) if m else None
+
+
+# --------------------------------------------------------------- workloads
+
+def make_workload(device, seed: int, small: bool):
+    from fasterbackprojection_gb300 import make_info, scenes
+
+    n, vres = (64, (64, 64, 64)) if small else (N_SCAN, VRES)
+    cap = scenes.confocal_patches_torch(n, N_BINS, DT, seed=seed, device=device)
+    hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 1.5))
+    info = make_info(num_laser_targets=n * n, num_time_bins=N_BINS, time_step=cap.time_step, voxel_res=vres,
+                     hidden_min=hmin, voxel_size=vs)
+    return cap, info
+
+
+def cpu_sample_rate(info, cube_np, lx_np, target_s=10.0, threads=0):
+    """The oracle's FP32 restatement of the reference kernel on the host cores,
+    over a voxel sample sized to about target_s seconds.  Returns
+    (samples/s, description, seconds)."""
+    import numpy as np
+    from oracle import cpu
+
+    V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
+    rng = np.random.default_rng(0)
+    n = 64
+    while True:
+        idx = np.sort(rng.choice(V, size=min(n, V), replace=False)).astype(np.int64)
+        t0 = time.perf_counter()
+        cpu.confocal_voxel_f32_subset(info, cube_np, lx_np, idx, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > target_s / 4 or n >= V:
+            break
+        n = int(min(V, n * max(2.0, min(16.0, (target_s / 4) / max(dt, 1e-3)))))
+    pairs = idx.shape[0] * info.num_laser_targets
+    return pairs / dt, f"{idx.shape[0]} random voxels x {info.num_laser_targets} scan points", dt
+
+
+# ------------------------------------------------------------- our arm
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from fasterbackprojection_gb300 import FBP_FILTER_LOG, Context
+
+    ws, rank, local = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cap, info = make_workload(dev, 2 + rank, args.small)
+    L = info.num_laser_targets
+    V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
+    samples = V * L
+    ctx = Context(local)
+    cube = cap.cube.contiguous()
+    lx = cap.laser_xyz.contiguous()
+    vol = torch.empty((VRES[2], VRES[1], VRES[0]) if not args.small else (64, 64, 64), device=dev)
+    vol2 = torch.empty_like(vol)
+    stream = torch.cuda.current_stream()
+
+    def step(c):
+        ctx.backproject_confocal(info, c, lx, out=vol)
+        ctx.postfilter(FBP_FILTER_LOG, vol, 5, 1.0, out=vol2)
+        ctx.normalize_(vol2)
+
+    for _ in range(args.warmup):
+        step(cube)
+    torch.cuda.synchronize()
+    ctx.check_device_status()
+
+    # Timed region: K full steps, plus per-launch events around the gather.
+    bp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = ctx.launches
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            bp_ev[k][0].record(stream)
+            ctx.backproject_confocal(info, cube, lx, out=vol)
+            bp_ev[k][1].record(stream)
+            ctx.postfilter(FBP_FILTER_LOG, vol, 5, 1.0, out=vol2)
+            ctx.normalize_(vol2)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    launches = ctx.launches - launches0
+    ms_total = t_start.elapsed_time(t_end)
+    ms_total = max_over_ranks(ms_total, ws, dev)
+    ms_step = ms_total / args.steps
+    bp_ms = statistics.mean(a.elapsed_time(b) for a, b in bp_ev)
+    value = ws * samples * args.steps / (ms_total / 1e3)
+    ctx.check_device_status()
+
+    # End to end through the C ABI from pinned host buffers.
+    host_cube = torch.empty(cube.shape, dtype=cube.dtype, pin_memory=True)
+    host_cube.copy_(cube)
+    host_lx = torch.empty(lx.shape, dtype=lx.dtype, pin_memory=True)
+    host_lx.copy_(lx)
+    host_vol = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True)
+    hc, hl, hv = host_cube.numpy(), host_lx.numpy(), host_vol.numpy()
+
+    def e2e_step():
+        ctx.reconstruct_shape_host(info, hc, hl, use_fourier_filter=False, postfilter=FBP_FILTER_LOG, kernel_size=5,
+                                   sigma=1.0, normalize=True, out=hv)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws, dev)
+    e2e_value = ws * samples * args.steps / e2e_s
+    # e2e parity with the device path (same kernels, same inputs).
+    e2e_matches = bool(torch.equal(host_vol.to(dev), vol2))
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # BF16 storage of the same capture.
+        cube16 = cube.to(torch.bfloat16)
+        for _ in range(2):
+            ctx.backproject_confocal(info, cube16, lx, out=vol)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.backproject_confocal(info, cube16, lx, out=vol)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bf_ms = e0.elapsed_time(e1) / args.steps
+        extras["bf16_storage"] = {"bp_ms": round(bf_ms, 3), "value": samples / (bf_ms / 1e3),
+                                  "achieved_gbs_2B_per_sample": samples * 2 / (bf_ms / 1e3) / 1e9}
+        del cube16
+        extras["reference_cuda"] = reference_cuda_rate(info, cube, lx, dev)
+
+    peak, peak_kind = measured_peaks()
+    achieved = samples * 4 / (bp_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded 8-patch scene, Poisson noise), generated on device",
+        "config": {"workload": WORKLOAD if not args.small else "small_64^2x1024_to_64^3",
+                   "scan": [int(round(L ** 0.5))] * 2, "bins": N_BINS, "bin_ps": 16,
+                   "volume": list(info.voxel_res), "storage": "f32", "postfilter": "LoG k=5 sigma=1",
+                   "l2": "inputs larger than L2 (cube 256 MiB)", "per_gpu": "one capture per rank"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(hc.nbytes + hl.nbytes),
+                "d2h_bytes_per_step": int(hv.nbytes), "matches_device_path": e2e_matches},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic(), "peak_source": peak_kind,
+                     "note": "achieved = 4 B per voxel-sample / gather launch time; the gather is "
+                             "FP32/MUFU issue-bound, see profiles/"},
+        "bp_ms_per_launch": bp_ms,
+        "gpu_launches": launches,
+    }
+    if not args.no_extras and rank == 0:
+        line["cpu_baseline"] = cpu_baseline(info, cube, lx)
+        line.update(extras)
+    line["clocks"] = clk.summary()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def reference_cuda_rate(info, cube, lx, dev):
+    """The reference's own backprojectConfocalVoxel (compiled from its sources,
+    oracle/_ref) on the same GPU, over the first depth slices of the volume."""
+    import ctypes
+
+    import torch
+
+    try:
+        from oracle import harness
+    except Exception as e:  # pragma: no cover
+        return {"unavailable": f"harness import failed: {e}"}
+    if not harness.available():
+        return {"unavailable": "reference kernels not built (needs the reference sources at build time)"}
+    sub = type(info)()
+    ctypes.memmove(ctypes.byref(sub), ctypes.byref(info), ctypes.sizeof(info))
+    nz = 8
+    sub.voxel_res[2] = nz
+    cube_tm = cube.t().contiguous()
+    harness.confocal_voxel(sub, cube_tm, lx)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    reps = 2
+    for _ in range(reps):
+        harness.confocal_voxel(sub, cube_tm, lx)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    samples = sub.voxel_res[0] * sub.voxel_res[1] * nz * sub.num_laser_targets
+    del cube_tm
+    return {"kernel": "backprojectConfocalVoxel (reference, sm_103a, fast math)", "value": samples / (ms / 1e3),
+            "unit": UNIT, "sample": f"{nz} of {info.voxel_res[2]} depth slices", "ms": ms}
+
+
+def cpu_baseline(info, cube, lx):
+    rate, desc, dt = cpu_sample_rate(info, cube.cpu().numpy(), lx.cpu().numpy(), target_s=12.0)
+    return {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": desc + f" ({dt:.1f} s)"}
+
+
+# ------------------------------------------------------- reference arm
+
+def run_reference(args):
+    ws, rank, local = dist_setup("gloo")
+    if rank != 0:
+        return
+    import torch
+
+    from fasterbackprojection_gb300 import make_info, scenes
+
+    # The capture itself comes from the same generator; it needs a device for
+    # the patch scene, otherwise fall back to a point scene of the same shape.
+    if torch.cuda.is_available():
+        cap, info = make_workload(torch.device("cuda", local), 2, args.small)
+        cube = cap.cube.cpu().numpy()
+        lx = cap.laser_xyz.cpu().numpy()
+    else:
+        n = 64 if args.small else N_SCAN
+        capn = scenes.confocal_points(n, N_BINS, DT, n_points=200, seed=2)
+        hmin, vs = scenes.volume_geometry(VRES, depth_range=(0.0, 1.5))
+        info = make_info(num_laser_targets=n * n, num_time_bins=N_BINS, time_step=capn.time_step, voxel_res=VRES,
+                         hidden_min=hmin, voxel_size=vs)
+        cube, lx = capn.cube, capn.laser_xyz
+    rates = []
+    desc = ""
+    for k in range(args.warmup + args.steps):
+        r, desc, dt = cpu_sample_rate(info, cube, lx, target_s=4.0)
+        if k >= args.warmup:
+            rates.append(r)
+    value = statistics.mean(rates)
+    L = info.num_laser_targets
+    V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": V * L / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "volume": list(info.voxel_res), "scan": [int(round(L ** 0.5))] * 2,
+                   "bins": N_BINS},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": desc + " per step; the reference has no CPU backprojection, this is the "
+                                          "oracle's FP32 restatement of backprojectConfocalVoxel"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,131 @@
+"""ctypes binding of libfbp.so (the C ABI declared in include/fbp.h).
+
+The library is loaded from the package's ``_lib/`` directory.  There is no
+fallback: if the shared object is missing the import raises, so a caller
+never silently runs anything but the CUDA path.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_uint32, c_uint64, c_void_p
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfbp.so"
+
+# fbp_status
+FBP_OK = 0
+FBP_ERR_INVALID_ARG = 1
+FBP_ERR_OOM = 2
+FBP_ERR_CUDA = 3
+FBP_ERR_TIMEOUT = 4
+FBP_ERR_UNSUPPORTED = 5
+FBP_ERR_DEVICE = 6
+FBP_ERR_IO = 7
+# fbp_dtype
+FBP_F32, FBP_BF16, FBP_F16 = 0, 1, 2
+# fbp_layout
+FBP_LAYOUT_TIME_MAJOR, FBP_LAYOUT_TIME_INNER = 0, 1
+# fbp_capture_system
+FBP_CONFOCAL, FBP_EXHAUSTIVE = 0, 1
+# fbp_filter
+FBP_FILTER_NONE, FBP_FILTER_LAPLACIAN, FBP_FILTER_LOG, FBP_FILTER_LOG_FFT = 0, 1, 2, 3
+# fbp_border
+FBP_BORDER_ZERO, FBP_BORDER_EDGE = 0, 1
+
+_F3 = c_float * 3
+_U3 = c_uint32 * 3
+
+
+class ReconInfo(ctypes.Structure):
+    """fbp_recon_info: the reference's ReconstructionInfo layout (148 bytes)."""
+
+    _fields_ = [
+        ("sensor_position", _F3),
+        ("capture_system", c_uint32),
+        ("laser_position", _F3),
+        ("time_offset", c_float),
+        ("num_laser_targets", c_uint32),
+        ("num_sensor_targets", c_uint32),
+        ("num_time_bins", c_uint32),
+        ("time_step", c_float),
+        ("hidden_min", _F3),
+        ("discard_first_last_bounces", c_uint32),
+        ("hidden_max", _F3),
+        ("hidden_size", _F3),
+        ("voxel_size", _F3),
+        ("wall_min", _F3),
+        ("wall_size", _F3),
+        ("wall_normal", _F3),
+        ("voxel_res", _U3),
+    ]
+
+
+assert ctypes.sizeof(ReconInfo) == 148
+
+
+class ShapeParams(ctypes.Structure):
+    _fields_ = [
+        ("use_fourier_filter", c_int),
+        ("postfilter", c_int),
+        ("kernel_size", c_int),
+        ("sigma", c_float),
+        ("normalize", c_int),
+    ]
+
+
+# (name, restype, argtypes) for every symbol include/fbp.h declares.
+SIGNATURES = {
+    "fbp_version": (c_char_p, []),
+    "fbp_last_error": (c_char_p, []),
+    "fbp_create": (c_int, [POINTER(c_void_p), c_int]),
+    "fbp_destroy": (c_int, [c_void_p]),
+    "fbp_check_device_status": (c_int, [c_void_p, c_void_p]),
+    "fbp_kernel_launch_count": (c_uint64, [c_void_p]),
+    "fbp_backproject_confocal": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_void_p,
+                                         c_void_p]),
+    "fbp_backproject_exhaustive": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_void_p, c_void_p,
+                                           c_void_p, c_void_p]),
+    "fbp_backproject_depths": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_void_p,
+                                       c_void_p, c_uint32, c_void_p, c_void_p]),
+    "fbp_debug_confocal_bins": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_void_p, c_uint64, c_void_p,
+                                        c_void_p]),
+    "fbp_debug_exhaustive_bins": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_void_p, c_void_p, c_uint64,
+                                          c_void_p, c_void_p]),
+    "fbp_linear_space": (c_int, [c_double, c_double, c_int, POINTER(c_double)]),
+    "fbp_postfilter": (c_int, [c_void_p, c_int, c_int, c_float, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32,
+                               c_void_p]),
+    "fbp_log_weights": (c_int, [c_int, c_float, POINTER(c_float)]),
+    "fbp_normalize_minmax": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p]),
+    "fbp_filter_h": (c_int, [c_void_p, c_void_p, c_uint64, c_uint32, c_float, c_float, c_float, c_int, c_void_p]),
+    "fbp_reconstruct_shape_host": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_void_p, c_void_p,
+                                           POINTER(ShapeParams), c_void_p, c_void_p]),
+}
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load libfbp.so once and attach the signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"libfbp.so not built ({LIB_PATH}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class FbpError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"fbp status {status}: {msg}")
+        self.status = status
+
+
+def check(status: int) -> None:
+    if status != FBP_OK:
+        raise FbpError(status, load().fbp_last_error().decode())

@@ -1,0 +1,226 @@
+"""Python-side handle on libfbp: a context plus one method per C entry point.
+
+Device arguments are CUDA torch tensors (contiguous); the calls run on the
+current torch stream unless one is given.  Every method raises FbpError on a
+non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_double, c_float, c_void_p
+
+import numpy as np
+
+from . import _lib
+from ._lib import ReconInfo, ShapeParams, check, load
+
+
+def make_info(*, num_laser_targets: int, num_time_bins: int, time_step: float, voxel_res, hidden_min, voxel_size,
+              num_sensor_targets: int | None = None, capture_system: int = _lib.FBP_CONFOCAL,
+              time_offset: float = 0.0, discard_first_last_bounces: int = 1, laser_position=(0.0, 0.0, 0.0),
+              sensor_position=(0.0, 0.0, 0.0), wall_normal=(0.0, -1.0, 0.0), wall_min=(-1.0, 0.0, -1.0),
+              wall_size=(2.0, 0.0, 2.0)) -> ReconInfo:
+    """Build an fbp_recon_info.  voxel_res is (Vx, Vy, Vz) of a [Vz][Vy][Vx]
+    volume; voxel (vx, vy, vz) sits at hidden_min + (vx, vz, vy)*voxel_size + voxel_size/2."""
+    info = ReconInfo()
+    info.capture_system = capture_system
+    info.num_laser_targets = num_laser_targets
+    info.num_sensor_targets = num_sensor_targets if num_sensor_targets is not None else num_laser_targets
+    info.num_time_bins = num_time_bins
+    info.time_step = time_step
+    info.time_offset = time_offset
+    info.discard_first_last_bounces = discard_first_last_bounces
+    for k in range(3):
+        info.laser_position[k] = laser_position[k]
+        info.sensor_position[k] = sensor_position[k]
+        info.hidden_min[k] = hidden_min[k]
+        info.voxel_size[k] = voxel_size[k]
+        info.voxel_res[k] = voxel_res[k]
+        info.wall_normal[k] = wall_normal[k]
+        info.wall_min[k] = wall_min[k]
+        info.wall_size[k] = wall_size[k]
+    # The reference derives voxel_size = size / res (NLosData.cpp:157), with
+    # size = max - min; keep those fields consistent for callers reading them.
+    for k in range(3):
+        size = float(info.voxel_size[k]) * float(voxel_res[k])
+        info.hidden_size[k] = size
+        info.hidden_max[k] = float(info.hidden_min[k]) + size
+    return info
+
+
+def _dtype_code(t) -> int:
+    import torch
+
+    if t.dtype == torch.float32:
+        return _lib.FBP_F32
+    if t.dtype == torch.bfloat16:
+        return _lib.FBP_BF16
+    if t.dtype == torch.float16:
+        return _lib.FBP_F16
+    raise TypeError(f"unsupported cube dtype {t.dtype}")
+
+
+def _np_dtype_code(a: np.ndarray) -> int:
+    if a.dtype == np.float32:
+        return _lib.FBP_F32
+    if a.dtype == np.float16:
+        return _lib.FBP_F16
+    if a.dtype == np.uint16:  # raw bfloat16 bits
+        return _lib.FBP_BF16
+    raise TypeError(f"unsupported host cube dtype {a.dtype} (float32, float16, or uint16 bfloat16 bits)")
+
+
+def _ptr(t) -> c_void_p:
+    if t is None:
+        return c_void_p(0)
+    if not t.is_contiguous():
+        raise ValueError("tensor must be contiguous")
+    return c_void_p(t.data_ptr())
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = c_void_p()
+        check(self._lib.fbp_create(byref(h), device))
+        self._h = h
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.fbp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def _stream(stream) -> c_void_p:
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream()
+        return c_void_p(s.cuda_stream)
+
+    @property
+    def launches(self) -> int:
+        return int(self._lib.fbp_kernel_launch_count(self._h))
+
+    def check_device_status(self, stream=None) -> None:
+        check(self._lib.fbp_check_device_status(self._h, self._stream(stream)))
+
+    # ---------------------------------------------------------- backprojection
+    def backproject_confocal(self, info: ReconInfo, cube, laser_xyz, out=None, layout=_lib.FBP_LAYOUT_TIME_INNER,
+                             stream=None):
+        import torch
+
+        vx, vy, vz = info.voxel_res
+        if out is None:
+            out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
+        check(self._lib.fbp_backproject_confocal(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
+                                                 _ptr(laser_xyz), _ptr(out), self._stream(stream)))
+        return out
+
+    def backproject_exhaustive(self, info: ReconInfo, cube, laser_xyz, sensor_xyz, out=None, stream=None):
+        import torch
+
+        vx, vy, vz = info.voxel_res
+        if out is None:
+            out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
+        check(self._lib.fbp_backproject_exhaustive(self._h, byref(info), _ptr(cube), _dtype_code(cube),
+                                                   _ptr(laser_xyz), _ptr(sensor_xyz), _ptr(out),
+                                                   self._stream(stream)))
+        return out
+
+    def backproject_depths(self, info: ReconInfo, cube, laser_xyz, depths, sensor_xyz=None, out=None,
+                           layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
+        import torch
+
+        L = info.num_laser_targets
+        D = int(depths.numel())
+        if out is None:
+            out = torch.empty((L, D), dtype=torch.float32, device=cube.device)
+        check(self._lib.fbp_backproject_depths(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
+                                               _ptr(laser_xyz), _ptr(sensor_xyz), _ptr(depths), D, _ptr(out),
+                                               self._stream(stream)))
+        return out
+
+    def debug_confocal_bins(self, info: ReconInfo, laser_xyz, voxel_idx, stream=None):
+        import torch
+
+        out = torch.empty((voxel_idx.numel(), info.num_laser_targets), dtype=torch.int32, device=laser_xyz.device)
+        check(self._lib.fbp_debug_confocal_bins(self._h, byref(info), _ptr(laser_xyz), _ptr(voxel_idx),
+                                                voxel_idx.numel(), _ptr(out), self._stream(stream)))
+        return out
+
+    def debug_exhaustive_bins(self, info: ReconInfo, laser_xyz, sensor_xyz, voxel_idx, stream=None):
+        import torch
+
+        out = torch.empty((voxel_idx.numel(), info.num_laser_targets, info.num_sensor_targets), dtype=torch.int32,
+                          device=laser_xyz.device)
+        check(self._lib.fbp_debug_exhaustive_bins(self._h, byref(info), _ptr(laser_xyz), _ptr(sensor_xyz),
+                                                  _ptr(voxel_idx), voxel_idx.numel(), _ptr(out),
+                                                  self._stream(stream)))
+        return out
+
+    # --------------------------------------------------------- post-processing
+    def postfilter(self, kind: int, vol, kernel_size: int = 5, sigma: float = 1.0, out=None, stream=None):
+        import torch
+
+        vz, vy, vx = vol.shape
+        if out is None:
+            out = torch.empty_like(vol)
+        check(self._lib.fbp_postfilter(self._h, kind, kernel_size, sigma, _ptr(vol), _ptr(out), vx, vy, vz,
+                                       self._stream(stream)))
+        return out
+
+    def normalize_(self, v, stream=None):
+        check(self._lib.fbp_normalize_minmax(self._h, _ptr(v), v.numel(), self._stream(stream)))
+        return v
+
+    def filter_h_(self, data, delta_t: float, wl_mean: float | None = None, wl_sigma: float = 0.0,
+                  border: int = _lib.FBP_BORDER_ZERO, stream=None):
+        """In-place temporal filter of data[num_series, T] (float32)."""
+        n, T = data.shape[0] if data.dim() > 1 else 1, data.shape[-1]
+        n = data.numel() // T
+        wl = delta_t * 10.0 if wl_mean is None else wl_mean
+        check(self._lib.fbp_filter_h(self._h, _ptr(data), n, T, delta_t, wl, wl_sigma, border, self._stream(stream)))
+        return data
+
+    # ------------------------------------------------------------- end to end
+    def reconstruct_shape_host(self, info: ReconInfo, cube: np.ndarray, laser_xyz: np.ndarray,
+                               sensor_xyz: np.ndarray | None = None, use_fourier_filter: bool = True,
+                               postfilter: int = _lib.FBP_FILTER_NONE, kernel_size: int = 5, sigma: float = 1.0,
+                               normalize: bool = True, out: np.ndarray | None = None, stream=None) -> np.ndarray:
+        vx, vy, vz = info.voxel_res
+        if out is None:
+            out = np.empty((vz, vy, vx), dtype=np.float32)
+        params = ShapeParams(int(use_fourier_filter), postfilter, kernel_size, sigma, int(normalize))
+        cube = np.ascontiguousarray(cube)
+        laser_xyz = np.ascontiguousarray(laser_xyz, dtype=np.float32)
+        sens = None if sensor_xyz is None else np.ascontiguousarray(sensor_xyz, dtype=np.float32)
+        check(self._lib.fbp_reconstruct_shape_host(
+            self._h, byref(info), c_void_p(cube.ctypes.data), _np_dtype_code(cube), c_void_p(laser_xyz.ctypes.data),
+            c_void_p(0 if sens is None else sens.ctypes.data), byref(params), c_void_p(out.ctypes.data),
+            self._stream(stream)))
+        return out
+
+
+def log_weights(size: int, sigma: float) -> np.ndarray:
+    w = np.empty(size ** 3, dtype=np.float32)
+    check(load().fbp_log_weights(size, sigma, w.ctypes.data_as(ctypes.POINTER(c_float))))
+    return w
+
+
+def linear_space(lo: float, hi: float, n: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.float64)
+    check(load().fbp_linear_space(lo, hi, n, out.ctypes.data_as(ctypes.POINTER(c_double))))
+    return out

@@ -1,0 +1,344 @@
+// Exhaustive (laser x SPAD) backprojection as a voxel-tiled gather.
+//
+// Replaces Laser::reconstructAABBExhaustive (Laser.cu:500-516) and
+// backprojectExhaustiveVoxel (transient_reconstruction.cuh:138-166).  Same
+// structure as the confocal gather: one CTA per voxel tile, the (laser, SPAD)
+// pairs walked in staged chunks, each pair's reachable time-bin window copied
+// to shared memory.  The pair index splits as l = ls / S, s = ls % S; the
+// reference splits by L (transient_reconstruction.cuh:147-148), which is the
+// same only when L == S and reads past the laser table otherwise.
+// Within a chunk, consecutive pairs usually share the laser point, so the
+// laser-to-voxel distance is computed once per laser point and reused.
+#include "fbp_internal.cuh"
+#include "bp_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace fbp {
+
+struct ExhaustiveGatherParams {
+    const float4* lscan;  // [L] (x, y, z, |l - laserPos| or 0)
+    const float4* sscan;  // [S] (x, y, z, |s - sensorPos| or 0)
+    const float* xs;
+    const float* ys;
+    const float* zs;
+    float* volume;
+    int* status;
+    const void* rows;  // [L*S][row_pitch]
+    uint32_t Vx, Vy, Vz, L, S, T;
+    float t0, dt;
+    uint32_t row_pitch, slot_w;
+
+    __host__ __device__ static constexpr size_t meta_bytes(int ch) {
+        return ((size_t)2 * ch * (2 * sizeof(float4) + sizeof(float) + 3 * sizeof(int)) + 2 * sizeof(int) + 15) &
+               ~size_t(15);
+    }
+};
+
+template <typename S, int KV, int WY, int WZ, int CH, bool BOUNCE, bool EXACT_TRUNC>
+__global__ void __launch_bounds__(32 * WY * WZ)
+exhaustive_gather_kernel(ExhaustiveGatherParams p) {
+    constexpr int NT = 32 * WY * WZ;
+    constexpr int ALIGN = 16 / sizeof(S);
+    constexpr int TY = 8 * WY, TZ = 4 * WZ;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const uint32_t slot_stride = p.slot_w + ALIGN;
+    float4* s_lg = reinterpret_cast<float4*>(smem_raw);  // [2][CH]
+    float4* s_sg = s_lg + 2 * CH;                        // [2][CH]
+    float* s_cl = reinterpret_cast<float*>(s_sg + 2 * CH);
+    int* s_cnt = reinterpret_cast<int*>(s_cl + 2 * CH);
+    int* s_src = s_cnt + 2 * CH;
+    int* s_lid = s_src + 2 * CH;
+    int* s_flag = s_lid + 2 * CH;
+    S* s_slots = reinterpret_cast<S*>(smem_raw + ExhaustiveGatherParams::meta_bytes(CH));
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int wy = warp % WY, wz = warp / WY;
+    const uint32_t tx0 = blockIdx.x * KV, ty0 = blockIdx.y * TY, tz0 = blockIdx.z * TZ;
+    const uint32_t vy = ty0 + wy * 8 + (lane & 7);
+    const uint32_t vz = tz0 + wz * 4 + (lane >> 3);
+    const bool row_ok = vy < p.Vy && vz < p.Vz;
+
+    const uint32_t tx1 = min(tx0 + KV, p.Vx) - 1, ty1 = min(ty0 + TY, p.Vy) - 1, tz1 = min(tz0 + TZ, p.Vz) - 1;
+    const float bx0 = fminf(p.xs[tx0], p.xs[tx1]), bx1 = fmaxf(p.xs[tx0], p.xs[tx1]);
+    const float by0 = fminf(p.ys[tz0], p.ys[tz1]), by1 = fmaxf(p.ys[tz0], p.ys[tz1]);
+    const float bz0 = fminf(p.zs[ty0], p.zs[ty1]), bz1 = fmaxf(p.zs[ty0], p.zs[ty1]);
+
+    const float py = p.ys[min(vz, p.Vz - 1)];
+    const float pz = p.zs[min(vy, p.Vy - 1)];
+    float px[KV];
+#pragma unroll
+    for (int k = 0; k < KV; ++k) px[k] = p.xs[min(tx0 + k, p.Vx - 1)];
+
+    const float rcp_dt = rcp_approx(p.dt);
+    const uint64_t npairs = (uint64_t)p.L * p.S;
+    const uint64_t nchunks = (npairs + CH - 1) / CH;
+
+    for (int i = tid; i < 2 * CH * ALIGN; i += NT) {
+        const int slot = i / ALIGN, e = i % ALIGN;
+        s_slots[(size_t)slot * slot_stride + p.slot_w + e] = from_f32<S>(0.f);
+    }
+
+    auto box_range = [&](const float4& g, float& dmin, float& dmax) {
+        const float cx = fminf(fmaxf(g.x, bx0), bx1), cy = fminf(fmaxf(g.y, by0), by1), cz = fminf(fmaxf(g.z, bz0), bz1);
+        dmin = sqrtf((g.x - cx) * (g.x - cx) + (g.y - cy) * (g.y - cy) + (g.z - cz) * (g.z - cz));
+        const float fx = fmaxf(fabsf(g.x - bx0), fabsf(g.x - bx1)), fy = fmaxf(fabsf(g.y - by0), fabsf(g.y - by1)),
+                    fz = fmaxf(fabsf(g.z - bz0), fabsf(g.z - bz1));
+        dmax = sqrtf(fx * fx + fy * fy + fz * fz);
+    };
+
+    auto plan_chunk = [&](uint64_t c, int buf) {
+        if (tid < CH) {
+            const uint64_t ls = c * CH + tid;
+            float4 lg = make_float4(0.f, 0.f, 0.f, 0.f), sg = lg;
+            float cl = 0.f;
+            int cnt = 0, src = 0, near = 0, lid = -1;
+            if (ls < npairs) {
+                const uint32_t l = (uint32_t)(ls / p.S), s = (uint32_t)(ls % p.S);
+                lg = p.lscan[l];
+                sg = p.sscan[s];
+                lid = (int)l;
+                float dl0, dl1, ds0, ds1;
+                box_range(lg, dl0, dl1);
+                box_range(sg, ds0, ds1);
+                const float bnc = BOUNCE ? lg.w + sg.w : 0.f;
+                const float pmin = dl0 + ds0 - p.t0 + bnc, pmax = dl1 + ds1 - p.t0 + bnc;
+                near = pmin < 0.0035f;
+                int blo = (int)fmaxf(fminf(floorf(pmin * rcp_dt), 1.0e9f), -1.0e9f) - 2;
+                int bhi = (int)fmaxf(fminf(floorf(pmax * rcp_dt), 1.0e9f), -1.0e9f) + 2;
+                int a = max(blo, 0) & ~(ALIGN - 1);
+                a = min(a, (int)(p.row_pitch - p.slot_w));
+                const int hi = min(bhi + 1, (int)p.row_pitch);
+                cnt = hi - a;
+                if (cnt < 0) cnt = 0;
+                cnt = (cnt + ALIGN - 1) & ~(ALIGN - 1);
+                if (cnt > (int)p.slot_w) {
+                    atomicExch(p.status, (int)FBP_ERR_DEVICE);
+                    cnt = (int)p.slot_w;
+                }
+                src = a;
+                cl = EXACT_TRUNC ? __int_as_float(a) : (float)(8388608 - a);
+            }
+            s_lg[buf * CH + tid] = lg;
+            s_sg[buf * CH + tid] = sg;
+            s_cl[buf * CH + tid] = cl;
+            s_cnt[buf * CH + tid] = cnt;
+            s_src[buf * CH + tid] = src;
+            s_lid[buf * CH + tid] = lid;
+            const unsigned any_near = __ballot_sync(CH >= 32 ? 0xffffffffu : ((1u << CH) - 1u), near);
+            if (tid == 0) s_flag[buf] = any_near != 0;
+        }
+    };
+
+    auto copy_chunk = [&](uint64_t c, int buf) {
+        const uint32_t vecs = p.slot_w / ALIGN;
+        for (uint32_t i = tid; i < CH * vecs; i += NT) {
+            const uint32_t s = i / vecs, j = i - s * vecs;
+            if ((int)(j * ALIGN) < s_cnt[buf * CH + s]) {
+                const uint64_t ls = c * CH + s;
+                const S* src = static_cast<const S*>(p.rows) + ls * p.row_pitch + s_src[buf * CH + s] + j * ALIGN;
+                cp_async_16(s_slots + (size_t)(buf * CH + s) * slot_stride + j * ALIGN, src);
+            }
+        }
+        cp_async_commit();
+    };
+
+    float acc[KV], ksum[KV], kcomp[KV], dl[KV];
+#pragma unroll
+    for (int k = 0; k < KV; ++k) acc[k] = ksum[k] = kcomp[k] = dl[k] = 0.f;
+    int cur_l = -1;
+
+    if (nchunks > 0) {
+        plan_chunk(0, 0);
+        __syncthreads();
+        copy_chunk(0, 0);
+    }
+    for (uint64_t c = 0; c < nchunks; ++c) {
+        const int buf = (int)(c & 1);
+        __syncthreads();  // every thread is done with chunk c-1, whose buffer plan(c+1) reuses
+        if (c + 1 < nchunks) plan_chunk(c + 1, buf ^ 1);
+        __syncthreads();  // plan(c+1) visible to the copy loop
+        if (c + 1 < nchunks) {
+            copy_chunk(c + 1, buf ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+
+        const bool safe = s_flag[buf] != 0;
+        const int np = (int)min((uint64_t)CH, npairs - c * CH);
+        for (int i = 0; i < np; ++i) {
+            const float4 lg = s_lg[buf * CH + i];
+            const float4 sg = s_sg[buf * CH + i];
+            const float cl = s_cl[buf * CH + i];
+            const int lid = s_lid[buf * CH + i];
+            const S* slot = s_slots + (size_t)(buf * CH + i) * slot_stride;
+            if (lid != cur_l) {  // uniform across the CTA
+                cur_l = lid;
+                const float ldy = sub_rn(py, lg.y), ldz = sub_rn(pz, lg.z);
+                const float ldy2 = mul_rn(ldy, ldy);
+#pragma unroll
+                for (int k = 0; k < KV; ++k) {
+                    const float dx = sub_rn(px[k], lg.x);
+                    dl[k] = sqrt_approx(fma_rn(ldz, ldz, fma_rn(dx, dx, ldy2)));
+                }
+            }
+            const float sdy = sub_rn(py, sg.y), sdz = sub_rn(pz, sg.z);
+            const float sdy2 = mul_rn(sdy, sdy);
+            const float bnc = BOUNCE ? add_rn(lg.w, sg.w) : 0.f;
+#pragma unroll
+            for (int k = 0; k < KV; ++k) {
+                const float dx = sub_rn(px[k], sg.x);
+                const float ds = sqrt_approx(fma_rn(sdz, sdz, fma_rn(dx, dx, sdy2)));
+                // transient_reconstruction.cuh:155-157
+                float dist = sub_rn(add_rn(dl[k], ds), p.t0);
+                if (BOUNCE) dist = add_rn(dist, bnc);
+                const float x = ref_bin_ratio(dist, rcp_dt);
+                uint32_t idx;
+                if (EXACT_TRUNC) {
+                    idx = min((uint32_t)(__float2int_rz(x) - __float_as_int(cl)), p.slot_w);
+                } else {
+                    idx = min(__float_as_uint(add_rz(x, cl)) - 0x4B000000u, p.slot_w);
+                }
+                const float I = to_f32(slot[idx]);
+                const float dd = mul_rn(dist, dist);
+                const float w = safe ? ref_safe_rcp(dd) : rcp_approx(dd);
+                acc[k] = fmaf(I, w, acc[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+            const float y = sub_rn(acc[k], kcomp[k]);
+            const float t = add_rn(ksum[k], y);
+            kcomp[k] = sub_rn(sub_rn(t, ksum[k]), y);
+            ksum[k] = t;
+            acc[k] = 0.f;
+        }
+    }
+
+    if (row_ok) {
+        float* out = p.volume + ((size_t)vz * p.Vy + vy) * p.Vx + tx0;
+#pragma unroll
+        for (int k = 0; k < KV; ++k)
+            if (tx0 + k < p.Vx) out[k] = ksum[k];
+    }
+}
+
+namespace {
+
+constexpr int kKV = 8, kWY = 2, kWZ = 4, kCH = 32;
+
+template <typename S>
+__global__ void pair_rows_kernel(S* __restrict__ rows, const S* __restrict__ cube, uint64_t npairs, uint32_t T,
+                                 uint32_t pitch) {
+    const uint64_t n = npairs * pitch;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = i / pitch;
+        const uint32_t t = (uint32_t)(i % pitch);
+        S v = from_f32<S>(0.f);
+        if (t < T) {
+            const S c = cube[r * T + t];
+            if (to_f32(c) > FBP_EPS) v = c;
+        }
+        rows[i] = v;
+    }
+}
+
+template <typename S>
+fbp_status launch_exhaustive(fbp_context* ctx, const fbp_recon_info& in, const void* cube, const float* laser_xyz,
+                             const float* sensor_xyz, float* volume, cudaStream_t stream) {
+    const uint32_t L = in.num_laser_targets, Sn = in.num_sensor_targets, T = in.num_time_bins;
+    const uint32_t Vx = in.voxel_res[0], Vy = in.voxel_res[1], Vz = in.voxel_res[2];
+    constexpr int ALIGN = 16 / sizeof(S);
+    const double ex = (double)kKV * std::fabs(in.voxel_size[0]);
+    const double ey = (double)(4 * kWZ) * std::fabs(in.voxel_size[1]);
+    const double ez = (double)(8 * kWY) * std::fabs(in.voxel_size[2]);
+    const double diag = std::sqrt(ex * ex + ey * ey + ez * ez);
+    const double span = 2.0 * diag / std::fabs((double)in.time_step) + 8.0 + ALIGN;
+    if (!(span < 65536.0)) return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_exhaustive: voxel tile spans too many bins");
+    const uint32_t slot_w = ((uint32_t)std::ceil(span) + ALIGN - 1) / ALIGN * ALIGN;
+    const uint32_t pitch = (T + slot_w + ALIGN - 1) / ALIGN * ALIGN;
+    const uint64_t npairs = (uint64_t)L * Sn;
+
+    void* rows = nullptr;
+    FBP_TRY(workspace(ctx, WS_CUBE_ROWS, npairs * pitch * sizeof(S), stream, &rows));
+    {
+        const uint64_t n = npairs * pitch;
+        const unsigned blocks = (unsigned)std::min<uint64_t>(cdiv(n, 256), (uint64_t)ctx->sm_count * 16);
+        pair_rows_kernel<S><<<blocks, 256, 0, stream>>>(static_cast<S*>(rows), static_cast<const S*>(cube), npairs, T,
+                                                        pitch);
+        FBP_CHECK_LAUNCH(ctx, "pair_rows_kernel");
+    }
+
+    ExhaustiveGatherParams p{};
+    const float4* lscan = nullptr;
+    FBP_TRY(build_tables(ctx, in, laser_xyz, stream, &lscan, &p.xs, &p.ys, &p.zs));
+    // build_tables stores |l-laser| + |l-sensor|; the exhaustive kernel needs
+    // |l - laserPos| and |s - sensorPos| separately, so rebuild both tables.
+    void* lp = nullptr;
+    void* sp = nullptr;
+    FBP_TRY(workspace(ctx, WS_SCAN_TABLE, (size_t)L * sizeof(float4), stream, &lp));
+    FBP_TRY(workspace(ctx, WS_SENSOR_TABLE, (size_t)Sn * sizeof(float4), stream, &sp));
+    scan_table_kernel<<<cdiv(L, 256), 256, 0, stream>>>(static_cast<float4*>(lp), laser_xyz, L,
+                                                       (int)in.discard_first_last_bounces, in.laser_position[0],
+                                                       in.laser_position[1], in.laser_position[2], 0.f, 0.f, 0.f, 0);
+    FBP_CHECK_LAUNCH(ctx, "scan_table_kernel");
+    scan_table_kernel<<<cdiv(Sn, 256), 256, 0, stream>>>(static_cast<float4*>(sp), sensor_xyz, Sn,
+                                                        (int)in.discard_first_last_bounces, in.sensor_position[0],
+                                                        in.sensor_position[1], in.sensor_position[2], 0.f, 0.f, 0.f, 0);
+    FBP_CHECK_LAUNCH(ctx, "scan_table_kernel");
+    p.lscan = static_cast<const float4*>(lp);
+    p.sscan = static_cast<const float4*>(sp);
+    p.volume = volume;
+    p.status = ctx->status_dev;
+    p.rows = rows;
+    p.Vx = Vx; p.Vy = Vy; p.Vz = Vz; p.L = L; p.S = Sn; p.T = T;
+    p.t0 = in.time_offset;
+    p.dt = in.time_step;
+    p.row_pitch = pitch;
+    p.slot_w = slot_w;
+
+    const size_t smem = ExhaustiveGatherParams::meta_bytes(kCH) + (size_t)2 * kCH * (slot_w + ALIGN) * sizeof(S);
+    if (smem > (size_t)ctx->smem_optin) return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_exhaustive: window too large");
+    dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(Vz, 4 * kWZ));
+    const bool bounce = in.discard_first_last_bounces == 0;
+    const bool exact = in.time_offset > 0.f;
+    auto go = [&](auto kernel) -> fbp_status {
+        FBP_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kernel<<<grid, 32 * kWY * kWZ, smem, stream>>>(p);
+        FBP_CHECK_LAUNCH(ctx, "exhaustive_gather_kernel");
+        return FBP_OK;
+    };
+    if (bounce) {
+        if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, true, true>);
+        return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, true, false>);
+    }
+    if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, false, true>);
+    return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, false, false>);
+}
+
+}  // namespace
+}  // namespace fbp
+
+using namespace fbp;
+
+extern "C" fbp_status fbp_backproject_exhaustive(fbp_context* ctx, const fbp_recon_info* info, const void* cube,
+                                                 int dtype, const float* laser_xyz, const float* sensor_xyz,
+                                                 float* volume, void* stream) {
+    clear_error();
+    FBP_TRY(check_ctx(ctx));
+    FBP_TRY(validate_info(info, true, "fbp_backproject_exhaustive"));
+    if (!cube || !laser_xyz || !sensor_xyz || !volume)
+        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_exhaustive: null buffer");
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (dtype) {
+        case FBP_F32: return launch_exhaustive<float>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
+        case FBP_BF16: return launch_exhaustive<__nv_bfloat16>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
+        case FBP_F16: return launch_exhaustive<__half>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
+        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_exhaustive: unknown dtype");
+    }
+}

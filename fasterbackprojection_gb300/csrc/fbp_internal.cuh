@@ -1,0 +1,183 @@
+// Internal declarations shared by the libfbp translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+
+#include "../../include/fbp.h"
+
+namespace fbp {
+
+// ---------------------------------------------------------------- errors --
+
+// Records `msg` as this thread's last error and returns `st`.
+fbp_status set_error(fbp_status st, const std::string& msg);
+fbp_status cuda_error(cudaError_t e, const char* what);
+void clear_error();
+
+#define FBP_TRY_CUDA(expr)                                               \
+    do {                                                                 \
+        cudaError_t e_ = (expr);                                         \
+        if (e_ != cudaSuccess) return ::fbp::cuda_error(e_, #expr);      \
+    } while (0)
+
+#define FBP_TRY(expr)                          \
+    do {                                       \
+        fbp_status s_ = (expr);                \
+        if (s_ != FBP_OK) return s_;           \
+    } while (0)
+
+#define FBP_CHECK_LAUNCH(ctx, name)                                      \
+    do {                                                                 \
+        cudaError_t e_ = cudaGetLastError();                             \
+        if (e_ != cudaSuccess) return ::fbp::cuda_error(e_, name);       \
+        (ctx)->launches++;                                               \
+    } while (0)
+
+// --------------------------------------------------------------- context --
+
+// Grow-only device scratch.  Slots are independent so one entry point can hold
+// several buffers at once; growing synchronises the stream first so no
+// in-flight kernel still reads the old allocation.
+enum WorkspaceSlot {
+    WS_CUBE_ROWS = 0,   // padded, thresholded scan-point rows for the gathers
+    WS_SCAN_TABLE,      // per scan point (x, y, z, bounce)
+    WS_SENSOR_TABLE,    // per SPAD point (x, y, z, bounce)
+    WS_AXIS_TABLES,     // voxel-centre coordinates per axis
+    WS_POINTS,          // explicit point sets (depth planes)
+    WS_PARTIALS,        // per-block partial results (reductions)
+    WS_FILTER,          // post-filter / temporal-filter temporaries
+    WS_FFT_A,
+    WS_FFT_B,
+    WS_FFT_C,
+    WS_MISC,
+    WS_HOST_STAGING_IN, // device copies for the host-buffer entry points
+    WS_HOST_STAGING_OUT,
+    WS_HOST_STAGING_AUX,
+    WS_HOST_STAGING_AUX2,
+    WS_NUM_SLOTS
+};
+
+}  // namespace fbp
+
+struct fbp_context {
+    int device = 0;
+    int sm_count = 0;
+    int smem_optin = 0;
+    void* ws[fbp::WS_NUM_SLOTS] = {};
+    size_t ws_bytes[fbp::WS_NUM_SLOTS] = {};
+    int* status_dev = nullptr;  // device status word: 0 ok, else an fbp_status
+    uint64_t launches = 0;
+};
+
+namespace fbp {
+
+fbp_status check_ctx(fbp_context* ctx);
+// Returns a device buffer of at least `bytes` in slot `slot`.
+fbp_status workspace(fbp_context* ctx, int slot, size_t bytes, cudaStream_t stream, void** out);
+
+inline unsigned cdiv(uint64_t a, uint64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// ---------------------------------------------------- element conversion --
+
+template <typename T> __device__ __forceinline__ float to_f32(T v);
+template <> __device__ __forceinline__ float to_f32<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f32<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <> __device__ __forceinline__ float to_f32<__half>(__half v) { return __half2float(v); }
+
+template <typename T> __device__ __forceinline__ T from_f32(float v);
+template <> __device__ __forceinline__ float from_f32<float>(float v) { return v; }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ __half from_f32<__half>(float v) { return __float2half_rn(v); }
+
+inline size_t dtype_size(int dtype) { return dtype == FBP_F32 ? 4 : 2; }
+
+// ---------------------------------------------------- reference arithmetic --
+//
+// The reference kernels are built with fast math and FMA contraction
+// (FasterBackprojection.vcxproj:66, 96).  The time-bin index
+//     int(dist / timeStep),  dist = 2 * distance(l, p) - t0 (+ bounces)
+// must be reproduced bit for bit, so the operations below pin each
+// instruction explicitly instead of leaving the rounding sequence to the
+// compiler: the square root, the division, and the FMA nesting of the dot
+// product.  The sequence was matched black-box against the reference kernels
+// compiled from the reference sources (bitwise-equal volumes on single-scan
+// runs), see tests/test_ref_parity_gpu.py.
+
+#define FBP_EPS 0.00001f  // math.cuh:11
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float div_full(float a, float b) {
+    float r;
+    asm("div.full.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float fma_rn(float a, float b, float c) {
+    float r;
+    asm("fma.rn.ftz.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float mul_rn(float a, float b) {
+    float r;
+    asm("mul.rn.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float add_rn(float a, float b) {
+    float r;
+    asm("add.rn.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float sub_rn(float a, float b) {
+    float r;
+    asm("sub.rn.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+// add with round-toward-zero: used for the float->bin truncation trick.
+__device__ __forceinline__ float add_rz(float a, float b) {
+    float r;
+    asm("add.rz.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+// |d|^2 of the difference vector with the reference's rounding sequence:
+// the y product is rounded first, then x and z are fused in.
+__device__ __forceinline__ float ref_dot3(float dx, float dy, float dz) {
+    return fma_rn(dz, dz, fma_rn(dx, dx, mul_rn(dy, dy)));
+}
+
+// distance(a, b) as compiled in the reference.
+__device__ __forceinline__ float ref_distance(float ax, float ay, float az, float bx, float by, float bz) {
+    return sqrt_approx(ref_dot3(sub_rn(bx, ax), sub_rn(by, ay), sub_rn(bz, az)));
+}
+
+// One coordinate of a voxel centre: min + i * size + 0.5 * size
+// (transient_reconstruction.cuh:106, contracted into two FMAs).
+__device__ __forceinline__ float ref_voxel_coord(uint32_t i, float size, float mn) {
+    return fma_rn(0.5f, size, fma_rn((float)i, size, mn));
+}
+
+// x = dist / timeStep as the reference's fast-math division computes it: the
+// division equals dist * rcp.approx(timeStep), so the reciprocal is hoisted
+// and passed in precomputed (rcp_dt = rcp_approx(timeStep)).
+__device__ __forceinline__ float ref_bin_ratio(float dist, float rcp_dt) { return mul_rn(dist, rcp_dt); }
+
+// safeRCP(x) (math.cuh:23-29) with the fast-math reciprocal.
+__device__ __forceinline__ float ref_safe_rcp(float x) {
+    if (x > FBP_EPS || x < -FBP_EPS) return rcp_approx(x);
+    return x >= 0.f ? 3.402823466e+38f : -3.402823466e+38f;
+}
+
+}  // namespace fbp

@@ -1,0 +1,199 @@
+/* fbp.h — C ABI of the GB300 reconstruction library (libfbp.so).
+ *
+ * Plain pointers and sizes only.  Every device pointer argument is a CUDA
+ * device address on the context's device; `stream` is a cudaStream_t passed
+ * as void* (NULL = legacy default stream).  Calls are asynchronous on
+ * `stream` unless stated otherwise and never throw: each returns an
+ * fbp_status, and fbp_last_error() gives the message of the last failure on
+ * the calling thread.
+ *
+ * Each entry point names the reference interface it replaces
+ * (paths relative to the reference's FasterBackprojection/ directory).
+ */
+#ifndef FBP_H
+#define FBP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FBP_ABI_VERSION 1
+
+typedef enum {
+    FBP_OK = 0,
+    FBP_ERR_INVALID_ARG = 1, /* null pointer, zero or inconsistent size, unknown enum */
+    FBP_ERR_OOM = 2,         /* device or host allocation failed */
+    FBP_ERR_CUDA = 3,        /* a CUDA runtime call or kernel launch failed */
+    FBP_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (status word set) */
+    FBP_ERR_UNSUPPORTED = 5, /* valid but not implemented for these arguments */
+    FBP_ERR_DEVICE = 6,      /* a kernel reported an internal check failure */
+    FBP_ERR_IO = 7           /* file could not be read or written */
+} fbp_status;
+
+/* Storage type of a transient cube. */
+typedef enum { FBP_F32 = 0, FBP_BF16 = 1, FBP_F16 = 2 } fbp_dtype;
+
+/* Order of a confocal cube with L scan points and T bins.
+ *   FBP_LAYOUT_TIME_MAJOR: cube[t*L + l] — what the reference kernels index
+ *                          (transient_utils.cuh:6-9).
+ *   FBP_LAYOUT_TIME_INNER: cube[l*T + t] — the order NLosData stores
+ *                          (NLosData.cpp:241, 264) and filter_H works on.
+ * Exhaustive cubes are always cube[(l*S + s)*T + t] (transient_utils.cuh:11-14). */
+typedef enum { FBP_LAYOUT_TIME_MAJOR = 0, FBP_LAYOUT_TIME_INNER = 1 } fbp_layout;
+
+typedef enum { FBP_CONFOCAL = 0, FBP_EXHAUSTIVE = 1 } fbp_capture_system;
+
+/* Reconstruction geometry.  Same field order and packing as the reference's
+ * ReconstructionInfo (GpuStructs.cuh:8-38), 148 bytes.  Distances and
+ * time_step are path lengths in metres (time_step = metres per bin).
+ * Voxel (vx, vy, vz) of a volume indexed [vz][vy][vx] sits at
+ *   hidden_min + (vx, vz, vy) * voxel_size + voxel_size / 2
+ * (transient_reconstruction.cuh:106): the outermost index drives world y. */
+typedef struct {
+    float sensor_position[3];
+    uint32_t capture_system; /* fbp_capture_system */
+    float laser_position[3];
+    float time_offset;
+    uint32_t num_laser_targets;
+    uint32_t num_sensor_targets;
+    uint32_t num_time_bins;
+    float time_step;
+    float hidden_min[3];
+    uint32_t discard_first_last_bounces; /* 0: add |l-laser| + |s-sensor| to each path */
+    float hidden_max[3];
+    float hidden_size[3];
+    float voxel_size[3];
+    float wall_min[3];
+    float wall_size[3];
+    float wall_normal[3];
+    uint32_t voxel_res[3]; /* (Vx, Vy, Vz) */
+} fbp_recon_info;
+
+typedef struct fbp_context fbp_context;
+
+/* ---- library / context ------------------------------------------------- */
+
+const char* fbp_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* fbp_last_error(void);
+
+/* Replaces CudaContext (CudaContext.cpp:6-58) and the reference's global
+ * __constant__ state (GpuStructs.cu:4-16): a context owns per-call geometry
+ * tables and grow-only scratch on one device, so calls are reentrant across
+ * contexts.  One context must not be used from two host threads at once. */
+fbp_status fbp_create(fbp_context** ctx, int device);
+fbp_status fbp_destroy(fbp_context* ctx);
+/* Read and clear the context's device status word (set by bounded waits and
+ * internal checks).  Synchronises `stream`. */
+fbp_status fbp_check_device_status(fbp_context* ctx, void* stream);
+/* Number of kernels this context launched since creation (instrumentation). */
+uint64_t fbp_kernel_launch_count(const fbp_context* ctx);
+
+/* ---- backprojection ------------------------------------------------------ */
+
+/* Confocal voxel backprojection.  Replaces Laser::reconstructAABBConfocal
+ * (Laser.cu:482-498) + backprojectConfocalVoxel (transient_reconstruction.cuh:93-136).
+ * volume[Vx*Vy*vz + vy*Vx + vx] = sum over scan points l of
+ *     I(l, bin) * safeRCP(dist^2)   for I > 1e-5 and 0 <= bin < T,
+ *     dist = 2|l - p| - time_offset (+ bounce terms), bin = int(dist / time_step).
+ * The volume is overwritten (the reference adds into a zeroed buffer).
+ * Bin indices follow the reference's FP32 fast-math expression bit for bit;
+ * sums are FP32 per block of scan points, compensated (Kahan) across blocks,
+ * in a fixed order, so results are reproducible run to run.
+ * cube: L*T elements of `dtype` in `layout`; laser_xyz: L*3 floats. */
+fbp_status fbp_backproject_confocal(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
+                                    int layout, const float* laser_xyz, float* volume, void* stream);
+
+/* Exhaustive (laser x SPAD) voxel backprojection.  Replaces
+ * Laser::reconstructAABBExhaustive (Laser.cu:500-516) + backprojectExhaustiveVoxel
+ * (transient_reconstruction.cuh:138-166), with the pair split l = ls / S,
+ * s = ls % S (the reference splits by L, which equals this only when L == S).
+ * cube: (l*S + s)*T + t; laser_xyz: L*3; sensor_xyz: S*3. */
+fbp_status fbp_backproject_exhaustive(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
+                                      const float* laser_xyz, const float* sensor_xyz, float* volume, void* stream);
+
+/* Depth-plane backprojection (unweighted).  Replaces Laser::reconstructDepthConfocal /
+ * reconstructDepthExhaustive (Laser.cu:379-480) + backprojectConfocal /
+ * backprojectExhaustive (transient_reconstruction.cuh:41-91).
+ * activation[c*D + d] for c < L: test point laser_xyz[c] + wall_normal * float(depths[d]).
+ * `layout` applies to confocal cubes only; sensor_xyz may be NULL for confocal. */
+fbp_status fbp_backproject_depths(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
+                                  int layout, const float* laser_xyz, const float* sensor_xyz,
+                                  const double* depths, uint32_t num_depths, float* activation, void* stream);
+
+/* Laser::linearSpace (Laser.cu:69-78) and the depth set reconstructShapeDepths
+ * uses (Laser.cu:365-377): out[i] = min + i*(max-min)/n.  Host function. */
+fbp_status fbp_linear_space(double min_value, double max_value, int n, double* out);
+
+/* Diagnostic: the time-bin index the backprojection uses for each
+ * (voxel, scan point) pair — bins[i*L + l] for voxel linear index voxel_idx[i]
+ * (confocal), bins[(i*L + l)*S + s] (exhaustive); -1 where the bin is outside
+ * [0, T).  Same FP32 expression as the gathers; used by the parity tests. */
+fbp_status fbp_debug_confocal_bins(fbp_context* ctx, const fbp_recon_info* info, const float* laser_xyz,
+                                   const int64_t* voxel_idx, uint64_t num_voxels, int32_t* bins, void* stream);
+fbp_status fbp_debug_exhaustive_bins(fbp_context* ctx, const fbp_recon_info* info, const float* laser_xyz,
+                                     const float* sensor_xyz, const int64_t* voxel_idx, uint64_t num_voxels,
+                                     int32_t* bins, void* stream);
+
+/* ---- post-processing ------------------------------------------------------ */
+
+typedef enum { FBP_FILTER_NONE = 0, FBP_FILTER_LAPLACIAN = 1, FBP_FILTER_LOG = 2, FBP_FILTER_LOG_FFT = 3 } fbp_filter;
+
+/* PostprocessingFilters::compute (PostprocessingFilters.h:5-39) for
+ * None / Laplacian / LoG / LoGFFT.  in and out are [nz][ny][nx] floats and
+ * must not alias (the reference writes a new buffer and swaps, :29-31).
+ * NONE copies in to out.  LOG_FFT keeps the reference's unnormalised inverse
+ * (scale nx*ny*nz) and requires power-of-two sizes. */
+fbp_status fbp_postfilter(fbp_context* ctx, int kind, int kernel_size, float sigma, const float* in, float* out,
+                          uint32_t nx, uint32_t ny, uint32_t nz, void* stream);
+
+/* The LoG weights the reference builds on the host
+ * (LoG::calculateLaplacianKernel, PostprocessingFilters.cu:102-175). Host function;
+ * w receives size^3 floats. */
+fbp_status fbp_log_weights(int size, float sigma, float* w);
+
+/* Laser::normalizeMatrix (Laser.cu:317-339): v = (v - min) * safeRCP(max - min),
+ * in place, min/max reduced on the device. */
+fbp_status fbp_normalize_minmax(fbp_context* ctx, float* v, uint64_t n, void* stream);
+
+/* ---- temporal filter ------------------------------------------------------ */
+
+typedef enum { FBP_BORDER_ZERO = 0, FBP_BORDER_EDGE = 1 } fbp_border;
+
+/* Laser::filter_H_cuda (Laser.cu:128-240) on device data, in place:
+ * data[i*T + t] for i < num_series.  Band-pass with the complex
+ * Gaussian-windowed wave of mean wavelength wl_mean (same units as
+ * delta_t), sigma = wl_sigma (0 selects wl_mean / sqrt(2)), zero or edge
+ * padding by t6sigma - 1, unnormalised inverse, real part kept — computed
+ * as the equivalent real correlation instead of padded FFTs. */
+fbp_status fbp_filter_h(fbp_context* ctx, float* data, uint64_t num_series, uint32_t num_bins, float delta_t,
+                        float wl_mean, float wl_sigma, int border, void* stream);
+
+/* ---- end to end (host buffers) ---------------------------------------------- */
+
+typedef struct {
+    int use_fourier_filter;   /* TransientParameters::_useFourierFilter (default 1) */
+    int postfilter;           /* fbp_filter (default NONE) */
+    int kernel_size;          /* default 5 */
+    float sigma;              /* default 1 */
+    int normalize;            /* min-max normalise the result (the reference always does) */
+} fbp_shape_params;
+
+/* Laser::reconstructShape for the AABB mode (Laser.cu:40-67, 341-363) from
+ * HOST buffers: optional filter_H on the time-innermost cube, upload,
+ * confocal or exhaustive backprojection, post-filter, min-max normalise,
+ * download into volume_host ([Vz][Vy][Vx] floats).  cube_host is
+ * time-innermost (NLosData::_data order) in `dtype`; for F32 and
+ * use_fourier_filter the filter runs on the device copy, the host cube is not
+ * modified.  Synchronous. */
+fbp_status fbp_reconstruct_shape_host(fbp_context* ctx, const fbp_recon_info* info, const void* cube_host,
+                                      int dtype, const float* laser_xyz_host, const float* sensor_xyz_host,
+                                      const fbp_shape_params* params, float* volume_host, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FBP_H */

@@ -1,0 +1,134 @@
+"""FP64 NumPy restatements of the temporal filter and the LCT pipeline.
+
+TEST INFRASTRUCTURE ONLY — see oracle/__init__.py.
+
+filter_h       Laser::filter_H_cuda + padIntensity (FasterBackprojection/Laser.cu:80-240),
+               the literal padded-FFT computation in float64.
+define_psf     python/lct.py:295-347
+resampling_operator  python/lct.py:350-419, built directly as the pooled M x M
+               matrix instead of the dense M^2 x M intermediate (same values).
+lct            python/lct.py:97-211 steps 1-4 for an already-loaded capture
+               (no downsampling, no z_trim: synthetic input).
+Pinned against the reference's own lct.py functions through the fixtures in
+tests/golden/ (made by tests/golden/make_golden.py).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import scipy.sparse as sp
+
+LIGHT_SPEED = 299792458.0  # math.cuh:10
+
+
+def filter_h_params(nt: int, delta_t: float, wl_mean: float, wl_sigma: float = 0.0):
+    f32 = np.float32
+    wl_sigma = f32(wl_sigma)
+    wl_mean = f32(wl_mean)
+    if abs(float(wl_sigma) - 0.0) < float(np.finfo(np.float32).eps):
+        wl_sigma = f32(wl_mean / f32(math.sqrt(2.0)))
+    r = f32(f32(6) * wl_sigma / f32(delta_t))
+    t6 = int(math.floor(float(r) + 0.5)) if r >= 0 else -int(math.floor(-float(r) + 0.5))
+    if t6 % 2 == 1:
+        t6 += 1
+    nt_pad = nt + 2 * (t6 - 1)
+    return float(wl_sigma), t6, nt_pad
+
+
+def filter_h_kernel(nt_pad: int, delta_t: float, wl_mean: float, wl_sigma: float) -> np.ndarray:
+    """The ifft-shifted complex kernel K (Laser.cu:142-172), float64."""
+    t = np.arange(nt_pad, dtype=np.float64) * delta_t
+    tmax = delta_t * (nt_pad - 1)
+    env = np.exp(-(((t - tmax * 0.5) / wl_sigma) ** 2) * 0.5)
+    phase = 2.0 * np.pi * t / wl_mean
+    K = env * (np.cos(phase) + 1j * np.sin(phase)) / env.sum()
+    shift = nt_pad // 2
+    return K[(np.arange(nt_pad) + shift) % nt_pad]
+
+
+def filter_h(data: np.ndarray, delta_t: float, wl_mean: float | None = None, wl_sigma: float = 0.0,
+             border: str = "zero") -> np.ndarray:
+    """data[..., T] float -> filtered float64, same shape."""
+    data = np.asarray(data)
+    T = data.shape[-1]
+    flat = data.reshape(-1, T).astype(np.float64)
+    wl_mean = delta_t * 10.0 if wl_mean is None else wl_mean
+    sigma, t6, n = filter_h_params(T, delta_t, wl_mean, wl_sigma)
+    K = filter_h_kernel(n, float(np.float32(delta_t)), float(np.float32(wl_mean)), sigma)
+    pad = (n - T) // 2
+    H = np.zeros((flat.shape[0], n), dtype=np.complex128)
+    H[:, pad:pad + T] = flat
+    if border == "edge":
+        H[:, :pad] = flat[:, :1]
+        H[:, pad + T:] = flat[:, -1:]
+    elif border not in ("zero", "constant"):
+        raise ValueError(border)
+    # cuFFT's inverse is unnormalised: n * ifft.
+    out = np.fft.ifft(np.fft.fft(H, axis=1) * np.fft.fft(K)[None, :], axis=1) * n
+    return out[:, pad:pad + T].real.reshape(data.shape)
+
+
+def define_psf(U: int, V: int, slope: float) -> np.ndarray:
+    x = np.linspace(-1, 1, 2 * U)
+    y = np.linspace(-1, 1, 2 * U)
+    z = np.linspace(0, 2, 2 * V)
+    gz, gy, gx = np.meshgrid(z, y, x, indexing="ij")
+    psf = np.abs(((4.0 * slope) ** 2) * (gx ** 2 + gy ** 2) - gz)
+    psf = (psf == np.min(psf, axis=0, keepdims=True)).astype(np.float64)
+    psf = psf / np.sum(psf[:, U - 1, U - 1])
+    psf = psf / np.linalg.norm(psf.ravel())
+    return np.roll(psf, shift=(0, U, U), axis=(0, 1, 2))
+
+
+def resampling_operator(M: int):
+    """(mtx, mtxi) as sparse M x M matrices; mtxi == mtx.T."""
+    K = int(round(math.log2(M)))
+    if 2 ** K != M:
+        raise ValueError("resampling operator needs a power-of-two bin count")
+    i = np.arange(M * M, dtype=np.float64)
+    col = np.clip(np.ceil(np.sqrt(i + 1)) - 1, 0, M - 1).astype(np.int64)
+    val = 1.0 / np.sqrt(i + 1)
+    row = (np.arange(M * M) // M).astype(np.int64)  # pooled 2^K = M rows into one, weight 1/M
+    mtx = sp.coo_matrix((val / M, (row, col)), shape=(M, M)).tocsr()
+    mtx.sum_duplicates()
+    return mtx, mtx.T.tocsr()
+
+
+def radiometric_grid(M: int, N: int, mode: str = "reference") -> np.ndarray:
+    """grid_z of python/lct.py:134-136.  The reference tiles linspace(0, 1, M)
+    with np.tile(col, (1, N, N)).reshape(M, N, N), which gives
+    grid_z[a, b, c] = linspace[(a*N + b) % M]; mode "depth" is the per-depth
+    grid the comment there describes (grid_z[a] = linspace[a])."""
+    lin = np.linspace(0, 1, M)
+    if mode == "reference":
+        a = np.arange(M)[:, None, None]
+        b = np.arange(N)[None, :, None]
+        return np.broadcast_to(lin[(a * N + b) % M], (M, N, N))
+    if mode == "depth":
+        return np.broadcast_to(lin[:, None, None], (M, N, N))
+    raise ValueError(mode)
+
+
+def lct(data_tmajor: np.ndarray, width: float, bin_length: float, snr: float = 0.8, diffuse: bool = True,
+        psf: np.ndarray | None = None, mtx=None, mtxi=None, grid: str = "reference") -> np.ndarray:
+    """Confocal LCT of data[M][N][N] (time-major; python/lct.py:129 order).
+
+    bin_length: path length per bin in metres (c * bin_resolution).
+    Returns vol[M][N][N] float64 (depth, y, x)."""
+    M, N, N2 = data_tmajor.shape
+    assert N == N2
+    range_max = M * bin_length
+    if psf is None:
+        psf = define_psf(N, M, width / range_max)
+    fpsf = np.fft.fftn(psf)
+    invpsf = np.conj(fpsf) / (np.abs(fpsf) ** 2 + 1.0 / snr)
+    if mtx is None:
+        mtx, mtxi = resampling_operator(M)
+    grid_z = radiometric_grid(M, N, grid)
+    data = data_tmajor.astype(np.float64) * (grid_z ** 4 if diffuse else grid_z ** 2)
+    tdata = np.zeros((2 * M, 2 * N, 2 * N), dtype=np.complex128)
+    tdata[:M, :N, :N] = (mtx @ data.reshape(M, N * N)).reshape(M, N, N)
+    tvol = np.fft.ifftn(np.fft.fftn(tdata) * invpsf)[:M, :N, :N]
+    vol = (mtxi @ tvol.reshape(M, N * N)).reshape(M, N, N)
+    return np.maximum(np.real(vol), 0)

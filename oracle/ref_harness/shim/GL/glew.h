@@ -1,0 +1,2 @@
+// Empty stand-in so the reference kernel headers compile without their GUI/graphics dependencies.
+#pragma once

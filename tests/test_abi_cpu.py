@@ -1,0 +1,119 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol the
+header declares, and its host-only functions match the oracle."""
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def header_functions():
+    text = (ROOT / "include" / "fbp.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fbp_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(built):
+    from fasterbackprojection_gb300 import _lib
+
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    names = header_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # The Python binding declares a signature for each of them.
+    assert sorted(_lib.SIGNATURES) == names
+
+
+def test_exports_are_plain_c_symbols(built):
+    from fasterbackprojection_gb300 import _lib
+
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (fbp_[a-z0-9_]+)$", out, flags=re.M))
+    assert set(header_functions()) <= exported
+
+
+def test_version_and_last_error(built):
+    from fasterbackprojection_gb300 import _lib
+
+    lib = _lib.load()
+    assert b"sm_103a" in lib.fbp_version()
+    assert lib.fbp_last_error() == b"" or isinstance(lib.fbp_last_error(), bytes)
+
+
+def test_log_weights_match_oracle_bitwise(built):
+    from fasterbackprojection_gb300.api import log_weights
+    from oracle import cpu
+
+    for k, s in [(5, 1.0), (3, 0.7), (7, 1.5), (9, 2.0)]:
+        np.testing.assert_array_equal(log_weights(k, s), cpu.log_weights(k, s))
+
+
+def test_linear_space_matches_reference_formula(built):
+    from fasterbackprojection_gb300.api import linear_space
+
+    got = linear_space(0.4, 0.6, 200)
+    step = (0.6 - 0.4) / 200
+    np.testing.assert_array_equal(got, 0.4 + step * np.arange(200))
+
+
+def test_invalid_arguments_are_reported_not_raised(built):
+    from fasterbackprojection_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.fbp_create(None, 0) == _lib.FBP_ERR_INVALID_ARG
+    assert b"null" in lib.fbp_last_error()
+    assert lib.fbp_linear_space(0.0, 1.0, 0, None) == _lib.FBP_ERR_INVALID_ARG
+    w = (ctypes.c_float * 1)()
+    assert lib.fbp_log_weights(0, 1.0, w) == _lib.FBP_ERR_INVALID_ARG
+
+
+def test_create_without_gpu_fails_cleanly(built):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from fasterbackprojection_gb300 import _lib
+
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    st = lib.fbp_create(ctypes.byref(h), 0)
+    assert st in (_lib.FBP_ERR_CUDA, _lib.FBP_ERR_INVALID_ARG)
+    assert lib.fbp_last_error() != b""
+
+
+def test_product_never_imports_the_oracle():
+    pkg = ROOT / "fasterbackprojection_gb300"
+    for f in list(pkg.rglob("*.py")) + list(pkg.rglob("*.cu")) + list(pkg.rglob("*.cpp")) + list(pkg.rglob("*.hpp")):
+        text = f.read_text()
+        assert not re.search(r"^\s*(from|import)\s+oracle", text, flags=re.M), f
+        assert "liboracle" not in text and "ref_kernels.cubin" not in text, f
+
+
+def test_scene_generator_known_answer():
+    from fasterbackprojection_gb300 import scenes
+
+    w = scenes.wall_grid(4)
+    assert w.shape == (16, 3) and w.dtype == np.float32
+    np.testing.assert_allclose(w[0], [-0.75, 0, -0.75])
+    np.testing.assert_allclose(w[1], [-0.25, 0, -0.75])  # l = iz * n + ix
+    cap = scenes.confocal_points(4, 1024, 32e-12, n_points=1, seed=4, noise=False)
+    pts, alb, _ = scenes.random_points(1, (0.4, 1.2), 4)
+    r = np.linalg.norm(w.astype(np.float64) - pts[0], axis=1)
+    b = np.rint(2 * r / cap.time_step).astype(int)
+    for l in range(16):
+        assert cap.cube[l, b[l]] == pytest.approx(alb[0] / r[l] ** 4, rel=1e-6)
+        assert np.count_nonzero(cap.cube[l]) == 1
+
+
+def test_bf16_bits_round_trip():
+    from fasterbackprojection_gb300 import scenes
+
+    a = np.array([0.0, 1.0, 3.0, 1e-3, 257.0, 65504.0], np.float32)
+    back = scenes.from_bits_bf16(scenes.to_bits_bf16(a))
+    np.testing.assert_allclose(back, a, rtol=2 ** -8)
+    assert back[2] == 3.0 and back[4] == 256.0  # round to nearest even

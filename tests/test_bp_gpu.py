@@ -1,0 +1,209 @@
+"""Backprojection kernels against the FP64 CPU oracle.
+
+Tolerances (relative L2 over the volume):
+  * 1e-6 when the oracle is given the GPU's own time bins (isolates the
+    accumulation: FP32 blocks + Kahan vs FP64), for FP32, BF16 and FP16
+    storage (the oracle reads the decoded 16-bit values);
+  * 1e-3 against fully independent FP64 bins, where rare pairs whose path
+    lands within an FP32 rounding of a bin edge fall in the neighbouring bin
+    (the count of such pairs is checked too).
+"""
+import numpy as np
+import pytest
+
+from oracle import cpu
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _confocal_case(n=12, T=512, vres=(28, 24, 32), seed=11, discard=1, t0=0.0, depth=(0.0, 2.4)):
+    from fasterbackprojection_gb300 import make_info, scenes
+
+    cap = scenes.confocal_points(n, T, 32e-12, n_points=40, seed=seed)
+    hmin, vs = scenes.volume_geometry(vres, depth_range=depth)
+    info = make_info(num_laser_targets=n * n, num_time_bins=T, time_step=cap.time_step, voxel_res=vres,
+                     hidden_min=hmin, voxel_size=vs, discard_first_last_bounces=discard, time_offset=t0,
+                     laser_position=(0.05, -0.25, 0.1), sensor_position=(-0.1, -0.2, 0.05))
+    return cap, info
+
+
+def _gpu_bins(ctx, info, lxyz_t, cuda):
+    import torch
+
+    V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
+    idx = torch.arange(V, dtype=torch.int64, device=cuda)
+    return ctx.debug_confocal_bins(info, lxyz_t, idx).cpu().numpy()
+
+
+@pytest.mark.parametrize("discard,t0", [(1, 0.0), (0, 0.0), (1, 0.3)])
+def test_confocal_f32_vs_fp64_oracle(ctx, cuda, discard, t0):
+    import torch
+
+    cap, info = _confocal_case(discard=discard, t0=t0)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    got = ctx.backproject_confocal(info, cube, lx).cpu().numpy()
+    ctx.check_device_status()
+    bins = _gpu_bins(ctx, info, lx, cuda)
+    want = cpu.confocal_voxel(info, cap.cube, cap.laser_xyz, bins=bins)
+    assert rel_l2(got, want) < 1e-6
+    # Fully independent FP64 bins.
+    want64 = cpu.confocal_voxel(info, cap.cube, cap.laser_xyz)
+    assert rel_l2(got, want64) < 1e-3
+
+
+@pytest.mark.parametrize("dtype", ["bf16", "f16"])
+def test_confocal_16bit_storage_vs_oracle(ctx, cuda, dtype):
+    import torch
+
+    cap, info = _confocal_case(seed=13)
+    tdt = torch.bfloat16 if dtype == "bf16" else torch.float16
+    cube16 = torch.from_numpy(cap.cube).to(cuda).to(tdt)
+    decoded = cube16.float().cpu().numpy()
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    got = ctx.backproject_confocal(info, cube16, lx).cpu().numpy()
+    bins = _gpu_bins(ctx, info, lx, cuda)
+    want = cpu.confocal_voxel(info, decoded, cap.laser_xyz, bins=bins)
+    assert rel_l2(got, want) < 1e-6
+
+
+def test_confocal_bins_agree_with_fp64_except_at_edges(ctx, cuda):
+    import torch
+
+    cap, info = _confocal_case(seed=17)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    bins = _gpu_bins(ctx, info, lx, cuda)
+    Vx, Vy, Vz = info.voxel_res
+    v = np.arange(Vx * Vy * Vz)
+    vz, r = np.divmod(v, Vx * Vy)
+    vy, vx = np.divmod(r, Vx)
+    p = np.stack([info.hidden_min[0] + (vx + 0.5) * info.voxel_size[0],
+                  info.hidden_min[1] + (vz + 0.5) * info.voxel_size[1],
+                  info.hidden_min[2] + (vy + 0.5) * info.voxel_size[2]], 1)
+    d = 2 * np.linalg.norm(p[:, None, :] - cap.laser_xyz[None].astype(np.float64), axis=2)
+    x = d / np.float64(np.float32(info.time_step))
+    b64 = np.where((x > -1) & (x < info.num_time_bins), np.trunc(x), -1).astype(np.int64)
+    diff = b64 != bins
+    assert diff.mean() < 1e-4
+    # Every disagreement sits within a few FP32 roundings of a bin edge.
+    frac = np.abs(x[diff] - np.rint(x[diff]))
+    assert np.all(frac < 1e-4)
+
+
+def test_confocal_is_deterministic_and_layouts_agree(ctx, cuda):
+    import torch
+
+    cap, info = _confocal_case(seed=19)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    a = ctx.backproject_confocal(info, cube, lx)
+    b = ctx.backproject_confocal(info, cube, lx)
+    c = ctx.backproject_confocal(info, cube.t().contiguous(), lx, layout=0)
+    assert torch.equal(a, b) and torch.equal(a, c)
+
+
+@pytest.mark.parametrize("n,vres,T", [(5, (3, 5, 7), 96), (7, (9, 1, 33), 300), (11, (65, 17, 9), 700)])
+def test_confocal_ragged_sizes(ctx, cuda, n, vres, T):
+    """Scan counts not a multiple of the chunk, volumes not a multiple of the tile."""
+    import torch
+
+    cap, info = _confocal_case(n=n, T=T, vres=vres, seed=n)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    got = ctx.backproject_confocal(info, cube, lx).cpu().numpy()
+    bins = _gpu_bins(ctx, info, lx, cuda)
+    want = cpu.confocal_voxel(info, cap.cube, cap.laser_xyz, bins=bins)
+    assert rel_l2(got, want) < 1e-6
+
+
+def test_confocal_voxels_touching_the_wall(ctx, cuda):
+    """Volumes reaching the wall exercise safeRCP's dist^2 <= EPS branch."""
+    import torch
+
+    cap, info = _confocal_case(seed=23, vres=(16, 16, 16), depth=(0.0, 0.2))
+    info.hidden_min[1] = -0.1
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    cube[:, :4] = 5.0  # make near-zero bins non-empty
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    got = ctx.backproject_confocal(info, cube, lx).cpu().numpy()
+    bins = _gpu_bins(ctx, info, lx, cuda)
+    want = cpu.confocal_voxel(info, cube.cpu().numpy(), cap.laser_xyz, bins=bins)
+    assert rel_l2(got, want) < 1e-6
+
+
+def test_confocal_empty_and_invalid_inputs(ctx, cuda):
+    import torch
+    from fasterbackprojection_gb300 import FbpError
+
+    cap, info = _confocal_case()
+    cube = torch.zeros_like(torch.from_numpy(cap.cube)).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    assert float(ctx.backproject_confocal(info, cube, lx).abs().max()) == 0.0
+    info.num_time_bins = 0
+    with pytest.raises(FbpError):
+        ctx.backproject_confocal(info, cube, lx)
+    cap, info = _confocal_case()
+    info.time_step = -1.0
+    with pytest.raises(FbpError):
+        ctx.backproject_confocal(info, cube, lx)
+
+
+@pytest.mark.parametrize("nl,ns,discard", [(3, 4, 1), (4, 3, 0), (2, 5, 1)])
+def test_exhaustive_vs_fp64_oracle(ctx, cuda, nl, ns, discard):
+    """Including L != S, where the reference's own pair split is out of range."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_EXHAUSTIVE, make_info, scenes
+
+    cap = scenes.exhaustive_points(nl, ns, 512, 32e-12, n_points=25, seed=nl * 10 + ns)
+    L, S, T = cap.cube.shape
+    vres = (20, 18, 22)
+    hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 2.0))
+    info = make_info(num_laser_targets=L, num_sensor_targets=S, num_time_bins=T, time_step=cap.time_step,
+                     voxel_res=vres, hidden_min=hmin, voxel_size=vs, capture_system=FBP_EXHAUSTIVE,
+                     discard_first_last_bounces=discard, laser_position=(0.0, -0.2, 0.1),
+                     sensor_position=(0.1, -0.3, 0.0))
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    sx = torch.from_numpy(cap.sensor_xyz).to(cuda)
+    got = ctx.backproject_exhaustive(info, cube, lx, sx).cpu().numpy()
+    V = vres[0] * vres[1] * vres[2]
+    bins = ctx.debug_exhaustive_bins(info, lx, sx, torch.arange(V, device=cuda)).cpu().numpy()
+    want = cpu.exhaustive_voxel(info, cap.cube, cap.laser_xyz, cap.sensor_xyz, bins=bins)
+    assert rel_l2(got, want) < 1e-6
+    assert rel_l2(got, cpu.exhaustive_voxel(info, cap.cube, cap.laser_xyz, cap.sensor_xyz)) < 1e-3
+
+
+def test_exhaustive_fp16_storage(ctx, cuda):
+    import torch
+    from fasterbackprojection_gb300 import FBP_EXHAUSTIVE, make_info, scenes
+
+    cap = scenes.exhaustive_points(3, 4, 512, 32e-12, n_points=25, seed=31)
+    L, S, T = cap.cube.shape
+    vres = (16, 16, 16)
+    hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 2.0))
+    info = make_info(num_laser_targets=L, num_sensor_targets=S, num_time_bins=T, time_step=cap.time_step,
+                     voxel_res=vres, hidden_min=hmin, voxel_size=vs, capture_system=FBP_EXHAUSTIVE)
+    cube = torch.from_numpy(cap.cube).to(cuda).half()
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    sx = torch.from_numpy(cap.sensor_xyz).to(cuda)
+    got = ctx.backproject_exhaustive(info, cube, lx, sx).cpu().numpy()
+    bins = ctx.debug_exhaustive_bins(info, lx, sx, torch.arange(16 ** 3, device=cuda)).cpu().numpy()
+    want = cpu.exhaustive_voxel(info, cube.float().cpu().numpy(), cap.laser_xyz, cap.sensor_xyz, bins=bins)
+    assert rel_l2(got, want) < 1e-6
+
+
+def test_depth_planes_vs_oracle(ctx, cuda):
+    import torch
+    from fasterbackprojection_gb300 import make_info, scenes
+    from fasterbackprojection_gb300.api import linear_space
+
+    cap = scenes.confocal_points(10, 512, 32e-12, n_points=30, seed=41)
+    L, T = cap.cube.shape
+    info = make_info(num_laser_targets=L, num_time_bins=T, time_step=cap.time_step, voxel_res=(1, 1, 1),
+                     hidden_min=(0, 0, 0), voxel_size=(1, 1, 1))
+    depths = linear_space(0.6, 1.0, 50)
+    got = ctx.backproject_depths(info, torch.from_numpy(cap.cube).to(cuda), torch.from_numpy(cap.laser_xyz).to(cuda),
+                                 torch.from_numpy(depths).to(cuda)).cpu().numpy()
+    want = cpu.depth_confocal(info, cap.cube, cap.laser_xyz, depths)
+    assert rel_l2(got, want) < 1e-3
