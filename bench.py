@@ -46,9 +46,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--small", action="store_true", help="64^2 scan, 64^3 volume (plumbing check)")
+    ap.add_argument("--size", choices=["full", "medium", "small"], default="full",
+                    help="full: 256^2 scan -> 256^3 (the benchmark); medium: 128^2 -> 128^3 and small: 64^2 -> 64^3 "
+                         "(profiling and plumbing checks)")
     ap.add_argument("--no-extras", action="store_true", help="skip bf16 / reference-CUDA / CPU legs")
-    return ap.parse_args()
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    a = ap.parse_args()
+    a.small = a.size != "full"
+    return a
+
+
+SIZES = {"full": (N_SCAN, VRES), "medium": (128, (128, 128, 128)), "small": (64, (64, 64, 64))}
 
 
 # ------------------------------------------------------------------ clocks
@@ -161,10 +169,10 @@ def profiled_traffic():
 
 # --------------------------------------------------------------- workloads
 
-def make_workload(device, seed: int, small: bool):
+def make_workload(device, seed: int, size: str):
     from fasterbackprojection_gb300 import make_info, scenes
 
-    n, vres = (64, (64, 64, 64)) if small else (N_SCAN, VRES)
+    n, vres = SIZES[size]
     cap = scenes.confocal_patches_torch(n, N_BINS, DT, seed=seed, device=device)
     hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 1.5))
     info = make_info(num_laser_targets=n * n, num_time_bins=N_BINS, time_step=cap.time_step, voxel_res=vres,
@@ -187,9 +195,9 @@ def cpu_sample_rate(info, cube_np, lx_np, target_s=10.0, threads=0):
         t0 = time.perf_counter()
         cpu.confocal_voxel_f32_subset(info, cube_np, lx_np, idx, threads=threads)
         dt = time.perf_counter() - t0
-        if dt > target_s / 4 or n >= V:
+        if dt > 0.7 * target_s or n >= V:
             break
-        n = int(min(V, n * max(2.0, min(16.0, (target_s / 4) / max(dt, 1e-3)))))
+        n = int(min(V, n * max(1.5, min(16.0, target_s / max(dt, 1e-3)))))
     pairs = idx.shape[0] * info.num_laser_targets
     return pairs / dt, f"{idx.shape[0]} random voxels x {info.num_laser_targets} scan points", dt
 
@@ -205,14 +213,15 @@ def run_ours(args):
     ws, rank, local = dist_setup("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    cap, info = make_workload(dev, 2 + rank, args.small)
+    cap, info = make_workload(dev, 2 + rank, args.size)
     L = info.num_laser_targets
     V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
     samples = V * L
     ctx = Context(local)
     cube = cap.cube.contiguous()
     lx = cap.laser_xyz.contiguous()
-    vol = torch.empty((VRES[2], VRES[1], VRES[0]) if not args.small else (64, 64, 64), device=dev)
+    vx, vy, vz = info.voxel_res
+    vol = torch.empty((vz, vy, vx), device=dev)
     vol2 = torch.empty_like(vol)
     stream = torch.cuda.current_stream()
 
@@ -253,27 +262,30 @@ def run_ours(args):
     ctx.check_device_status()
 
     # End to end through the C ABI from pinned host buffers.
-    host_cube = torch.empty(cube.shape, dtype=cube.dtype, pin_memory=True)
-    host_cube.copy_(cube)
-    host_lx = torch.empty(lx.shape, dtype=lx.dtype, pin_memory=True)
-    host_lx.copy_(lx)
-    host_vol = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True)
-    hc, hl, hv = host_cube.numpy(), host_lx.numpy(), host_vol.numpy()
+    e2e = None
+    if not args.no_e2e:
+        host_cube = torch.empty(cube.shape, dtype=cube.dtype, pin_memory=True)
+        host_cube.copy_(cube)
+        host_lx = torch.empty(lx.shape, dtype=lx.dtype, pin_memory=True)
+        host_lx.copy_(lx)
+        host_vol = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True)
+        hc, hl, hv = host_cube.numpy(), host_lx.numpy(), host_vol.numpy()
 
-    def e2e_step():
-        ctx.reconstruct_shape_host(info, hc, hl, use_fourier_filter=False, postfilter=FBP_FILTER_LOG, kernel_size=5,
-                                   sigma=1.0, normalize=True, out=hv)
+        def e2e_step():
+            ctx.reconstruct_shape_host(info, hc, hl, use_fourier_filter=False, postfilter=FBP_FILTER_LOG,
+                                       kernel_size=5, sigma=1.0, normalize=True, out=hv)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    barrier(ws)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = max_over_ranks(time.perf_counter() - t0, ws, dev)
-    e2e_value = ws * samples * args.steps / e2e_s
-    # e2e parity with the device path (same kernels, same inputs).
-    e2e_matches = bool(torch.equal(host_vol.to(dev), vol2))
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = max_over_ranks(time.perf_counter() - t0, ws, dev)
+        e2e = {"value": ws * samples * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(hc.nbytes + hl.nbytes),
+               "d2h_bytes_per_step": int(hv.nbytes),
+               # same kernels, same inputs as the device-resident step
+               "matches_device_path": bool(torch.equal(host_vol.to(dev), vol2))}
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -299,12 +311,11 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded 8-patch scene, Poisson noise), generated on device",
-        "config": {"workload": WORKLOAD if not args.small else "small_64^2x1024_to_64^3",
+        "config": {"workload": WORKLOAD if not args.small else f"{args.size}_{int(round(L ** 0.5))}^2x1024_to_{vx}^3",
                    "scan": [int(round(L ** 0.5))] * 2, "bins": N_BINS, "bin_ps": 16,
                    "volume": list(info.voxel_res), "storage": "f32", "postfilter": "LoG k=5 sigma=1",
                    "l2": "inputs larger than L2 (cube 256 MiB)", "per_gpu": "one capture per rank"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(hc.nbytes + hl.nbytes),
-                "d2h_bytes_per_step": int(hv.nbytes), "matches_device_path": e2e_matches},
+        "e2e": e2e,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": profiled_traffic(), "peak_source": peak_kind,
                      "note": "achieved = 4 B per voxel-sample / gather launch time; the gather is "
@@ -374,11 +385,11 @@ def run_reference(args):
     # The capture itself comes from the same generator; it needs a device for
     # the patch scene, otherwise fall back to a point scene of the same shape.
     if torch.cuda.is_available():
-        cap, info = make_workload(torch.device("cuda", local), 2, args.small)
+        cap, info = make_workload(torch.device("cuda", local), 2, args.size)
         cube = cap.cube.cpu().numpy()
         lx = cap.laser_xyz.cpu().numpy()
     else:
-        n = 64 if args.small else N_SCAN
+        n = SIZES[args.size][0]
         capn = scenes.confocal_points(n, N_BINS, DT, n_points=200, seed=2)
         hmin, vs = scenes.volume_geometry(VRES, depth_range=(0.0, 1.5))
         info = make_info(num_laser_targets=n * n, num_time_bins=N_BINS, time_step=capn.time_step, voxel_res=VRES,

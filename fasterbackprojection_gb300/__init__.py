@@ -18,6 +18,8 @@ from ._lib import (  # noqa: F401
     FBP_FILTER_NONE,
     FBP_LAYOUT_TIME_INNER,
     FBP_LAYOUT_TIME_MAJOR,
+    FBP_LCT_GRID_DEPTH,
+    FBP_LCT_GRID_REFERENCE,
     FbpError,
     ReconInfo,
     ShapeParams,

@@ -23,7 +23,8 @@ LIBFBP = LIBDIR / "libfbp.so"
 LIBFBP_HOST = LIBDIR / "libfbp_host.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                     "--expt-relaxed-constexpr",
                      "-diag-suppress", "177"]
 
 

@@ -63,6 +63,19 @@ class ReconInfo(ctypes.Structure):
 assert ctypes.sizeof(ReconInfo) == 148
 
 
+class LctParams(ctypes.Structure):
+    _fields_ = [
+        ("width", c_float),
+        ("bin_length", c_float),
+        ("snr", c_float),
+        ("diffuse", c_int),
+        ("grid_mode", c_int),
+    ]
+
+
+FBP_LCT_GRID_REFERENCE, FBP_LCT_GRID_DEPTH = 0, 1
+
+
 class ShapeParams(ctypes.Structure):
     _fields_ = [
         ("use_fourier_filter", c_int),
@@ -97,6 +110,7 @@ SIGNATURES = {
     "fbp_log_weights": (c_int, [c_int, c_float, POINTER(c_float)]),
     "fbp_normalize_minmax": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p]),
     "fbp_filter_h": (c_int, [c_void_p, c_void_p, c_uint64, c_uint32, c_float, c_float, c_float, c_int, c_void_p]),
+    "fbp_lct": (c_int, [c_void_p, c_void_p, c_int, c_uint32, c_uint32, POINTER(LctParams), c_void_p, c_void_p]),
     "fbp_reconstruct_shape_host": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_void_p, c_void_p,
                                            POINTER(ShapeParams), c_void_p, c_void_p]),
 }

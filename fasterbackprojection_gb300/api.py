@@ -12,7 +12,7 @@ from ctypes import byref, c_double, c_float, c_void_p
 import numpy as np
 
 from . import _lib
-from ._lib import ReconInfo, ShapeParams, check, load
+from ._lib import LctParams, ReconInfo, ShapeParams, check, load
 
 
 def make_info(*, num_laser_targets: int, num_time_bins: int, time_step: float, voxel_res, hidden_min, voxel_size,
@@ -194,6 +194,23 @@ class Context:
         wl = delta_t * 10.0 if wl_mean is None else wl_mean
         check(self._lib.fbp_filter_h(self._h, _ptr(data), n, T, delta_t, wl, wl_sigma, border, self._stream(stream)))
         return data
+
+    # ------------------------------------------------------------------- LCT
+    def lct(self, data, width: float, bin_length: float, snr: float = 0.8, diffuse: bool = True,
+            grid_mode: int = _lib.FBP_LCT_GRID_REFERENCE, layout: int = _lib.FBP_LAYOUT_TIME_MAJOR, out=None,
+            stream=None):
+        """Confocal LCT.  data: [M][N][N] (time-major) or [N][N][M] (time-inner), float32."""
+        import torch
+
+        if layout == _lib.FBP_LAYOUT_TIME_MAJOR:
+            M, N, _ = data.shape
+        else:
+            N, _, M = data.shape
+        if out is None:
+            out = torch.empty((M, N, N), dtype=torch.float32, device=data.device)
+        prm = LctParams(width, bin_length, snr, int(diffuse), grid_mode)
+        check(self._lib.fbp_lct(self._h, _ptr(data), layout, N, M, byref(prm), _ptr(out), self._stream(stream)))
+        return out
 
     # ------------------------------------------------------------- end to end
     def reconstruct_shape_host(self, info: ReconInfo, cube: np.ndarray, laser_xyz: np.ndarray,

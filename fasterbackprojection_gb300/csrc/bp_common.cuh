@@ -30,6 +30,7 @@ struct ConfocalGatherParams {
     float t0, dt;
     uint32_t row_pitch;  // elements per padded row
     uint32_t slot_w;     // window width in elements (the sentinel zero sits at slot_w)
+    int ch;              // scan points per pipeline stage (<= 32)
     const void* rows;    // [L][row_pitch] of the storage type
 
     // Bytes of per-chunk metadata in front of the window slots (16-byte aligned).
@@ -79,6 +80,18 @@ __device__ __forceinline__ void confocal_chunk(const float4* __restrict__ geo, c
         }
     }
 }
+
+// Window geometry shared by the gathers: the widest bin span a tile of the
+// given world extents can need, capped at the whole row (T bins plus one
+// alignment step), the padded row pitch, and the stage size that fits the
+// shared-memory budget.
+struct WindowPlan {
+    uint32_t slot_w, pitch;
+    int ch;
+    size_t smem;
+};
+fbp_status plan_window(const fbp_context* ctx, double ex, double ey, double ez, double time_step, uint32_t T, int align,
+                       size_t elem_bytes, size_t meta_bytes, WindowPlan* out, const char* who);
 
 // Shared host helpers.
 fbp_status build_tables(fbp_context* ctx, const fbp_recon_info& in, const float* laser_xyz, cudaStream_t stream,

@@ -111,21 +111,23 @@ __global__ void rows_zero_tail_kernel(S* __restrict__ rows, uint32_t L, uint32_t
 //   EXACT_TRUNC  bin = int(x) with a conversion (needed when time_offset > 0
 //            makes negative paths possible); otherwise the truncation uses a
 //            round-toward-zero add, valid because every path is >= 0.
-template <typename S, int KV, int WY, int WZ, int CH, bool BOUNCE, bool EXACT_TRUNC>
+template <typename S, int KV, int WY, int WZ, bool BOUNCE, bool EXACT_TRUNC>
 __global__ void __launch_bounds__(32 * WY * WZ)
 confocal_gather_kernel(ConfocalGatherParams p) {
     constexpr int NT = 32 * WY * WZ;
+    constexpr int CHMAX = 32;  // scan points (pairs) per stage, upper bound
+    const int CH = p.ch;
     constexpr int ALIGN = 16 / sizeof(S);  // elements per 16-byte copy
     constexpr int TY = 8 * WY, TZ = 4 * WZ;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t slot_stride = p.slot_w + ALIGN;  // zero element(s) at slot_w
-    float4* s_geo = reinterpret_cast<float4*>(smem_raw);                  // [2][CH]
-    float* s_cl = reinterpret_cast<float*>(s_geo + 2 * CH);              // [2][CH]
-    int* s_cnt = reinterpret_cast<int*>(s_cl + 2 * CH);                  // [2][CH]
-    int* s_src = s_cnt + 2 * CH;                                         // [2][CH]
-    int* s_flag = s_src + 2 * CH;                                        // [2]
-    S* s_slots = reinterpret_cast<S*>(smem_raw + ConfocalGatherParams::meta_bytes(CH));  // [2][CH][slot_stride]
+    float4* s_geo = reinterpret_cast<float4*>(smem_raw);                  // [2][CHMAX]
+    float* s_cl = reinterpret_cast<float*>(s_geo + 2 * CHMAX);           // [2][CHMAX]
+    int* s_cnt = reinterpret_cast<int*>(s_cl + 2 * CHMAX);               // [2][CHMAX]
+    int* s_src = s_cnt + 2 * CHMAX;                                      // [2][CHMAX]
+    int* s_flag = s_src + 2 * CHMAX;                                     // [2]
+    S* s_slots = reinterpret_cast<S*>(smem_raw + ConfocalGatherParams::meta_bytes(CHMAX));  // [2][CH][slot_stride]
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
@@ -190,17 +192,22 @@ confocal_gather_kernel(ConfocalGatherParams p) {
                 cnt = hi - a;
                 if (cnt < 0) cnt = 0;
                 cnt = (cnt + ALIGN - 1) & ~(ALIGN - 1);
-                if (cnt > (int)p.slot_w) {
+                // A window capped at slot_w still covers every valid bin as long
+                // as the bins below T it needs fit; bins past the copy map to the
+                // zero sentinel.
+                if (min(bhi + 1, (int)p.T) - a > (int)p.slot_w) {
                     atomicExch(p.status, (int)FBP_ERR_DEVICE);  // window too small: should not happen
+                }
+                if (cnt > (int)p.slot_w) {
                     cnt = (int)p.slot_w;
                 }
                 src = a;
                 cl = EXACT_TRUNC ? __int_as_float(a) : (float)(8388608 - a);
             }
-            s_geo[buf * CH + tid] = g;
-            s_cl[buf * CH + tid] = cl;
-            s_cnt[buf * CH + tid] = cnt;
-            s_src[buf * CH + tid] = src;
+            s_geo[buf * CHMAX + tid] = g;
+            s_cl[buf * CHMAX + tid] = cl;
+            s_cnt[buf * CHMAX + tid] = cnt;
+            s_src[buf * CHMAX + tid] = src;
             // Warp 0 holds every planning thread (CH <= 32): vote the flag.
             const unsigned any_near = __ballot_sync(CH >= 32 ? 0xffffffffu : ((1u << CH) - 1u), near);
             if (tid == 0) s_flag[buf] = any_near != 0;
@@ -212,9 +219,9 @@ confocal_gather_kernel(ConfocalGatherParams p) {
         const uint32_t vecs_per_slot = p.slot_w / ALIGN;
         for (uint32_t i = tid; i < CH * vecs_per_slot; i += NT) {
             const uint32_t s = i / vecs_per_slot, j = i - s * vecs_per_slot;
-            if ((int)(j * ALIGN) < s_cnt[buf * CH + s]) {
+            if ((int)(j * ALIGN) < s_cnt[buf * CHMAX + s]) {
                 const uint32_t l = c * CH + s;
-                const S* src = static_cast<const S*>(p.rows) + (size_t)l * p.row_pitch + s_src[buf * CH + s] + j * ALIGN;
+                const S* src = static_cast<const S*>(p.rows) + (size_t)l * p.row_pitch + s_src[buf * CHMAX + s] + j * ALIGN;
                 S* dst = s_slots + (size_t)(buf * CH + s) * slot_stride + j * ALIGN;
                 cp_async_16(dst, src);
             }
@@ -245,8 +252,8 @@ confocal_gather_kernel(ConfocalGatherParams p) {
         }
         __syncthreads();  // chunk c's windows visible
 
-        const float4* geo = s_geo + buf * CH;
-        const float* clv = s_cl + buf * CH;
+        const float4* geo = s_geo + buf * CHMAX;
+        const float* clv = s_cl + buf * CHMAX;
         const S* slots = s_slots + (size_t)buf * CH * slot_stride;
         const bool safe = s_flag[buf] != 0;
         const int nl = (int)min((uint32_t)CH, p.L - c * CH);
@@ -310,7 +317,7 @@ fbp_status prepare_rows(fbp_context* ctx, const void* cube, int layout, uint32_t
     return FBP_OK;
 }
 
-constexpr int kKV = 8, kWY = 2, kWZ = 4, kCH = 32;
+constexpr int kKV = 8, kWY = 2, kWZ = 4;
 
 template <typename S>
 fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int layout,
@@ -319,15 +326,14 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     const uint32_t Vx = in.voxel_res[0], Vy = in.voxel_res[1], Vz = in.voxel_res[2];
     constexpr int ALIGN = 16 / sizeof(S);
 
-    // Window width: the largest bin span any tile can need.
-    const double ex = (double)kKV * std::fabs(in.voxel_size[0]);
-    const double ey = (double)(4 * kWZ) * std::fabs(in.voxel_size[1]);
-    const double ez = (double)(8 * kWY) * std::fabs(in.voxel_size[2]);
-    const double diag = std::sqrt(ex * ex + ey * ey + ez * ez);
-    const double span = 2.0 * diag / std::fabs((double)in.time_step) + 8.0 + ALIGN;
-    if (!(span < 65536.0)) return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_confocal: voxel tile spans too many bins");
-    const uint32_t slot_w = ((uint32_t)std::ceil(span) + ALIGN - 1) / ALIGN * ALIGN;
-    const uint32_t pitch = (T + slot_w + ALIGN - 1) / ALIGN * ALIGN;
+    // World extents of the largest tile (clamped to the volume).
+    const double ex = (double)std::min<uint32_t>(kKV, Vx) * std::fabs(in.voxel_size[0]);
+    const double ey = (double)std::min<uint32_t>(4 * kWZ, Vz) * std::fabs(in.voxel_size[1]);
+    const double ez = (double)std::min<uint32_t>(8 * kWY, Vy) * std::fabs(in.voxel_size[2]);
+    WindowPlan wp;
+    FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(S), ConfocalGatherParams::meta_bytes(32), &wp,
+                        "fbp_backproject_confocal"));
+    const uint32_t slot_w = wp.slot_w, pitch = wp.pitch;
 
     S* rows = nullptr;
     FBP_TRY(prepare_rows<S>(ctx, cube, layout, L, T, pitch, stream, &rows));
@@ -342,9 +348,8 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     p.dt = in.time_step;
     p.row_pitch = pitch;
     p.slot_w = slot_w;
-
-    const size_t smem = ConfocalGatherParams::meta_bytes(kCH) + (size_t)2 * kCH * (slot_w + ALIGN) * sizeof(S);
-    if (smem > (size_t)ctx->smem_optin) return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_confocal: window too large");
+    p.ch = wp.ch;
+    const size_t smem = wp.smem;
     dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(Vz, 4 * kWZ));
     const bool bounce = in.discard_first_last_bounces == 0;
     const bool exact = in.time_offset > 0.f;
@@ -355,11 +360,11 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
         return FBP_OK;
     };
     if (bounce) {
-        if (exact) return go(confocal_gather_kernel<S, kKV, kWY, kWZ, kCH, true, true>);
-        return go(confocal_gather_kernel<S, kKV, kWY, kWZ, kCH, true, false>);
+        if (exact) return go(confocal_gather_kernel<S, kKV, kWY, kWZ, true, true>);
+        return go(confocal_gather_kernel<S, kKV, kWY, kWZ, true, false>);
     }
-    if (exact) return go(confocal_gather_kernel<S, kKV, kWY, kWZ, kCH, false, true>);
-    return go(confocal_gather_kernel<S, kKV, kWY, kWZ, kCH, false, false>);
+    if (exact) return go(confocal_gather_kernel<S, kKV, kWY, kWZ, false, true>);
+    return go(confocal_gather_kernel<S, kKV, kWY, kWZ, false, false>);
 }
 
 }  // namespace
@@ -387,6 +392,27 @@ fbp_status build_tables(fbp_context* ctx, const fbp_recon_info& in, const float*
     *xs = a;
     *ys = a + Vx;
     *zs = a + Vx + Vz;
+    return FBP_OK;
+}
+
+fbp_status plan_window(const fbp_context* ctx, double ex, double ey, double ez, double time_step, uint32_t T, int align,
+                       size_t elem_bytes, size_t meta_bytes, WindowPlan* out, const char* who) {
+    const double diag = std::sqrt(ex * ex + ey * ey + ez * ez);
+    // Round trip across the tile, a 2-bin margin on each side, alignment slack.
+    const double span = 2.0 * diag / std::fabs(time_step) + 8.0 + align;
+    const uint32_t t_round = (T + align - 1) / align * align;
+    const uint32_t cap = t_round + align;
+    uint32_t slot_w = span < (double)cap ? ((uint32_t)std::ceil(span) + align - 1) / align * align : cap;
+    if (slot_w > cap) slot_w = cap;
+    out->slot_w = slot_w;
+    out->pitch = t_round + slot_w;
+    const size_t per_stage = (size_t)2 * (slot_w + align) * elem_bytes;  // double-buffered, per scan point
+    int ch = 32;
+    while (ch > 1 && meta_bytes + (size_t)ch * per_stage > (size_t)ctx->smem_optin) ch >>= 1;
+    if (meta_bytes + (size_t)ch * per_stage > (size_t)ctx->smem_optin)
+        return set_error(FBP_ERR_UNSUPPORTED, std::string(who) + ": time-bin window too large for shared memory");
+    out->ch = ch;
+    out->smem = meta_bytes + (size_t)ch * per_stage;
     return FBP_OK;
 }
 

@@ -29,6 +29,7 @@ struct ExhaustiveGatherParams {
     uint32_t Vx, Vy, Vz, L, S, T;
     float t0, dt;
     uint32_t row_pitch, slot_w;
+    int ch;
 
     __host__ __device__ static constexpr size_t meta_bytes(int ch) {
         return ((size_t)2 * ch * (2 * sizeof(float4) + sizeof(float) + 3 * sizeof(int)) + 2 * sizeof(int) + 15) &
@@ -36,23 +37,25 @@ struct ExhaustiveGatherParams {
     }
 };
 
-template <typename S, int KV, int WY, int WZ, int CH, bool BOUNCE, bool EXACT_TRUNC>
+template <typename S, int KV, int WY, int WZ, bool BOUNCE, bool EXACT_TRUNC>
 __global__ void __launch_bounds__(32 * WY * WZ)
 exhaustive_gather_kernel(ExhaustiveGatherParams p) {
     constexpr int NT = 32 * WY * WZ;
+    constexpr int CHMAX = 32;  // scan points (pairs) per stage, upper bound
+    const int CH = p.ch;
     constexpr int ALIGN = 16 / sizeof(S);
     constexpr int TY = 8 * WY, TZ = 4 * WZ;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t slot_stride = p.slot_w + ALIGN;
-    float4* s_lg = reinterpret_cast<float4*>(smem_raw);  // [2][CH]
-    float4* s_sg = s_lg + 2 * CH;                        // [2][CH]
-    float* s_cl = reinterpret_cast<float*>(s_sg + 2 * CH);
-    int* s_cnt = reinterpret_cast<int*>(s_cl + 2 * CH);
-    int* s_src = s_cnt + 2 * CH;
-    int* s_lid = s_src + 2 * CH;
-    int* s_flag = s_lid + 2 * CH;
-    S* s_slots = reinterpret_cast<S*>(smem_raw + ExhaustiveGatherParams::meta_bytes(CH));
+    float4* s_lg = reinterpret_cast<float4*>(smem_raw);  // [2][CHMAX]
+    float4* s_sg = s_lg + 2 * CHMAX;                     // [2][CHMAX]
+    float* s_cl = reinterpret_cast<float*>(s_sg + 2 * CHMAX);
+    int* s_cnt = reinterpret_cast<int*>(s_cl + 2 * CHMAX);
+    int* s_src = s_cnt + 2 * CHMAX;
+    int* s_lid = s_src + 2 * CHMAX;
+    int* s_flag = s_lid + 2 * CHMAX;
+    S* s_slots = reinterpret_cast<S*>(smem_raw + ExhaustiveGatherParams::meta_bytes(CHMAX));
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
@@ -115,19 +118,24 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
                 cnt = hi - a;
                 if (cnt < 0) cnt = 0;
                 cnt = (cnt + ALIGN - 1) & ~(ALIGN - 1);
+                // A window capped at slot_w still covers every valid bin as long
+                // as the bins below T it needs fit; bins past the copy map to the
+                // zero sentinel.
+                if (min(bhi + 1, (int)p.T) - a > (int)p.slot_w) {
+                    atomicExch(p.status, (int)FBP_ERR_DEVICE);  // window too small: should not happen
+                }
                 if (cnt > (int)p.slot_w) {
-                    atomicExch(p.status, (int)FBP_ERR_DEVICE);
                     cnt = (int)p.slot_w;
                 }
                 src = a;
                 cl = EXACT_TRUNC ? __int_as_float(a) : (float)(8388608 - a);
             }
-            s_lg[buf * CH + tid] = lg;
-            s_sg[buf * CH + tid] = sg;
-            s_cl[buf * CH + tid] = cl;
-            s_cnt[buf * CH + tid] = cnt;
-            s_src[buf * CH + tid] = src;
-            s_lid[buf * CH + tid] = lid;
+            s_lg[buf * CHMAX + tid] = lg;
+            s_sg[buf * CHMAX + tid] = sg;
+            s_cl[buf * CHMAX + tid] = cl;
+            s_cnt[buf * CHMAX + tid] = cnt;
+            s_src[buf * CHMAX + tid] = src;
+            s_lid[buf * CHMAX + tid] = lid;
             const unsigned any_near = __ballot_sync(CH >= 32 ? 0xffffffffu : ((1u << CH) - 1u), near);
             if (tid == 0) s_flag[buf] = any_near != 0;
         }
@@ -137,9 +145,9 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
         const uint32_t vecs = p.slot_w / ALIGN;
         for (uint32_t i = tid; i < CH * vecs; i += NT) {
             const uint32_t s = i / vecs, j = i - s * vecs;
-            if ((int)(j * ALIGN) < s_cnt[buf * CH + s]) {
+            if ((int)(j * ALIGN) < s_cnt[buf * CHMAX + s]) {
                 const uint64_t ls = c * CH + s;
-                const S* src = static_cast<const S*>(p.rows) + ls * p.row_pitch + s_src[buf * CH + s] + j * ALIGN;
+                const S* src = static_cast<const S*>(p.rows) + ls * p.row_pitch + s_src[buf * CHMAX + s] + j * ALIGN;
                 cp_async_16(s_slots + (size_t)(buf * CH + s) * slot_stride + j * ALIGN, src);
             }
         }
@@ -172,10 +180,10 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
         const bool safe = s_flag[buf] != 0;
         const int np = (int)min((uint64_t)CH, npairs - c * CH);
         for (int i = 0; i < np; ++i) {
-            const float4 lg = s_lg[buf * CH + i];
-            const float4 sg = s_sg[buf * CH + i];
-            const float cl = s_cl[buf * CH + i];
-            const int lid = s_lid[buf * CH + i];
+            const float4 lg = s_lg[buf * CHMAX + i];
+            const float4 sg = s_sg[buf * CHMAX + i];
+            const float cl = s_cl[buf * CHMAX + i];
+            const int lid = s_lid[buf * CHMAX + i];
             const S* slot = s_slots + (size_t)(buf * CH + i) * slot_stride;
             if (lid != cur_l) {  // uniform across the CTA
                 cur_l = lid;
@@ -230,7 +238,7 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
 
 namespace {
 
-constexpr int kKV = 8, kWY = 2, kWZ = 4, kCH = 32;
+constexpr int kKV = 8, kWY = 2, kWZ = 4;
 
 template <typename S>
 __global__ void pair_rows_kernel(S* __restrict__ rows, const S* __restrict__ cube, uint64_t npairs, uint32_t T,
@@ -254,14 +262,13 @@ fbp_status launch_exhaustive(fbp_context* ctx, const fbp_recon_info& in, const v
     const uint32_t L = in.num_laser_targets, Sn = in.num_sensor_targets, T = in.num_time_bins;
     const uint32_t Vx = in.voxel_res[0], Vy = in.voxel_res[1], Vz = in.voxel_res[2];
     constexpr int ALIGN = 16 / sizeof(S);
-    const double ex = (double)kKV * std::fabs(in.voxel_size[0]);
-    const double ey = (double)(4 * kWZ) * std::fabs(in.voxel_size[1]);
-    const double ez = (double)(8 * kWY) * std::fabs(in.voxel_size[2]);
-    const double diag = std::sqrt(ex * ex + ey * ey + ez * ez);
-    const double span = 2.0 * diag / std::fabs((double)in.time_step) + 8.0 + ALIGN;
-    if (!(span < 65536.0)) return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_exhaustive: voxel tile spans too many bins");
-    const uint32_t slot_w = ((uint32_t)std::ceil(span) + ALIGN - 1) / ALIGN * ALIGN;
-    const uint32_t pitch = (T + slot_w + ALIGN - 1) / ALIGN * ALIGN;
+    const double ex = (double)std::min<uint32_t>(kKV, Vx) * std::fabs(in.voxel_size[0]);
+    const double ey = (double)std::min<uint32_t>(4 * kWZ, Vz) * std::fabs(in.voxel_size[1]);
+    const double ez = (double)std::min<uint32_t>(8 * kWY, Vy) * std::fabs(in.voxel_size[2]);
+    WindowPlan wp;
+    FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(S), ExhaustiveGatherParams::meta_bytes(32), &wp,
+                        "fbp_backproject_exhaustive"));
+    const uint32_t slot_w = wp.slot_w, pitch = wp.pitch;
     const uint64_t npairs = (uint64_t)L * Sn;
 
     void* rows = nullptr;
@@ -301,9 +308,8 @@ fbp_status launch_exhaustive(fbp_context* ctx, const fbp_recon_info& in, const v
     p.dt = in.time_step;
     p.row_pitch = pitch;
     p.slot_w = slot_w;
-
-    const size_t smem = ExhaustiveGatherParams::meta_bytes(kCH) + (size_t)2 * kCH * (slot_w + ALIGN) * sizeof(S);
-    if (smem > (size_t)ctx->smem_optin) return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_exhaustive: window too large");
+    p.ch = wp.ch;
+    const size_t smem = wp.smem;
     dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(Vz, 4 * kWZ));
     const bool bounce = in.discard_first_last_bounces == 0;
     const bool exact = in.time_offset > 0.f;
@@ -314,11 +320,11 @@ fbp_status launch_exhaustive(fbp_context* ctx, const fbp_recon_info& in, const v
         return FBP_OK;
     };
     if (bounce) {
-        if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, true, true>);
-        return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, true, false>);
+        if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, true>);
+        return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, false>);
     }
-    if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, false, true>);
-    return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, kCH, false, false>);
+    if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, true>);
+    return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, false>);
 }
 
 }  // namespace

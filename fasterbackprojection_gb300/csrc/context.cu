@@ -97,6 +97,8 @@ fbp_status fbp_destroy(fbp_context* ctx) {
     cudaDeviceSynchronize();
     for (int i = 0; i < WS_NUM_SLOTS; ++i)
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);
+    for (void* t : ctx->twiddles)
+        if (t) cudaFree(t);
     if (ctx->status_dev) cudaFree(ctx->status_dev);
     delete ctx;
     return FBP_OK;

@@ -54,6 +54,7 @@ enum WorkspaceSlot {
     WS_FFT_A,
     WS_FFT_B,
     WS_FFT_C,
+    WS_LCT_OPERATOR,    // resampling operator CSR (mtx and its transpose)
     WS_MISC,
     WS_HOST_STAGING_IN, // device copies for the host-buffer entry points
     WS_HOST_STAGING_OUT,
@@ -72,6 +73,14 @@ struct fbp_context {
     size_t ws_bytes[fbp::WS_NUM_SLOTS] = {};
     int* status_dev = nullptr;  // device status word: 0 ok, else an fbp_status
     uint64_t launches = 0;
+    // FFT twiddle tables, one per power-of-two length (index log2 n).
+    void* twiddles[16] = {};
+    // Cached LCT plan: Wiener filter of the PSF and the resampling operator
+    // for the last (N, M, slope, snr) seen; valid while lct_key_valid.
+    bool lct_key_valid = false;
+    uint32_t lct_N = 0, lct_M = 0;
+    double lct_slope = 0.0, lct_snr = 0.0;
+    size_t lct_nnz = 0;
 };
 
 namespace fbp {

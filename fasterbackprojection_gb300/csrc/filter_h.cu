@@ -21,27 +21,32 @@ namespace fbp {
 constexpr int kMaxTaps = 2048;
 __constant__ float c_filter_taps[kMaxTaps];
 
-// One CTA filters one series at a time (grid-stride over series).  The
-// extended series h_ext[-R, T+R) lives in shared memory.
-__global__ void filter_h_kernel(float* __restrict__ data, uint64_t nseries, uint32_t T, int R, int pad, int edge) {
-    extern __shared__ float sh[];  // T + 2R floats
-    const int E = (int)T + 2 * R;
+// One CTA filters one series at a time (grid-stride over series).  Shared
+// memory holds the padded period P[k] = h_ext[k - pad], k < n, extended
+// circularly by R on both sides: S[i] = P[(i - R) mod n], i < n + 2R, so
+//     out[t] = sum_{j=0}^{2R} taps[j] * S[t + pad + 2R - j]
+// is the circular correlation the padded FFTs compute.
+__global__ void filter_h_kernel(float* __restrict__ data, uint64_t nseries, uint32_t T, int n, int R, int pad,
+                                int edge) {
+    extern __shared__ float sh[];  // n + 2R floats
+    const int E = n + 2 * R;
     for (uint64_t s = blockIdx.x; s < nseries; s += gridDim.x) {
         float* h = data + s * T;
         const float first = h[0], last = h[T - 1];
         for (int i = threadIdx.x; i < E; i += blockDim.x) {
-            const int u = i - R;  // signal index
+            int k = (i - R) % n;
+            if (k < 0) k += n;
+            const int u = k - pad;  // signal index
             float v;
             if (u >= 0 && u < (int)T) v = h[u];
-            else if (edge && u >= -pad && u < (int)T + pad) v = u < 0 ? first : last;
+            else if (edge) v = u < 0 ? first : last;
             else v = 0.f;
             sh[i] = v;
         }
         __syncthreads();
         for (int t = threadIdx.x; t < (int)T; t += blockDim.x) {
-            // taps[j] is the weight of lag delta = j - R (delta = t - u).
             float acc = 0.f;
-            const float* hp = sh + t + 2 * R;  // u = t - delta  ->  sh index t - delta + R
+            const float* hp = sh + t + pad + 2 * R;
             for (int j = 0; j <= 2 * R; ++j) acc = fmaf(hp[-j], c_filter_taps[j], acc);
             h[t] = acc;
         }
@@ -79,12 +84,12 @@ fbp_status filter_h_taps(uint32_t nt, float delta_t, float wl_mean, float wl_sig
         const double phase = 2.0 * M_PI * (src * dt) / (double)wl_mean;
         return env[src] * std::cos(phase) / envsum;
     };
+    // Lags are circular over the padded period: |lag| <= n/2 covers them all.
     double kmax = 0.0;
-    for (int m = -(n - 1); m <= n - 1; ++m) kmax = std::max(kmax, std::fabs(kr(m)));
+    for (int m = -n / 2; m <= n / 2; ++m) kmax = std::max(kmax, std::fabs(kr(m)));
     int r = 0;
-    for (int m = 1; m < n; ++m)
+    for (int m = 1; m <= n / 2; ++m)
         if (std::fabs(kr(m)) > 1e-12 * kmax || std::fabs(kr(-m)) > 1e-12 * kmax) r = m;
-    r = std::min(r, (int)nt + pad);  // lags beyond the extended support never meet data
     if (2 * r + 1 > kMaxTaps) return set_error(FBP_ERR_UNSUPPORTED, "filter_H: filter longer than 2047 taps");
     R = r;
     taps.assign(2 * r + 1, 0.f);
@@ -99,11 +104,11 @@ fbp_status filter_h_device(fbp_context* ctx, float* data, uint64_t nseries, uint
     FBP_TRY(filter_h_taps(T, delta_t, wl_mean, wl_sigma, taps, R, pad, n));
     FBP_TRY_CUDA(cudaMemcpyToSymbolAsync(c_filter_taps, taps.data(), taps.size() * sizeof(float), 0,
                                          cudaMemcpyHostToDevice, stream));
-    const size_t smem = (size_t)(T + 2 * R) * sizeof(float);
+    const size_t smem = (size_t)(n + 2 * R) * sizeof(float);
     if (smem > (size_t)ctx->smem_optin) return set_error(FBP_ERR_UNSUPPORTED, "filter_H: series too long for one CTA");
     FBP_TRY_CUDA(cudaFuncSetAttribute(filter_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned blocks = (unsigned)std::min<uint64_t>(nseries, (uint64_t)ctx->sm_count * 8);
-    filter_h_kernel<<<blocks, 256, smem, stream>>>(data, nseries, T, R, pad, border == FBP_BORDER_EDGE);
+    filter_h_kernel<<<blocks, 256, smem, stream>>>(data, nseries, T, n, R, pad, border == FBP_BORDER_EDGE);
     FBP_CHECK_LAUNCH(ctx, "filter_h_kernel");
     return FBP_OK;
 }

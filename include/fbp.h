@@ -172,6 +172,32 @@ typedef enum { FBP_BORDER_ZERO = 0, FBP_BORDER_EDGE = 1 } fbp_border;
 fbp_status fbp_filter_h(fbp_context* ctx, float* data, uint64_t num_series, uint32_t num_bins, float delta_t,
                         float wl_mean, float wl_sigma, int border, void* stream);
 
+/* ---- light-cone transform ------------------------------------------------ */
+
+/* Radiometric grid of the LCT.  python/lct.py:134-136 builds grid_z with
+ * np.tile(..., (1, N, N)).reshape(M, N, N), so voxel (z, y, x) is scaled by
+ * linspace(0, 1, M)[(z*N + y) % M]; FBP_LCT_GRID_DEPTH scales by [z] instead,
+ * the per-depth grid the surrounding comments describe. */
+typedef enum { FBP_LCT_GRID_REFERENCE = 0, FBP_LCT_GRID_DEPTH = 1 } fbp_lct_grid;
+
+typedef struct {
+    float width;      /* half-width of the scanned wall area in metres (lct.py `width`) */
+    float bin_length; /* metres of path per bin (c * bin resolution) */
+    float snr;        /* Wiener filter SNR (lct.py: 0.8) */
+    int diffuse;      /* 1: grid_z^4 radiometry (diffuse), 0: grid_z^2 */
+    int grid_mode;    /* fbp_lct_grid */
+} fbp_lct_params;
+
+/* Confocal LCT reconstruction (python/lct.py:97-211 without the file loading,
+ * downsampling and z_trim; the C++ LCT::reconstructAABB, LCT.cpp:16-18, is an
+ * empty stub in the reference).  data: N x N scan points x M bins, either
+ * FBP_LAYOUT_TIME_MAJOR [M][N][N] or FBP_LAYOUT_TIME_INNER [N][N][M];
+ * volume: [M][N][N] floats (depth, y, x).  N, M powers of two <= 2048.
+ * The PSF's Wiener filter and the resampling operator are cached in the
+ * context for the last (N, M, width/range, snr). */
+fbp_status fbp_lct(fbp_context* ctx, const float* data, int layout, uint32_t N, uint32_t M,
+                   const fbp_lct_params* params, float* volume, void* stream);
+
 /* ---- end to end (host buffers) ---------------------------------------------- */
 
 typedef struct {

@@ -17,7 +17,8 @@ def test_log_filter_vs_oracle(ctx, cuda, shape, ksize, sigma):
     vol = rng.gamma(2.0, 1.0, shape).astype(np.float32)
     got = ctx.postfilter(FBP_FILTER_LOG, torch.from_numpy(vol).to(cuda), ksize, sigma).cpu().numpy()
     want = cpu.log_filter(vol, cpu.log_weights(ksize, sigma), ksize)
-    assert rel_l2(got, want) < 1e-6
+    # FP32 sums of k^3 zero-sum taps (the reference's order) vs FP64.
+    assert rel_l2(got, want) < 5e-6
 
 
 @pytest.mark.parametrize("ksize", [3, 5])
