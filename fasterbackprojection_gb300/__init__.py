@@ -20,6 +20,10 @@ from ._lib import (  # noqa: F401
     FBP_LAYOUT_TIME_MAJOR,
     FBP_LCT_GRID_DEPTH,
     FBP_LCT_GRID_REFERENCE,
+    FBP_MIS_LEARNED,
+    FBP_MIS_REFERENCE,
+    FBP_MIS_SPATIAL,
+    FBP_MIS_UNIFORM,
     FbpError,
     ReconInfo,
     ShapeParams,

@@ -76,6 +76,22 @@ class LctParams(ctypes.Structure):
 FBP_LCT_GRID_REFERENCE, FBP_LCT_GRID_DEPTH = 0, 1
 
 
+class MisParams(ctypes.Structure):
+    _fields_ = [
+        ("proposal", c_int),
+        ("samples", c_uint32),
+        ("seed", c_uint64),
+        ("noise", c_void_p),
+        ("noise_size", c_uint64),
+        ("tile_cluster_cdf", c_void_p),
+        ("cluster_side", c_uint32),
+        ("scan_side", c_uint32),
+    ]
+
+
+FBP_MIS_UNIFORM, FBP_MIS_SPATIAL, FBP_MIS_LEARNED, FBP_MIS_REFERENCE = 0, 1, 2, 3
+
+
 class ShapeParams(ctypes.Structure):
     _fields_ = [
         ("use_fourier_filter", c_int),
@@ -110,6 +126,11 @@ SIGNATURES = {
     "fbp_log_weights": (c_int, [c_int, c_float, POINTER(c_float)]),
     "fbp_normalize_minmax": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p]),
     "fbp_filter_h": (c_int, [c_void_p, c_void_p, c_uint64, c_uint32, c_float, c_float, c_float, c_int, c_void_p]),
+    "fbp_mis_backproject": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p,
+                                    POINTER(MisParams), c_void_p, c_void_p]),
+    "fbp_mis_reference_tables": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_void_p,
+                                         c_void_p, c_void_p]),
+    "fbp_mis_tile_grid": (c_int, [POINTER(ReconInfo), POINTER(c_uint32)]),
     "fbp_lct": (c_int, [c_void_p, c_void_p, c_int, c_uint32, c_uint32, POINTER(LctParams), c_void_p, c_void_p]),
     "fbp_reconstruct_shape_host": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_void_p, c_void_p,
                                            POINTER(ShapeParams), c_void_p, c_void_p]),

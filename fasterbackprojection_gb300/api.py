@@ -12,7 +12,7 @@ from ctypes import byref, c_double, c_float, c_void_p
 import numpy as np
 
 from . import _lib
-from ._lib import LctParams, ReconInfo, ShapeParams, check, load
+from ._lib import LctParams, MisParams, ReconInfo, ShapeParams, check, load
 
 
 def make_info(*, num_laser_targets: int, num_time_bins: int, time_step: float, voxel_res, hidden_min, voxel_size,
@@ -195,6 +195,31 @@ class Context:
         check(self._lib.fbp_filter_h(self._h, _ptr(data), n, T, delta_t, wl, wl_sigma, border, self._stream(stream)))
         return data
 
+    # -------------------------------------------------------------------- MIS
+    def mis_backproject(self, info: ReconInfo, cube, laser_xyz, proposal: int, samples: int, seed: int = 0,
+                        noise=None, tile_cluster_cdf=None, cluster_side: int = 0, scan_side: int = 0, out=None,
+                        layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
+        import torch
+
+        vx, vy, vz = info.voxel_res
+        if out is None:
+            out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
+        prm = MisParams(proposal, samples, seed, _ptr(noise), 0 if noise is None else noise.numel(),
+                        _ptr(tile_cluster_cdf), cluster_side, scan_side)
+        check(self._lib.fbp_mis_backproject(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
+                                            _ptr(laser_xyz), byref(prm), _ptr(out), self._stream(stream)))
+        return out
+
+    def mis_reference_tables(self, info: ReconInfo, cube, layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
+        L = info.num_laser_targets
+        cdf = np.empty(L, np.float32)
+        alias = np.empty(L, np.uint32)
+        prob = np.empty(L, np.float32)
+        check(self._lib.fbp_mis_reference_tables(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
+                                                 c_void_p(cdf.ctypes.data), c_void_p(alias.ctypes.data),
+                                                 c_void_p(prob.ctypes.data), self._stream(stream)))
+        return cdf, alias, prob
+
     # ------------------------------------------------------------------- LCT
     def lct(self, data, width: float, bin_length: float, snr: float = 0.8, diffuse: bool = True,
             grid_mode: int = _lib.FBP_LCT_GRID_REFERENCE, layout: int = _lib.FBP_LAYOUT_TIME_MAJOR, out=None,
@@ -229,6 +254,12 @@ class Context:
             c_void_p(0 if sens is None else sens.ctypes.data), byref(params), c_void_p(out.ctypes.data),
             self._stream(stream)))
         return out
+
+
+def mis_tile_grid(info: ReconInfo):
+    t = (ctypes.c_uint32 * 3)()
+    check(load().fbp_mis_tile_grid(byref(info), t))
+    return tuple(t)
 
 
 def log_weights(size: int, sigma: float) -> np.ndarray:

@@ -19,6 +19,35 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // ------------------------------------------------------ confocal gather --
 
+// Scan-point sampling for the unbiased MIS estimator: each voxel tile draws
+// K scan points i.i.d. from a proposal p(l | tile) and weights each pair by
+// 1 / (K p(l | tile)), so sum_k f(v, l_k) / (K p(l_k)) is an unbiased estimate
+// of the full backprojection sum at every voxel of the tile.
+enum SampleMode { SAMPLE_UNIFORM = 0, SAMPLE_ALIAS = 1, SAMPLE_CLUSTERS = 2 };
+struct SampleParams {
+    int mode;
+    uint32_t K;              // samples per tile
+    unsigned long long seed;
+    const float* prob;       // SAMPLE_ALIAS: Vose tables over scan points
+    const uint32_t* alias;
+    const float* pl;         // SAMPLE_ALIAS: p(l)
+    const float* tile_cdf;   // SAMPLE_CLUSTERS: [tiles][G] inclusive CDF over clusters
+    uint32_t G;              // clusters
+    uint32_t cluster_side;   // scan points per cluster side
+    uint32_t n_side;         // scan grid side (scan point l = iz * n_side + ix)
+};
+
+// Counter-based uniforms in [0, 1): a 64-bit mix of (seed, tile, k, stream).
+__device__ __forceinline__ float hash_uniform(unsigned long long seed, unsigned long long tile, unsigned k, unsigned s) {
+    unsigned long long x = seed ^ (tile * 0x9E3779B97F4A7C15ull) ^ ((unsigned long long)k << 32 | s) * 0xD1B54A32D192ED03ull;
+    x ^= x >> 31;
+    x *= 0x7FB5D329728EA185ull;
+    x ^= x >> 27;
+    x *= 0x81DADEF4BC2DD44Dull;
+    x ^= x >> 33;
+    return (float)(x >> 40) * (1.0f / 16777216.0f);
+}
+
 struct ConfocalGatherParams {
     const float4* scan;
     const float* xs;
@@ -32,54 +61,15 @@ struct ConfocalGatherParams {
     uint32_t slot_w;     // window width in elements (the sentinel zero sits at slot_w)
     int ch;              // scan points per pipeline stage (<= 32)
     const void* rows;    // [L][row_pitch] of the storage type
+    SampleParams smp;    // used by the sampled (MIS) variant only
 
     // Bytes of per-chunk metadata in front of the window slots (16-byte aligned).
     __host__ __device__ static constexpr size_t meta_bytes(int ch) {
-        return ((size_t)2 * ch * (sizeof(float4) + sizeof(float) + 2 * sizeof(int)) + 2 * sizeof(int) + 15) & ~size_t(15);
+        return ((size_t)2 * ch * (sizeof(float4) + sizeof(int2) + sizeof(float) + 3 * sizeof(int)) + 2 * sizeof(int) +
+                15) &
+               ~size_t(15);
     }
 };
-
-// One staged chunk of scan points against a thread's KV voxels (consecutive
-// along x, sharing the y/z offsets).  The per-pair sequence reproduces the
-// reference's time-bin arithmetic exactly (see fbp_internal.cuh); the bin then
-// indexes the scan point's staged window, whose element slot_w is zero.
-template <typename S, int KV, bool BOUNCE, bool EXACT_TRUNC, bool SAFE>
-__device__ __forceinline__ void confocal_chunk(const float4* __restrict__ geo, const float* __restrict__ clv,
-                                               const S* __restrict__ slots, uint32_t slot_stride, uint32_t slot_w,
-                                               int nl, const float (&px)[KV], float py, float pz, float neg_t0,
-                                               float rcp_dt, float (&acc)[KV]) {
-#pragma unroll 2
-    for (int i = 0; i < nl; ++i) {
-        const float4 g = geo[i];
-        const float c = clv[i];
-        const S* slot = slots + (size_t)i * slot_stride;
-        const float dy = sub_rn(py, g.y), dz = sub_rn(pz, g.z);
-        const float dy2 = mul_rn(dy, dy);
-#pragma unroll
-        for (int k = 0; k < KV; ++k) {
-            const float dx = sub_rn(px[k], g.x);
-            const float q = fma_rn(dz, dz, fma_rn(dx, dx, dy2));
-            const float d = sqrt_approx(q);
-            float dist = fma_rn(d, 2.f, neg_t0);
-            if (BOUNCE) dist = add_rn(dist, g.w);
-            const float x = ref_bin_ratio(dist, rcp_dt);
-            uint32_t idx;
-            if (EXACT_TRUNC) {
-                const int b = __float2int_rz(x);  // static_cast<int>, like the reference
-                idx = min((uint32_t)(b - __float_as_int(c)), slot_w);
-            } else {
-                // x >= 0 here: round-toward-zero add of 2^23 - a leaves
-                // floor(x) - a in the low mantissa bits.
-                const float y = add_rz(x, c);
-                idx = min(__float_as_uint(y) - 0x4B000000u, slot_w);
-            }
-            const float I = to_f32(slot[idx]);
-            const float dd = mul_rn(dist, dist);
-            const float w = SAFE ? ref_safe_rcp(dd) : rcp_approx(dd);
-            acc[k] = fmaf(I, w, acc[k]);
-        }
-    }
-}
 
 // Window geometry shared by the gathers: the widest bin span a tile of the
 // given world extents can need, capped at the whole row (T bins plus one
@@ -88,10 +78,17 @@ __device__ __forceinline__ void confocal_chunk(const float4* __restrict__ geo, c
 struct WindowPlan {
     uint32_t slot_w, pitch;
     int ch;
+    bool capped;  // slot_w is the whole row: bins past a window must be clamped
     size_t smem;
 };
 fbp_status plan_window(const fbp_context* ctx, double ex, double ey, double ez, double time_step, uint32_t T, int align,
                        size_t elem_bytes, size_t meta_bytes, WindowPlan* out, const char* who);
+
+// The confocal gather over all scan points (smp == nullptr) or over K sampled
+// scan points per tile (the unbiased MIS estimator).
+fbp_status confocal_gather(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype, int layout,
+                           const float* laser_xyz, float* volume, cudaStream_t s, const SampleParams* smp);
+void confocal_tile_grid(const fbp_recon_info& in, uint32_t out[3]);
 
 // Shared host helpers.
 fbp_status build_tables(fbp_context* ctx, const fbp_recon_info& in, const float* laser_xyz, cudaStream_t stream,

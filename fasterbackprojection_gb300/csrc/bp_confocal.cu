@@ -101,39 +101,126 @@ __global__ void rows_zero_tail_kernel(S* __restrict__ rows, uint32_t L, uint32_t
 
 // ----------------------------------------------------------- gather kernel --
 
-// The main kernel.  Template parameters:
-//   S        storage type of the rows (float, bf16, half)
-//   KV       voxels per thread, consecutive along x (they share dy, dz)
-//   WY, WZ   warps per CTA along the tile's y (voxel rows) and z (depth) axes;
-//            a warp covers 8 rows x 4 depth slices
-//   CH       scan points staged per pipeline stage
-//   BOUNCE   add the per-scan-point bounce term
-//   EXACT_TRUNC  bin = int(x) with a conversion (needed when time_offset > 0
-//            makes negative paths possible); otherwise the truncation uses a
-//            round-toward-zero add, valid because every path is >= 0.
-template <typename S, int KV, int WY, int WZ, bool BOUNCE, bool EXACT_TRUNC>
+// Arithmetic paths of the pair loop (all reproduce the reference's bins):
+//   PATH_2D     time_offset == 0, no bounce terms: dist = 2d exactly, so
+//               x = d * (2 rcp(dt)) and the weight is rcp(d^2) = 4 rcp(dist^2);
+//               the stage's partial sum is scaled by 1/4 (exact).
+//   PATH_FAST   time_offset <= 0 (every path >= 0): dist = fma(d, 2, -t0) [+ bounce].
+//   PATH_EXACT  time_offset > 0: negative paths possible, bin by conversion.
+// In PATH_2D / PATH_FAST the bin is floor(x) - a via a round-toward-zero add of
+// 2^23 - a; without CLAMP the window planner guarantees every bin of the tile
+// lies inside its window, so the -2^23 bias folds into the shared-memory base.
+enum { PATH_2D = 0, PATH_FAST = 1, PATH_EXACT = 2 };
+
+template <typename S>
+__device__ __forceinline__ float lds_elem(uint32_t addr);
+template <>
+__device__ __forceinline__ float lds_elem<float>(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+template <>
+__device__ __forceinline__ float lds_elem<__nv_bfloat16>(uint32_t addr) {
+    unsigned short v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr));
+    return __uint_as_float((uint32_t)v << 16);
+}
+template <>
+__device__ __forceinline__ float lds_elem<__half>(uint32_t addr) {
+    unsigned short v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr));
+    return __half2float(__ushort_as_half(v));
+}
+
+template <typename S> struct ElemShift;
+template <> struct ElemShift<float> { static constexpr int value = 2; };
+template <> struct ElemShift<__nv_bfloat16> { static constexpr int value = 1; };
+template <> struct ElemShift<__half> { static constexpr int value = 1; };
+
+// One staged stage of scan points against a thread's KV voxels (consecutive
+// along x, sharing the y/z offsets).
+template <typename S, int KV, int PATH, bool BOUNCE, bool CLAMP, bool SAFE, bool WEIGHTED>
+__device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, const int2* __restrict__ meta,
+                                               const float* __restrict__ wts, int nl, const float (&px)[KV], float py,
+                                               float pz, float neg_t0, float rcp_dt, uint32_t slot_w,
+                                               float (&acc)[KV]) {
+    constexpr int SH = ElemShift<S>::value;
+    const float rcp2 = 2.f * rcp_dt;  // exact
+#pragma unroll 2
+    for (int i = 0; i < nl; ++i) {
+        const float4 g = geo[i];
+        const int2 m = meta[i];  // (bin bias: float 2^23 - a, or a; slot shared address)
+        const float wl = WEIGHTED ? wts[i] : 1.f;
+        const float dy = sub_rn(py, g.y), dz = sub_rn(pz, g.z);
+        const float dy2 = mul_rn(dy, dy);
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+            const float dx = sub_rn(px[k], g.x);
+            const float d = sqrt_approx(fma_rn(dz, dz, fma_rn(dx, dx, dy2)));
+            float x, dist = 0.f;
+            if (PATH == PATH_2D && !SAFE) {
+                x = mul_rn(d, rcp2);
+            } else {
+                dist = fma_rn(d, 2.f, neg_t0);
+                if (BOUNCE) dist = add_rn(dist, g.w);
+                x = ref_bin_ratio(dist, rcp_dt);
+            }
+            uint32_t addr;
+            if (PATH == PATH_EXACT) {
+                const int b = __float2int_rz(x);  // static_cast<int>, like the reference
+                addr = (uint32_t)m.y + (min((uint32_t)(b - m.x), slot_w) << SH);
+            } else {
+                const uint32_t bits = __float_as_uint(add_rz(x, __int_as_float(m.x)));
+                if (CLAMP) addr = (uint32_t)m.y + (min(bits - 0x4B000000u, slot_w) << SH);
+                else addr = (uint32_t)m.y + (bits << SH);  // bias folded into m.y
+            }
+            float I = lds_elem<S>(addr);
+            if (WEIGHTED) I *= wl;
+            float w;
+            if (PATH == PATH_2D && !SAFE) w = rcp_approx(mul_rn(d, d));
+            else w = SAFE ? ref_safe_rcp(mul_rn(dist, dist)) : rcp_approx(mul_rn(dist, dist));
+            acc[k] = fmaf(I, w, acc[k]);
+        }
+    }
+}
+
+// The main kernel.  One CTA of 32*WY*WZ threads owns a tile of KV (x) x 8*WY
+// (rows) x 4*WZ (depth slices) voxels; a warp covers 8 rows x 4 slices, a
+// thread KV consecutive voxels along x.  Scan points (or, SAMPLED, K scan
+// points drawn per tile) are walked in stages of up to 32: one warp plans the
+// bin windows of the stage, all threads copy them from the padded rows into
+// shared memory with cp.async (double buffered), then every thread runs the
+// pair loop against the staged windows.  FP32 partials per stage, Kahan
+// across stages.
+template <typename S, int KV, int WY, int WZ, int PATH, bool BOUNCE, bool SAMPLED, bool CLAMP>
 __global__ void __launch_bounds__(32 * WY * WZ)
 confocal_gather_kernel(ConfocalGatherParams p) {
     constexpr int NT = 32 * WY * WZ;
-    constexpr int CHMAX = 32;  // scan points (pairs) per stage, upper bound
-    const int CH = p.ch;
+    constexpr int CHMAX = 32;
     constexpr int ALIGN = 16 / sizeof(S);  // elements per 16-byte copy
+    constexpr int SH = ElemShift<S>::value;
     constexpr int TY = 8 * WY, TZ = 4 * WZ;
+    const int CH = p.ch;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const uint32_t slot_stride = p.slot_w + ALIGN;  // zero element(s) at slot_w
-    float4* s_geo = reinterpret_cast<float4*>(smem_raw);                  // [2][CHMAX]
-    float* s_cl = reinterpret_cast<float*>(s_geo + 2 * CHMAX);           // [2][CHMAX]
-    int* s_cnt = reinterpret_cast<int*>(s_cl + 2 * CHMAX);               // [2][CHMAX]
-    int* s_src = s_cnt + 2 * CHMAX;                                      // [2][CHMAX]
-    int* s_flag = s_src + 2 * CHMAX;                                     // [2]
-    S* s_slots = reinterpret_cast<S*>(smem_raw + ConfocalGatherParams::meta_bytes(CHMAX));  // [2][CH][slot_stride]
+    const uint32_t slot_stride = p.slot_w + ALIGN;  // sentinel element(s) at slot_w
+    float4* s_geo = reinterpret_cast<float4*>(smem_raw);         // [2][CHMAX]
+    int2* s_meta = reinterpret_cast<int2*>(s_geo + 2 * CHMAX);   // [2][CHMAX]
+    int* s_cnt = reinterpret_cast<int*>(s_meta + 2 * CHMAX);     // [2][CHMAX]
+    int* s_src = s_cnt + 2 * CHMAX;                              // [2][CHMAX]
+    int* s_row = s_src + 2 * CHMAX;                              // [2][CHMAX]
+    float* s_w = reinterpret_cast<float*>(s_row + 2 * CHMAX);    // [2][CHMAX]
+    int* s_flag = reinterpret_cast<int*>(s_w + 2 * CHMAX);       // [2]
+    const size_t slots_off = ConfocalGatherParams::meta_bytes(CHMAX);
+    S* s_slots = reinterpret_cast<S*>(smem_raw + slots_off);     // [2][CH][slot_stride], then the zero slot
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem_raw);
+    const uint32_t zero_slot = 2u * CH * slot_stride;            // element index of the all-zero slot
 
     const int tid = threadIdx.x;
     const int lane = tid & 31, warp = tid >> 5;
     const int wy = warp % WY, wz = warp / WY;
 
-    // Tile origin.
     const uint32_t tx0 = blockIdx.x * KV, ty0 = blockIdx.y * TY, tz0 = blockIdx.z * TZ;
     const uint32_t vy = ty0 + wy * 8 + (lane & 7);
     const uint32_t vz = tz0 + wz * 4 + (lane >> 3);
@@ -154,22 +241,57 @@ confocal_gather_kernel(ConfocalGatherParams p) {
     const float rcp_dt = rcp_approx(p.dt);
     const float neg_t0 = -p.t0;
 
-    // Zero the sentinel element(s) of every slot once.
+    // Sentinels of every slot and the whole zero slot.
     for (int i = tid; i < 2 * CH * ALIGN; i += NT) {
         const int slot = i / ALIGN, e = i % ALIGN;
         s_slots[(size_t)slot * slot_stride + p.slot_w + e] = from_f32<S>(0.f);
     }
+    for (uint32_t i = tid; i < slot_stride; i += NT) s_slots[zero_slot + i] = from_f32<S>(0.f);
 
-    const uint32_t nchunks = (p.L + CH - 1) / CH;
+    const uint32_t nitems = SAMPLED ? p.smp.K : p.L;
+    const uint32_t nchunks = (nitems + CH - 1) / CH;
+    const unsigned long long tile_id =
+        ((unsigned long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
 
-    // Stage-1 of a chunk: window bounds for each scan point (threads < CH).
+    // Plan a stage: bin window of each scan point (threads < CH, all in warp 0).
     auto plan_chunk = [&](uint32_t c, int buf) {
         if (tid < CH) {
-            const uint32_t l = c * CH + tid;
+            const uint32_t item = c * CH + tid;
+            uint32_t l = item;
+            float wgt = 1.f;
+            if (SAMPLED && item < nitems) {
+                const float u1 = hash_uniform(p.smp.seed, tile_id, item, 0);
+                const float u2 = hash_uniform(p.smp.seed, tile_id, item, 1);
+                float pl;
+                if (p.smp.mode == SAMPLE_UNIFORM) {
+                    l = min((uint32_t)(u1 * (float)p.L), p.L - 1);
+                    pl = 1.f / (float)p.L;
+                } else if (p.smp.mode == SAMPLE_ALIAS) {
+                    const uint32_t kk = min((uint32_t)(u1 * (float)p.L), p.L - 1);
+                    l = u2 < p.smp.prob[kk] ? kk : p.smp.alias[kk];
+                    pl = p.smp.pl[l];
+                } else {
+                    // Cluster from the tile's CDF (binary search), then uniform inside it.
+                    const float* cdf = p.smp.tile_cdf + tile_id * p.smp.G;
+                    uint32_t lo = 0, hi = p.smp.G - 1;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (u1 < cdf[mid]) hi = mid; else lo = mid + 1;
+                    }
+                    const float pc = cdf[lo] - (lo > 0 ? cdf[lo - 1] : 0.f);
+                    const uint32_t cs = p.smp.cluster_side, cpr = (p.smp.n_side + cs - 1) / cs;
+                    const uint32_t cx = lo % cpr, cz = lo / cpr;
+                    const uint32_t w0 = min(cs, p.smp.n_side - cx * cs), h0 = min(cs, p.smp.n_side - cz * cs);
+                    const uint32_t inner = min((uint32_t)(u2 * (float)(w0 * h0)), w0 * h0 - 1);
+                    l = (cz * cs + inner / w0) * p.smp.n_side + cx * cs + inner % w0;
+                    pl = pc / (float)(w0 * h0);
+                }
+                wgt = pl > 0.f ? 1.f / ((float)nitems * pl) : 0.f;
+            }
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-            float cl = 0.f;  // x + 0 < 2^23 -> always the zero sentinel
-            int cnt = 0, src = 0, near = 0;
-            if (l < p.L) {
+            int cnt = 0, src = 0, near = 0, a = 0;
+            bool skip = true;
+            if (item < nitems && l < p.L) {
                 g = p.scan[l];
                 // Nearest and farthest voxel-centre distance of the tile.
                 const float cx = fminf(fmaxf(g.x, bx0), bx1), cy = fminf(fmaxf(g.y, by0), by1),
@@ -180,47 +302,70 @@ confocal_gather_kernel(ConfocalGatherParams p) {
                 const float dmax = sqrtf(fx * fx + fy * fy + fz * fz);
                 const float bnc = BOUNCE ? g.w : 0.f;
                 const float pmin = 2.f * dmin + neg_t0 + bnc, pmax = 2.f * dmax + neg_t0 + bnc;
-                // Paths this close make dist^2 <= EPS possible: use safeRCP's branch.
+                // Paths this short make dist^2 <= EPS possible: use safeRCP's branch.
                 near = pmin < 0.0035f;
-                const float xlo = pmin * rcp_dt, xhi = pmax * rcp_dt;
                 // Conservative bin range with a 2-bin margin for rounding.
-                int blo = (int)fmaxf(fminf(floorf(xlo), 1.0e9f), -1.0e9f) - 2;
-                int bhi = (int)fmaxf(fminf(floorf(xhi), 1.0e9f), -1.0e9f) + 2;
-                int a = max(blo, 0) & ~(ALIGN - 1);
-                a = min(a, (int)(p.row_pitch - p.slot_w));
-                const int hi = min(bhi + 1, (int)p.row_pitch);
-                cnt = hi - a;
-                if (cnt < 0) cnt = 0;
-                cnt = (cnt + ALIGN - 1) & ~(ALIGN - 1);
-                // A window capped at slot_w still covers every valid bin as long
-                // as the bins below T it needs fit; bins past the copy map to the
-                // zero sentinel.
-                if (min(bhi + 1, (int)p.T) - a > (int)p.slot_w) {
-                    atomicExch(p.status, (int)FBP_ERR_DEVICE);  // window too small: should not happen
+                const int blo = (int)fmaxf(fminf(floorf(pmin * rcp_dt), 1.0e9f), -1.0e9f) - 2;
+                const int bhi = (int)fmaxf(fminf(floorf(pmax * rcp_dt), 1.0e9f), -1.0e9f) + 2;
+                a = max(blo, 0) & ~(ALIGN - 1);
+                skip = bhi < 0 || blo >= (int)p.T;  // no bin of this tile is inside [0, T)
+                if (!skip) {
+                    if (CLAMP) a = min(a, (int)(p.row_pitch - p.slot_w));
+                    const int hi = min(bhi + 1, (int)p.row_pitch);
+                    cnt = (max(hi - a, 0) + ALIGN - 1) & ~(ALIGN - 1);
+                    if (cnt > (int)p.slot_w) {
+                        if (CLAMP) {
+                            // Capped window: bins past it map to the sentinel; only an
+                            // uncovered valid bin would be an error.
+                            if (min(bhi + 1, (int)p.T) - a > (int)p.slot_w) atomicExch(p.status, (int)FBP_ERR_DEVICE);
+                            cnt = (int)p.slot_w;
+                        } else {
+                            // The planner's span bound failed: read zeros, report.
+                            atomicExch(p.status, (int)FBP_ERR_DEVICE);
+                            skip = true;
+                            cnt = 0;
+                        }
+                    }
+                    src = a;
                 }
-                if (cnt > (int)p.slot_w) {
-                    cnt = (int)p.slot_w;
-                }
-                src = a;
-                cl = EXACT_TRUNC ? __int_as_float(a) : (float)(8388608 - a);
+            }
+            // Slot of this scan point (or the zero slot) as a shared address.
+            const uint32_t slot_elem = skip ? zero_slot : (uint32_t)(buf * CH + tid) * slot_stride;
+            uint32_t saddr = sbase + (uint32_t)slots_off + (slot_elem << SH);
+            int bias;
+            if (PATH == PATH_EXACT) {
+                bias = a;
+            } else {
+                bias = __float_as_int((float)(8388608 - a));
+                if (!CLAMP) saddr -= (0x4B000000u << SH);
+            }
+            if (item >= nitems || l >= p.L) {
+                // Beyond the last scan point: x + 0 < 2^23 lands on the sentinel
+                // (CLAMP) or, unclamped, reads the zero slot at index 0.
+                bias = PATH == PATH_EXACT ? 0x40000000 : 0;
+                saddr = sbase + (uint32_t)slots_off + (zero_slot << SH);
+                if (!CLAMP && PATH != PATH_EXACT) saddr -= (__float_as_uint(0.f) << SH);
+                g = make_float4(3.0e18f, 3.0e18f, 3.0e18f, 0.f);  // far away: x is huge
+                wgt = 0.f;
             }
             s_geo[buf * CHMAX + tid] = g;
-            s_cl[buf * CHMAX + tid] = cl;
+            s_meta[buf * CHMAX + tid] = make_int2(bias, (int)saddr);
             s_cnt[buf * CHMAX + tid] = cnt;
             s_src[buf * CHMAX + tid] = src;
-            // Warp 0 holds every planning thread (CH <= 32): vote the flag.
+            s_row[buf * CHMAX + tid] = (int)l;
+            s_w[buf * CHMAX + tid] = wgt;
             const unsigned any_near = __ballot_sync(CH >= 32 ? 0xffffffffu : ((1u << CH) - 1u), near);
             if (tid == 0) s_flag[buf] = any_near != 0;
         }
     };
 
-    // Stage-2 of a chunk: issue the window copies (all threads).
-    auto copy_chunk = [&](uint32_t c, int buf) {
+    // Copy a stage's windows (all threads).
+    auto copy_chunk = [&](int buf) {
         const uint32_t vecs_per_slot = p.slot_w / ALIGN;
         for (uint32_t i = tid; i < CH * vecs_per_slot; i += NT) {
             const uint32_t s = i / vecs_per_slot, j = i - s * vecs_per_slot;
             if ((int)(j * ALIGN) < s_cnt[buf * CHMAX + s]) {
-                const uint32_t l = c * CH + s;
+                const uint32_t l = (uint32_t)s_row[buf * CHMAX + s];
                 const S* src = static_cast<const S*>(p.rows) + (size_t)l * p.row_pitch + s_src[buf * CHMAX + s] + j * ALIGN;
                 S* dst = s_slots + (size_t)(buf * CH + s) * slot_stride + j * ALIGN;
                 cp_async_16(dst, src);
@@ -236,40 +381,41 @@ confocal_gather_kernel(ConfocalGatherParams p) {
     if (nchunks > 0) {
         plan_chunk(0, 0);
         __syncthreads();
-        copy_chunk(0, 0);
+        copy_chunk(0);
     }
 
     for (uint32_t c = 0; c < nchunks; ++c) {
         const int buf = c & 1;
-        __syncthreads();  // every thread is done with chunk c-1, whose buffer plan(c+1) reuses
+        __syncthreads();  // every thread is done with stage c-1, whose buffers plan(c+1) reuses
         if (c + 1 < nchunks) plan_chunk(c + 1, buf ^ 1);
         __syncthreads();  // plan(c+1) visible to the copy loop
         if (c + 1 < nchunks) {
-            copy_chunk(c + 1, buf ^ 1);
+            copy_chunk(buf ^ 1);
             cp_async_wait<1>();
         } else {
             cp_async_wait<0>();
         }
-        __syncthreads();  // chunk c's windows visible
+        __syncthreads();  // stage c's windows visible
 
         const float4* geo = s_geo + buf * CHMAX;
-        const float* clv = s_cl + buf * CHMAX;
-        const S* slots = s_slots + (size_t)buf * CH * slot_stride;
+        const int2* meta = s_meta + buf * CHMAX;
+        const float* wts = s_w + buf * CHMAX;
         const bool safe = s_flag[buf] != 0;
-        const int nl = (int)min((uint32_t)CH, p.L - c * CH);
-
+        const int nl = (int)min((uint32_t)CH, nitems - c * CH);
+        float scale = 1.f;
         if (!safe) {
-            confocal_chunk<S, KV, BOUNCE, EXACT_TRUNC, false>(geo, clv, slots, slot_stride, p.slot_w, nl, px, py, pz,
-                                                              neg_t0, rcp_dt, acc);
+            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, false, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
+                                                                        p.slot_w, acc);
+            if (PATH == PATH_2D) scale = 0.25f;  // w was rcp(d^2) = 4 rcp(dist^2)
         } else {
-            confocal_chunk<S, KV, BOUNCE, EXACT_TRUNC, true>(geo, clv, slots, slot_stride, p.slot_w, nl, px, py, pz,
-                                                             neg_t0, rcp_dt, acc);
+            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, true, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
+                                                                       p.slot_w, acc);
         }
 
-        // Compensated (Kahan) fold of this chunk's partial sums.
+        // Compensated (Kahan) fold of this stage's partial sums.
 #pragma unroll
         for (int k = 0; k < KV; ++k) {
-            const float y = sub_rn(acc[k], kcomp[k]);
+            const float y = sub_rn(mul_rn(acc[k], scale), kcomp[k]);
             const float t = add_rn(ksum[k], y);
             kcomp[k] = sub_rn(sub_rn(t, ksum[k]), y);
             ksum[k] = t;
@@ -319,9 +465,37 @@ fbp_status prepare_rows(fbp_context* ctx, const void* cube, int layout, uint32_t
 
 constexpr int kKV = 8, kWY = 2, kWZ = 4;
 
+template <typename S, int PATH, bool BOUNCE, bool SAMPLED, bool CLAMP>
+fbp_status go_confocal(fbp_context* ctx, const ConfocalGatherParams& p, dim3 grid, size_t smem, cudaStream_t stream) {
+    auto kernel = confocal_gather_kernel<S, kKV, kWY, kWZ, PATH, BOUNCE, SAMPLED, CLAMP>;
+    FBP_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<grid, 32 * kWY * kWZ, smem, stream>>>(p);
+    FBP_CHECK_LAUNCH(ctx, "confocal_gather_kernel");
+    return FBP_OK;
+}
+
+template <typename S, bool SAMPLED>
+fbp_status dispatch_confocal(fbp_context* ctx, const ConfocalGatherParams& p, dim3 grid, size_t smem,
+                             cudaStream_t stream, bool bounce, float t0, bool capped) {
+    if (t0 > 0.f) {
+        if (bounce) return go_confocal<S, PATH_EXACT, true, SAMPLED, true>(ctx, p, grid, smem, stream);
+        return go_confocal<S, PATH_EXACT, false, SAMPLED, true>(ctx, p, grid, smem, stream);
+    }
+    if (!bounce && t0 == 0.f) {
+        if (capped) return go_confocal<S, PATH_2D, false, SAMPLED, true>(ctx, p, grid, smem, stream);
+        return go_confocal<S, PATH_2D, false, SAMPLED, false>(ctx, p, grid, smem, stream);
+    }
+    if (bounce) {
+        if (capped) return go_confocal<S, PATH_FAST, true, SAMPLED, true>(ctx, p, grid, smem, stream);
+        return go_confocal<S, PATH_FAST, true, SAMPLED, false>(ctx, p, grid, smem, stream);
+    }
+    if (capped) return go_confocal<S, PATH_FAST, false, SAMPLED, true>(ctx, p, grid, smem, stream);
+    return go_confocal<S, PATH_FAST, false, SAMPLED, false>(ctx, p, grid, smem, stream);
+}
+
 template <typename S>
 fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int layout,
-                           const float* laser_xyz, float* volume, cudaStream_t stream) {
+                           const float* laser_xyz, float* volume, cudaStream_t stream, const SampleParams* smp) {
     const uint32_t L = in.num_laser_targets, T = in.num_time_bins;
     const uint32_t Vx = in.voxel_res[0], Vy = in.voxel_res[1], Vz = in.voxel_res[2];
     constexpr int ALIGN = 16 / sizeof(S);
@@ -333,10 +507,9 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     WindowPlan wp;
     FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(S), ConfocalGatherParams::meta_bytes(32), &wp,
                         "fbp_backproject_confocal"));
-    const uint32_t slot_w = wp.slot_w, pitch = wp.pitch;
 
     S* rows = nullptr;
-    FBP_TRY(prepare_rows<S>(ctx, cube, layout, L, T, pitch, stream, &rows));
+    FBP_TRY(prepare_rows<S>(ctx, cube, layout, L, T, wp.pitch, stream, &rows));
 
     ConfocalGatherParams p{};
     FBP_TRY(build_tables(ctx, in, laser_xyz, stream, &p.scan, &p.xs, &p.ys, &p.zs));
@@ -346,28 +519,34 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     p.Vx = Vx; p.Vy = Vy; p.Vz = Vz; p.L = L; p.T = T;
     p.t0 = in.time_offset;
     p.dt = in.time_step;
-    p.row_pitch = pitch;
-    p.slot_w = slot_w;
+    p.row_pitch = wp.pitch;
+    p.slot_w = wp.slot_w;
     p.ch = wp.ch;
-    const size_t smem = wp.smem;
+    if (smp) p.smp = *smp;
     dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(Vz, 4 * kWZ));
     const bool bounce = in.discard_first_last_bounces == 0;
-    const bool exact = in.time_offset > 0.f;
-    auto go = [&](auto kernel) -> fbp_status {
-        FBP_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kernel<<<grid, 32 * kWY * kWZ, smem, stream>>>(p);
-        FBP_CHECK_LAUNCH(ctx, "confocal_gather_kernel");
-        return FBP_OK;
-    };
-    if (bounce) {
-        if (exact) return go(confocal_gather_kernel<S, kKV, kWY, kWZ, true, true>);
-        return go(confocal_gather_kernel<S, kKV, kWY, kWZ, true, false>);
-    }
-    if (exact) return go(confocal_gather_kernel<S, kKV, kWY, kWZ, false, true>);
-    return go(confocal_gather_kernel<S, kKV, kWY, kWZ, false, false>);
+    if (smp) return dispatch_confocal<S, true>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
+    return dispatch_confocal<S, false>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
 }
 
 }  // namespace
+
+// Tile grid of the confocal gather (also the MIS sampling tiles).
+void confocal_tile_grid(const fbp_recon_info& in, uint32_t out[3]) {
+    out[0] = cdiv(in.voxel_res[0], kKV);
+    out[1] = cdiv(in.voxel_res[1], 8 * kWY);
+    out[2] = cdiv(in.voxel_res[2], 4 * kWZ);
+}
+
+fbp_status confocal_gather(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype, int layout,
+                           const float* laser_xyz, float* volume, cudaStream_t s, const SampleParams* smp) {
+    switch (dtype) {
+        case FBP_F32: return launch_confocal<float>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
+        case FBP_BF16: return launch_confocal<__nv_bfloat16>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
+        case FBP_F16: return launch_confocal<__half>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
+        default: return set_error(FBP_ERR_INVALID_ARG, "unknown dtype");
+    }
+}
 
 fbp_status build_tables(fbp_context* ctx, const fbp_recon_info& in, const float* laser_xyz, cudaStream_t stream,
                         const float4** scan, const float** xs, const float** ys, const float** zs) {
@@ -405,14 +584,16 @@ fbp_status plan_window(const fbp_context* ctx, double ex, double ey, double ez, 
     uint32_t slot_w = span < (double)cap ? ((uint32_t)std::ceil(span) + align - 1) / align * align : cap;
     if (slot_w > cap) slot_w = cap;
     out->slot_w = slot_w;
+    out->capped = slot_w == cap;
     out->pitch = t_round + slot_w;
     const size_t per_stage = (size_t)2 * (slot_w + align) * elem_bytes;  // double-buffered, per scan point
+    const size_t zero_slot = (size_t)(slot_w + align) * elem_bytes;
     int ch = 32;
-    while (ch > 1 && meta_bytes + (size_t)ch * per_stage > (size_t)ctx->smem_optin) ch >>= 1;
-    if (meta_bytes + (size_t)ch * per_stage > (size_t)ctx->smem_optin)
+    while (ch > 1 && meta_bytes + (size_t)ch * per_stage + zero_slot > (size_t)ctx->smem_optin) ch >>= 1;
+    if (meta_bytes + (size_t)ch * per_stage + zero_slot > (size_t)ctx->smem_optin)
         return set_error(FBP_ERR_UNSUPPORTED, std::string(who) + ": time-bin window too large for shared memory");
     out->ch = ch;
-    out->smem = meta_bytes + (size_t)ch * per_stage;
+    out->smem = meta_bytes + (size_t)ch * per_stage + zero_slot;
     return FBP_OK;
 }
 
@@ -449,13 +630,9 @@ extern "C" fbp_status fbp_backproject_confocal(fbp_context* ctx, const fbp_recon
     if (!cube || !laser_xyz || !volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: null buffer");
     if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
         return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: unknown layout");
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (dtype) {
-        case FBP_F32: return launch_confocal<float>(ctx, *info, cube, layout, laser_xyz, volume, s);
-        case FBP_BF16: return launch_confocal<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, volume, s);
-        case FBP_F16: return launch_confocal<__half>(ctx, *info, cube, layout, laser_xyz, volume, s);
-        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: unknown dtype");
-    }
+    if (dtype != FBP_F32 && dtype != FBP_BF16 && dtype != FBP_F16)
+        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: unknown dtype");
+    return confocal_gather(ctx, *info, cube, dtype, layout, laser_xyz, volume, (cudaStream_t)stream, nullptr);
 }
 
 // ------------------------------------------------------------ diagnostics --

@@ -104,6 +104,10 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(flo
 template <> __device__ __forceinline__ __half from_f32<__half>(float v) { return __float2half_rn(v); }
 
 inline size_t dtype_size(int dtype) { return dtype == FBP_F32 ? 4 : 2; }
+template <typename T> constexpr int dtype_of();
+template <> constexpr int dtype_of<float>() { return FBP_F32; }
+template <> constexpr int dtype_of<__nv_bfloat16>() { return FBP_BF16; }
+template <> constexpr int dtype_of<__half>() { return FBP_F16; }
 
 // ---------------------------------------------------- reference arithmetic --
 //

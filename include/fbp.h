@@ -138,6 +138,44 @@ fbp_status fbp_debug_exhaustive_bins(fbp_context* ctx, const fbp_recon_info* inf
                                      const float* sensor_xyz, const int64_t* voxel_idx, uint64_t num_voxels,
                                      int32_t* bins, void* stream);
 
+/* ---- sampled (MIS) backprojection ----------------------------------------- */
+
+typedef enum {
+    FBP_MIS_UNIFORM = 0,   /* unbiased, scan points uniform per voxel tile */
+    FBP_MIS_SPATIAL = 1,   /* unbiased, p(l) proportional to scan point l's total intensity */
+    FBP_MIS_LEARNED = 2,   /* unbiased, per-tile cluster distribution (e.g. from the MLP) */
+    FBP_MIS_REFERENCE = 3  /* the reference kernel's one-sample balance-heuristic MIS */
+} fbp_mis_proposal;
+
+typedef struct {
+    int proposal;            /* fbp_mis_proposal */
+    uint32_t samples;        /* per voxel tile (unbiased modes) or per voxel (REFERENCE; 0 = L/4) */
+    uint64_t seed;           /* unbiased modes: counter-based RNG seed */
+    const float* noise;      /* REFERENCE: device uniform buffer (NULL: numVoxels from std::mt19937) */
+    uint64_t noise_size;
+    const float* tile_cluster_cdf; /* LEARNED: device [tiles][G] inclusive CDF over scan clusters,
+                                      tiles in fbp_mis_tile_grid order (x fastest) */
+    uint32_t cluster_side;   /* LEARNED: clusters are cluster_side^2 blocks of the scan grid */
+    uint32_t scan_side;      /* LEARNED: scan grid side (L = scan_side^2, l = iz*side + ix) */
+} fbp_mis_params;
+
+/* Sampled confocal backprojection.  Replaces Laser::reconstructAABBConfocalMIS
+ * (Laser.cu:526-611), buildAliasTables (:253-315) and backprojectConfocalVoxelMIS
+ * (transient_reconstruction.cuh:194-260).  The unbiased modes estimate the full
+ * backprojection: every voxel tile draws `samples` scan points from the proposal
+ * and weights each by 1/(samples * p(l)).  REFERENCE keeps the reference's
+ * arithmetic and RNG (biased), with its spatial CDF built from the capture and
+ * samples summed in order per voxel. */
+fbp_status fbp_mis_backproject(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
+                               int layout, const float* laser_xyz, const fbp_mis_params* params, float* volume,
+                               void* stream);
+/* Diagnostic: the REFERENCE mode's proposal tables for this capture, copied
+ * to host arrays of L entries (normalised spatial CDF, alias, probability). */
+fbp_status fbp_mis_reference_tables(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
+                                    int layout, float* spatial_cdf, uint32_t* alias, float* prob, void* stream);
+/* Voxel tiles of the gather / MIS sampling: tiles[0..2] along (vx, vy, vz). */
+fbp_status fbp_mis_tile_grid(const fbp_recon_info* info, uint32_t tiles[3]);
+
 /* ---- post-processing ------------------------------------------------------ */
 
 typedef enum { FBP_FILTER_NONE = 0, FBP_FILTER_LAPLACIAN = 1, FBP_FILTER_LOG = 2, FBP_FILTER_LOG_FFT = 3 } fbp_filter;

@@ -1,0 +1,100 @@
+"""Sampled (MIS) backprojection: the reference's one-sample MIS arithmetic
+against its compiled kernel, and unbiasedness of the new estimators."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(n=16, T=512, vres=(24, 20, 28), seed=11):
+    from fasterbackprojection_gb300 import make_info, scenes
+
+    cap = scenes.confocal_points(n, T, 32e-12, n_points=60, seed=seed)
+    hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 2.4))
+    info = make_info(num_laser_targets=n * n, num_time_bins=T, time_step=cap.time_step, voxel_res=vres,
+                     hidden_min=hmin, voxel_size=vs)
+    return cap, info
+
+
+def test_reference_mis_matches_reference_kernel_one_sample(ctx, cuda):
+    """One sample per voxel (the reference kernel's += only races with more)."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE
+    from oracle import harness
+
+    if not harness.available():
+        pytest.skip("reference kernel harness not built")
+    harness.load()
+    cap, info = _case()
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    cdf, alias, prob = ctx.mis_reference_tables(info, cube)
+    assert cdf[0] == 0.0 and cdf[-1] == pytest.approx(1.0)
+    V = 24 * 20 * 28
+    noise = torch.rand(V, generator=torch.Generator().manual_seed(5)).to(cuda)
+    got = ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE, 1, noise=noise)
+    ref = harness.confocal_voxel_mis(info, cube.t().contiguous(), lx, torch.from_numpy(cdf).to(cuda), noise,
+                                     torch.from_numpy(alias.astype(np.int32)).to(cuda),
+                                     torch.from_numpy(prob).to(cuda), 1)
+    assert torch.equal(got, ref)
+
+
+def test_reference_mis_many_samples_is_deterministic(ctx, cuda):
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE
+
+    cap, info = _case()
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    a = ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE, 0)  # 0 = L/4 samples, default noise
+    b = ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE, 0)
+    assert torch.equal(a, b) and float(a.abs().max()) > 0
+
+
+@pytest.mark.parametrize("proposal", ["uniform", "spatial", "clusters"])
+def test_unbiased_estimators_converge_to_full_backprojection(ctx, cuda, proposal):
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_LEARNED, FBP_MIS_SPATIAL, FBP_MIS_UNIFORM
+    from fasterbackprojection_gb300.api import mis_tile_grid
+
+    cap, info = _case(seed=13)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    full = ctx.backproject_confocal(info, cube, lx).double()
+    kw = {}
+    mode = {"uniform": FBP_MIS_UNIFORM, "spatial": FBP_MIS_SPATIAL, "clusters": FBP_MIS_LEARNED}[proposal]
+    if proposal == "clusters":
+        tiles = mis_tile_grid(info)
+        G = 16  # 4 x 4 clusters of 4 x 4 scan points
+        rng = np.random.default_rng(0)
+        w = rng.uniform(0.2, 1.0, (int(np.prod(tiles)), G))
+        cdf = np.cumsum(w / w.sum(1, keepdims=True), axis=1).astype(np.float32)
+        cdf[:, -1] = 1.0
+        kw = dict(tile_cluster_cdf=torch.from_numpy(cdf).to(cuda), cluster_side=4, scan_side=16)
+    K = 64
+    runs = 200
+    acc = torch.zeros_like(full)
+    single = None
+    for r in range(runs):
+        est = ctx.mis_backproject(info, cube, lx, mode, K, seed=1000 + r, **kw).double()
+        if single is None:
+            single = rel_l2(est.cpu().numpy(), full.cpu().numpy())
+        acc += est
+    mean_err = rel_l2((acc / runs).cpu().numpy(), full.cpu().numpy())
+    # Averaging R independent unbiased estimates shrinks the error ~ 1/sqrt(R).
+    assert mean_err < 2.5 * single / np.sqrt(runs), (single, mean_err)
+
+
+def test_more_samples_lower_error(ctx, cuda):
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_SPATIAL
+
+    cap, info = _case(seed=17)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    full = ctx.backproject_confocal(info, cube, lx).cpu().numpy()
+    errs = [rel_l2(ctx.mis_backproject(info, cube, lx, FBP_MIS_SPATIAL, K, seed=3).cpu().numpy(), full)
+            for K in (16, 64, 256)]
+    assert errs[0] > errs[1] > errs[2]
