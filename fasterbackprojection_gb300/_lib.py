@@ -125,6 +125,7 @@ SIGNATURES = {
                                c_void_p]),
     "fbp_log_weights": (c_int, [c_int, c_float, POINTER(c_float)]),
     "fbp_normalize_minmax": (c_int, [c_void_p, c_void_p, c_uint64, c_void_p]),
+    "fbp_normalize_minmax_noalloc": (c_int, [c_void_p, c_uint64, c_void_p]),
     "fbp_filter_h": (c_int, [c_void_p, c_void_p, c_uint64, c_uint32, c_float, c_float, c_float, c_int, c_void_p]),
     "fbp_mis_backproject": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p,
                                     POINTER(MisParams), c_void_p, c_void_p]),

@@ -11,6 +11,7 @@
 #include "fbp_internal.cuh"
 
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 namespace fbp {
@@ -311,6 +312,68 @@ extern "C" fbp_status fbp_normalize_minmax(fbp_context* ctx, float* v, uint64_t 
     FBP_TRY(check_ctx(ctx));
     if (!v || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_normalize_minmax: null buffer or n == 0");
     return normalize_device(ctx, v, n, (cudaStream_t)stream);
+}
+
+// ------------------------------------------ allocation-free normalisation --
+//
+// fbp_normalize_minmax_noalloc: the same three passes as fbp_normalize_minmax,
+// but its scratch (one min/max pair per reduction block plus the final pair)
+// lives in this file-scope array instead of context workspace, so the call
+// allocates nothing and needs no fbp_context.  Every device that loads the
+// library holds the array (8 KiB) until the process exits.  One block reduces
+// up to 2^20 elements and there are at most 1024 partial slots, so inputs are
+// limited to 2^30 elements.  All calls on a device share the array: each call
+// overwrites every slot it reads before reading it, and two calls that overlap
+// on the GPU (different streams, no ordering between them) race on it.
+namespace fbp {
+constexpr int kNoAllocMaxBlocks = 1024;
+constexpr uint64_t kNoAllocElemsPerBlock = 1ull << 20;
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocMaxBlocks + 2];
+
+// Device address of g_noalloc_scratch, resolved once per device (host code
+// must not pass the symbol itself to a kernel: on the host it only names a
+// stand-in object).
+static std::mutex g_noalloc_mu;
+static float* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+static fbp_status noalloc_scratch(float** out) {
+    int dev = -1;
+    FBP_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return set_error(FBP_ERR_UNSUPPORTED, "fbp_normalize_minmax_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "fbp_normalize_minmax_noalloc: cudaGetSymbolAddress");
+        g_noalloc_addr[dev] = static_cast<float*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return FBP_OK;
+}
+}  // namespace fbp
+
+extern "C" fbp_status fbp_normalize_minmax_noalloc(float* v, uint64_t n, void* stream) {
+    clear_error();
+    if (!v || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_normalize_minmax_noalloc: null buffer or n == 0");
+    if (n > (uint64_t)kNoAllocMaxBlocks * kNoAllocElemsPerBlock)
+        return set_error(FBP_ERR_UNSUPPORTED,
+                         "fbp_normalize_minmax_noalloc: n exceeds 2^30 elements (the static scratch holds 1024 "
+                         "partial min/max pairs of 2^20 elements each); use fbp_normalize_minmax");
+    float* scratch = nullptr;
+    FBP_TRY(noalloc_scratch(&scratch));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nb = (int)((n + kNoAllocElemsPerBlock - 1) / kNoAllocElemsPerBlock);
+    float* mm = scratch + 2 * kNoAllocMaxBlocks;
+    minmax_partial_kernel<<<nb, kReduceThreads, 0, s>>>(v, n, scratch);
+    FBP_TRY_CUDA(cudaGetLastError());
+    minmax_final_kernel<<<1, kReduceThreads, 0, s>>>(scratch, nb, mm);
+    FBP_TRY_CUDA(cudaGetLastError());
+    const unsigned ab = (unsigned)std::min<uint64_t>(cdiv(n, 256), 1216);
+    normalize_apply_kernel<<<ab, 256, 0, s>>>(v, n, mm);
+    FBP_TRY_CUDA(cudaGetLastError());
+    return FBP_OK;
 }
 
 extern "C" fbp_status fbp_postfilter(fbp_context* ctx, int kind, int kernel_size, float sigma, const float* in,

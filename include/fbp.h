@@ -197,6 +197,17 @@ fbp_status fbp_log_weights(int size, float sigma, float* w);
  * in place, min/max reduced on the device. */
 fbp_status fbp_normalize_minmax(fbp_context* ctx, float* v, uint64_t n, void* stream);
 
+/* fbp_normalize_minmax without allocating: no counterpart in the reference.
+ * For callers that cannot let a library call cudaMalloc — an acquisition
+ * loop that reserves the whole device memory budget up front, or a host
+ * application whose own allocator owns every device byte.  Needs no
+ * context; its scratch is a fixed 8 KiB array inside libfbp on each device,
+ * so n is limited to 2^30 elements (FBP_ERR_UNSUPPORTED beyond).  The first
+ * call on a device looks up that array's device address; make that first call
+ * before any stream capture.  Calls that overlap on the GPU share the array
+ * and race; order them (one stream, or events). */
+fbp_status fbp_normalize_minmax_noalloc(float* v, uint64_t n, void* stream);
+
 /* ---- temporal filter ------------------------------------------------------ */
 
 typedef enum { FBP_BORDER_ZERO = 0, FBP_BORDER_EDGE = 1 } fbp_border;
