@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--size", choices=["full", "medium", "small"], default="full",
                     help="full: 256^2 scan -> 256^3 (the benchmark); medium: 128^2 -> 128^3 and small: 64^2 -> 64^3 "
                          "(profiling and plumbing checks)")
-    ap.add_argument("--no-extras", action="store_true", help="skip bf16 / reference-CUDA / CPU legs")
+    ap.add_argument("--no-extras", action="store_true", help="skip bf16 / reference-CUDA / CPU / batched legs")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-capture batched leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     a = ap.parse_args()
     a.small = a.size != "full"
@@ -304,6 +305,10 @@ def run_ours(args):
                                   "achieved_gbs_2B_per_sample": samples * 2 / (bf_ms / 1e3) / 1e9}
         del cube16
         extras["reference_cuda"] = reference_cuda_rate(info, cube, lx, dev)
+        ctx.backproject_confocal(info, cube, lx, out=vol)
+        extras["error_vs_fp64"] = fp64_error(ctx, info, cube, lx, vol)
+        if not args.no_batch:
+            extras["batched"] = batched_leg(ctx, dev, 2)
 
     peak, peak_kind = measured_peaks()
     achieved = samples * 4 / (bp_ms / 1e3) / 1e9
@@ -364,6 +369,119 @@ def reference_cuda_rate(info, cube, lx, dev):
     del cube_tm
     return {"kernel": "backprojectConfocalVoxel (reference, sm_103a, fast math)", "value": samples / (ms / 1e3),
             "unit": UNIT, "sample": f"{nz} of {info.voxel_res[2]} depth slices", "ms": ms}
+
+
+def fp64_error(ctx, info, cube, lx, vol, nvox=512, seed=5):
+    """rel-L2 of a gathered volume against the FP64 oracle over a random voxel
+    sample: with the oracle's own FP64 bins, and with the GPU's bins (which
+    isolates the accumulation).  cube is the device cube the gather read."""
+    import numpy as np
+    import torch
+    from oracle import cpu
+
+    V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(V, size=min(nvox, V), replace=False)).astype(np.int64)
+    idx_t = torch.from_numpy(idx).to(lx.device)
+    bins = ctx.debug_confocal_bins(info, lx, idx_t).cpu().numpy()
+    host = cube.float().cpu().numpy()
+    lxn = lx.cpu().numpy()
+    got = vol.reshape(-1)[idx_t].double().cpu().numpy()
+    want64 = cpu.confocal_voxel_subset(info, host, lxn, idx)
+    want_same = cpu.confocal_voxel_subset(info, host, lxn, idx, bins=bins)
+
+    def rel(a, b):
+        nb = float(np.linalg.norm(b))
+        return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+    return {"rel_l2_vs_fp64": rel(got, want64), "rel_l2_vs_fp64_same_bins": rel(got, want_same),
+            "voxels": int(idx.shape[0])}
+
+
+def batched_leg(ctx, dev, steps):
+    """64 confocal captures of uneven sizes (scan N in {32,64,128,256}^2, bins
+    in {256..2048} over the same 16.4 ns window, volume N^3, BF16 storage)
+    reconstructed by one persistent launch replayed from a CUDA graph, tile
+    shape chosen by the autotuner.  Per-capture error vs FP64 on 128 voxels."""
+    import numpy as np
+    import torch
+
+    from fasterbackprojection_gb300 import FBP_LAYOUT_TIME_INNER, Batch, make_info, scenes
+    from oracle import cpu
+
+    caps, errs_in = [], []
+    for c in scenes.batched_configs(seed0=100, count=64):
+        n, T, vres = c["n"], c["T"], c["vres"]
+        cap = scenes.confocal_patches_torch(n, T, DT * N_BINS / T, seed=c["seed"], device=dev)
+        hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 1.5))
+        info = make_info(num_laser_targets=n * n, num_time_bins=T, time_step=cap.time_step, voxel_res=vres,
+                         hidden_min=hmin, voxel_size=vs)
+        cube16 = cap.cube.to(torch.bfloat16).contiguous()
+        lx = cap.laser_xyz.contiguous()
+        V = vres[0] * vres[1] * vres[2]
+        idx = np.sort(np.random.default_rng(c["seed"]).choice(V, size=min(128, V), replace=False)).astype(np.int64)
+        idx_t = torch.from_numpy(idx).to(dev)
+        bins = ctx.debug_confocal_bins(info, lx, idx_t).cpu().numpy()
+        lxn = lx.cpu().numpy()
+        dec = cube16.float().cpu().numpy()
+        want64 = cpu.confocal_voxel_subset(info, dec, lxn, idx)
+        want_same = cpu.confocal_voxel_subset(info, dec, lxn, idx, bins=bins)
+        want_f32 = cpu.confocal_voxel_subset(info, cap.cube.cpu().numpy(), lxn, idx)
+        del cap, dec
+        vol = torch.empty((vres[2], vres[1], vres[0]), device=dev)
+        caps.append((info, cube16, lx, vol, FBP_LAYOUT_TIME_INNER))
+        errs_in.append((idx_t, want64, want_same, want_f32))
+    samples = sum(c[0].num_laser_targets * c[0].voxel_res[0] * c[0].voxel_res[1] * c[0].voxel_res[2] for c in caps)
+    b = Batch(ctx, caps)
+    s = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(s):
+        chosen = b.autotune(stream=s)
+        b.run(use_graph=True, stream=s)  # capture + first replay (warm-up)
+        s.synchronize()
+        ctx.check_device_status(stream=s)
+        launches0 = ctx.launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(steps):
+            b.run(use_graph=True, stream=s)
+        e1.record(s)
+        s.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        launches = (ctx.launches - launches0) // steps
+        # The same captures one after another through the single-capture call.
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tmp = [torch.empty_like(c[3]) for c in caps]
+        q0.record(s)
+        for c, t in zip(caps, tmp):
+            ctx.backproject_confocal(c[0], c[1], c[2], out=t, stream=s)
+        q1.record(s)
+        s.synchronize()
+        seq_ms = q0.elapsed_time(q1)
+    same_as_single = all(torch.equal(c[3], t) for c, t in zip(caps, tmp)) if chosen == 0 else None
+    del tmp
+
+    def rel(a, b_):
+        nb = float(np.linalg.norm(b_))
+        return float(np.linalg.norm(a - b_) / (nb if nb > 0 else 1.0))
+
+    per = []
+    for c, (idx_t, w64, wsame, wf32) in zip(caps, errs_in):
+        got = c[3].reshape(-1)[idx_t].double().cpu().numpy()
+        per.append((rel(got, w64), rel(got, wsame), rel(got, wf32)))
+    b.close()
+    sizes = [f"{int(round(c[0].num_laser_targets ** 0.5))}^2x{c[0].num_time_bins}" for c in caps]
+    return {
+        "workload": "64 confocal captures, scan {32,64,128,256}^2, bins {256,512,1024,2048}, volume N^3, bf16",
+        "captures": len(caps), "samples_per_step": samples, "ms_per_step": ms, "value": samples / (ms / 1e3),
+        "unit": UNIT, "steps": steps, "graph": True, "autotuned_tile": chosen, "gpu_launches_per_step": launches,
+        "sequential_single_capture_ms": seq_ms, "tile0_equals_single_capture": same_as_single,
+        "max_rel_l2_vs_fp64": max(p[0] for p in per), "max_rel_l2_vs_fp64_same_bins": max(p[1] for p in per),
+        "max_rel_l2_vs_fp32_cube": max(p[2] for p in per),
+        "per_capture": [{"capture": z, "rel_l2_vs_fp64": round(p[0], 9), "rel_l2_vs_fp32_cube": round(p[2], 6)}
+                        for z, p in zip(sizes, per)],
+        "error_sample": "128 random voxels per capture; FP64 oracle on the decoded BF16 cube (vs_fp64) and on "
+                        "the FP32 cube before rounding (vs_fp32_cube, includes the storage rounding)",
+    }
 
 
 def cpu_baseline(info, cube, lx):

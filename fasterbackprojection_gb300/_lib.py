@@ -102,6 +102,19 @@ class ShapeParams(ctypes.Structure):
     ]
 
 
+class CaptureDesc(ctypes.Structure):
+    """fbp_capture_desc: one capture of a batch."""
+
+    _fields_ = [
+        ("info", ReconInfo),
+        ("cube", c_void_p),
+        ("dtype", c_int),
+        ("layout", c_int),
+        ("laser_xyz", c_void_p),
+        ("volume", c_void_p),
+    ]
+
+
 # (name, restype, argtypes) for every symbol include/fbp.h declares.
 SIGNATURES = {
     "fbp_version": (c_char_p, []),
@@ -133,6 +146,11 @@ SIGNATURES = {
                                          c_void_p, c_void_p]),
     "fbp_mis_tile_grid": (c_int, [POINTER(ReconInfo), POINTER(c_uint32)]),
     "fbp_lct": (c_int, [c_void_p, c_void_p, c_int, c_uint32, c_uint32, POINTER(LctParams), c_void_p, c_void_p]),
+    "fbp_batch_create": (c_int, [c_void_p, c_uint32, POINTER(CaptureDesc), POINTER(c_void_p)]),
+    "fbp_batch_run": (c_int, [c_void_p, c_int, c_void_p]),
+    "fbp_batch_autotune": (c_int, [c_void_p, c_void_p, POINTER(c_int)]),
+    "fbp_batch_set_config": (c_int, [c_void_p, c_int, c_void_p]),
+    "fbp_batch_destroy": (c_int, [c_void_p]),
     "fbp_reconstruct_shape_host": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_void_p, c_void_p,
                                            POINTER(ShapeParams), c_void_p, c_void_p]),
 }

@@ -12,7 +12,7 @@ from ctypes import byref, c_double, c_float, c_void_p
 import numpy as np
 
 from . import _lib
-from ._lib import LctParams, MisParams, ReconInfo, ShapeParams, check, load
+from ._lib import CaptureDesc, LctParams, MisParams, ReconInfo, ShapeParams, check, load
 
 
 def make_info(*, num_laser_targets: int, num_time_bins: int, time_step: float, voxel_res, hidden_min, voxel_size,
@@ -254,6 +254,55 @@ class Context:
             c_void_p(0 if sens is None else sens.ctypes.data), byref(params), c_void_p(out.ctypes.data),
             self._stream(stream)))
         return out
+
+
+class Batch:
+    """Many confocal captures reconstructed together (fbp_batch_*).
+
+    ``captures`` is a list of (info, cube, laser_xyz, volume, layout) with
+    CUDA tensors; they are referenced, not copied, and must outlive the batch.
+    Every ``run`` re-reads each cube and overwrites each volume.
+    """
+
+    def __init__(self, ctx: Context, captures):
+        self._lib = ctx._lib
+        self._ctx = ctx
+        self._keep = []
+        descs = (CaptureDesc * len(captures))()
+        for i, (info, cube, laser_xyz, volume, layout) in enumerate(captures):
+            d = descs[i]
+            d.info = info
+            d.cube = _ptr(cube).value
+            d.dtype = _dtype_code(cube)
+            d.layout = layout
+            d.laser_xyz = _ptr(laser_xyz).value
+            d.volume = _ptr(volume).value
+            self._keep.append((cube, laser_xyz, volume))
+        h = c_void_p()
+        check(self._lib.fbp_batch_create(ctx._h, len(captures), descs, byref(h)))
+        self._h = h
+
+    def run(self, use_graph: bool = False, stream=None) -> None:
+        check(self._lib.fbp_batch_run(self._h, int(use_graph), Context._stream(stream)))
+
+    def autotune(self, stream=None) -> int:
+        chosen = ctypes.c_int(-1)
+        check(self._lib.fbp_batch_autotune(self._h, Context._stream(stream), byref(chosen)))
+        return chosen.value
+
+    def set_config(self, config: int, stream=None) -> None:
+        check(self._lib.fbp_batch_set_config(self._h, config, Context._stream(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.fbp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def mis_tile_grid(info: ReconInfo):

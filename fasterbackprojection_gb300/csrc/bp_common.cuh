@@ -90,6 +90,15 @@ fbp_status confocal_gather(fbp_context* ctx, const fbp_recon_info& in, const voi
                            const float* laser_xyz, float* volume, cudaStream_t s, const SampleParams* smp);
 void confocal_tile_grid(const fbp_recon_info& in, uint32_t out[3]);
 
+// Padded, thresholded rows [L][pitch] of a confocal cube, written to dst.
+template <typename S>
+fbp_status prepare_rows_into(fbp_context* ctx, const void* cube, int layout, uint32_t L, uint32_t T, uint32_t pitch,
+                             S* dst, cudaStream_t stream);
+
+__global__ void axis_tables_kernel(float* __restrict__ xs, float* __restrict__ ys, float* __restrict__ zs,
+                                   uint32_t Vx, uint32_t Vy, uint32_t Vz, float mnx, float mny, float mnz, float sx,
+                                   float sy, float sz);
+
 // Shared host helpers.
 fbp_status build_tables(fbp_context* ctx, const fbp_recon_info& in, const float* laser_xyz, cudaStream_t stream,
                         const float4** scan, const float** xs, const float** ys, const float** zs);

@@ -17,6 +17,7 @@
 //   axes   xs[Vx], ys[Vz], zs[Vy]         voxel-centre coordinates
 #include "fbp_internal.cuh"
 #include "bp_common.cuh"
+#include "bp_gather.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -99,348 +100,11 @@ __global__ void rows_zero_tail_kernel(S* __restrict__ rows, uint32_t L, uint32_t
         rows[(i / w) * pitch + from + (i % w)] = from_f32<S>(0.f);
 }
 
-// ----------------------------------------------------------- gather kernel --
-
-// Arithmetic paths of the pair loop (all reproduce the reference's bins):
-//   PATH_2D     time_offset == 0, no bounce terms: dist = 2d exactly, so
-//               x = d * (2 rcp(dt)) and the weight is rcp(d^2) = 4 rcp(dist^2);
-//               the stage's partial sum is scaled by 1/4 (exact).
-//   PATH_FAST   time_offset <= 0 (every path >= 0): dist = fma(d, 2, -t0) [+ bounce].
-//   PATH_EXACT  time_offset > 0: negative paths possible, bin by conversion.
-// In PATH_2D / PATH_FAST the bin is floor(x) - a via a round-toward-zero add of
-// 2^23 - a; without CLAMP the window planner guarantees every bin of the tile
-// lies inside its window, so the -2^23 bias folds into the shared-memory base.
-enum { PATH_2D = 0, PATH_FAST = 1, PATH_EXACT = 2 };
-
-template <typename S>
-__device__ __forceinline__ float lds_elem(uint32_t addr);
-template <>
-__device__ __forceinline__ float lds_elem<float>(uint32_t addr) {
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
-    return v;
-}
-template <>
-__device__ __forceinline__ float lds_elem<__nv_bfloat16>(uint32_t addr) {
-    unsigned short v;
-    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr));
-    return __uint_as_float((uint32_t)v << 16);
-}
-template <>
-__device__ __forceinline__ float lds_elem<__half>(uint32_t addr) {
-    unsigned short v;
-    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(addr));
-    return __half2float(__ushort_as_half(v));
-}
-
-template <typename S> struct ElemShift;
-template <> struct ElemShift<float> { static constexpr int value = 2; };
-template <> struct ElemShift<__nv_bfloat16> { static constexpr int value = 1; };
-template <> struct ElemShift<__half> { static constexpr int value = 1; };
-
-// One staged stage of scan points against a thread's KV voxels (consecutive
-// along x, sharing the y/z offsets).
-template <typename S, int KV, int PATH, bool BOUNCE, bool CLAMP, bool SAFE, bool WEIGHTED>
-__device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, const int2* __restrict__ meta,
-                                               const float* __restrict__ wts, int nl, const float (&px)[KV], float py,
-                                               float pz, float neg_t0, float rcp_dt, uint32_t slot_w,
-                                               float (&acc)[KV]) {
-    constexpr int SH = ElemShift<S>::value;
-    const float rcp2 = 2.f * rcp_dt;  // exact
-#pragma unroll 2
-    for (int i = 0; i < nl; ++i) {
-        const float4 g = geo[i];
-        const int2 m = meta[i];  // (bin bias: float 2^23 - a, or a; slot shared address)
-        const float wl = WEIGHTED ? wts[i] : 1.f;
-        const float dy = sub_rn(py, g.y), dz = sub_rn(pz, g.z);
-        const float dy2 = mul_rn(dy, dy);
-#pragma unroll
-        for (int k = 0; k < KV; ++k) {
-            const float dx = sub_rn(px[k], g.x);
-            const float d = sqrt_approx(fma_rn(dz, dz, fma_rn(dx, dx, dy2)));
-            float x, dist = 0.f;
-            if (PATH == PATH_2D && !SAFE) {
-                x = mul_rn(d, rcp2);
-            } else {
-                dist = fma_rn(d, 2.f, neg_t0);
-                if (BOUNCE) dist = add_rn(dist, g.w);
-                x = ref_bin_ratio(dist, rcp_dt);
-            }
-            uint32_t addr;
-            if (PATH == PATH_EXACT) {
-                const int b = __float2int_rz(x);  // static_cast<int>, like the reference
-                addr = (uint32_t)m.y + (min((uint32_t)(b - m.x), slot_w) << SH);
-            } else {
-                const uint32_t bits = __float_as_uint(add_rz(x, __int_as_float(m.x)));
-                if (CLAMP) addr = (uint32_t)m.y + (min(bits - 0x4B000000u, slot_w) << SH);
-                else addr = (uint32_t)m.y + (bits << SH);  // bias folded into m.y
-            }
-            float I = lds_elem<S>(addr);
-            if (WEIGHTED) I *= wl;
-            float w;
-            if (PATH == PATH_2D && !SAFE) w = rcp_approx(mul_rn(d, d));
-            else w = SAFE ? ref_safe_rcp(mul_rn(dist, dist)) : rcp_approx(mul_rn(dist, dist));
-            acc[k] = fmaf(I, w, acc[k]);
-        }
-    }
-}
-
-// The main kernel.  One CTA of 32*WY*WZ threads owns a tile of KV (x) x 8*WY
-// (rows) x 4*WZ (depth slices) voxels; a warp covers 8 rows x 4 slices, a
-// thread KV consecutive voxels along x.  Scan points (or, SAMPLED, K scan
-// points drawn per tile) are walked in stages of up to 32: one warp plans the
-// bin windows of the stage, all threads copy them from the padded rows into
-// shared memory with cp.async (double buffered), then every thread runs the
-// pair loop against the staged windows.  FP32 partials per stage, Kahan
-// across stages.
-template <typename S, int KV, int WY, int WZ, int PATH, bool BOUNCE, bool SAMPLED, bool CLAMP>
-__global__ void __launch_bounds__(32 * WY * WZ)
-confocal_gather_kernel(ConfocalGatherParams p) {
-    constexpr int NT = 32 * WY * WZ;
-    constexpr int CHMAX = 32;
-    constexpr int ALIGN = 16 / sizeof(S);  // elements per 16-byte copy
-    constexpr int SH = ElemShift<S>::value;
-    constexpr int TY = 8 * WY, TZ = 4 * WZ;
-    const int CH = p.ch;
-
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const uint32_t slot_stride = p.slot_w + ALIGN;  // sentinel element(s) at slot_w
-    float4* s_geo = reinterpret_cast<float4*>(smem_raw);         // [2][CHMAX]
-    int2* s_meta = reinterpret_cast<int2*>(s_geo + 2 * CHMAX);   // [2][CHMAX]
-    int* s_cnt = reinterpret_cast<int*>(s_meta + 2 * CHMAX);     // [2][CHMAX]
-    int* s_src = s_cnt + 2 * CHMAX;                              // [2][CHMAX]
-    int* s_row = s_src + 2 * CHMAX;                              // [2][CHMAX]
-    float* s_w = reinterpret_cast<float*>(s_row + 2 * CHMAX);    // [2][CHMAX]
-    int* s_flag = reinterpret_cast<int*>(s_w + 2 * CHMAX);       // [2]
-    const size_t slots_off = ConfocalGatherParams::meta_bytes(CHMAX);
-    S* s_slots = reinterpret_cast<S*>(smem_raw + slots_off);     // [2][CH][slot_stride], then the zero slot
-    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem_raw);
-    const uint32_t zero_slot = 2u * CH * slot_stride;            // element index of the all-zero slot
-
-    const int tid = threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5;
-    const int wy = warp % WY, wz = warp / WY;
-
-    const uint32_t tx0 = blockIdx.x * KV, ty0 = blockIdx.y * TY, tz0 = blockIdx.z * TZ;
-    const uint32_t vy = ty0 + wy * 8 + (lane & 7);
-    const uint32_t vz = tz0 + wz * 4 + (lane >> 3);
-    const bool row_ok = vy < p.Vy && vz < p.Vz;
-
-    // Tile AABB of voxel centres (clamped to the volume).
-    const uint32_t tx1 = min(tx0 + KV, p.Vx) - 1, ty1 = min(ty0 + TY, p.Vy) - 1, tz1 = min(tz0 + TZ, p.Vz) - 1;
-    const float bx0 = fminf(p.xs[tx0], p.xs[tx1]), bx1 = fmaxf(p.xs[tx0], p.xs[tx1]);
-    const float by0 = fminf(p.ys[tz0], p.ys[tz1]), by1 = fmaxf(p.ys[tz0], p.ys[tz1]);
-    const float bz0 = fminf(p.zs[ty0], p.zs[ty1]), bz1 = fmaxf(p.zs[ty0], p.zs[ty1]);
-
-    const float py = p.ys[min(vz, p.Vz - 1)];
-    const float pz = p.zs[min(vy, p.Vy - 1)];
-    float px[KV];
-#pragma unroll
-    for (int k = 0; k < KV; ++k) px[k] = p.xs[min(tx0 + k, p.Vx - 1)];
-
-    const float rcp_dt = rcp_approx(p.dt);
-    const float neg_t0 = -p.t0;
-
-    // Sentinels of every slot and the whole zero slot.
-    for (int i = tid; i < 2 * CH * ALIGN; i += NT) {
-        const int slot = i / ALIGN, e = i % ALIGN;
-        s_slots[(size_t)slot * slot_stride + p.slot_w + e] = from_f32<S>(0.f);
-    }
-    for (uint32_t i = tid; i < slot_stride; i += NT) s_slots[zero_slot + i] = from_f32<S>(0.f);
-
-    const uint32_t nitems = SAMPLED ? p.smp.K : p.L;
-    const uint32_t nchunks = (nitems + CH - 1) / CH;
-    const unsigned long long tile_id =
-        ((unsigned long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-
-    // Plan a stage: bin window of each scan point (threads < CH, all in warp 0).
-    auto plan_chunk = [&](uint32_t c, int buf) {
-        if (tid < CH) {
-            const uint32_t item = c * CH + tid;
-            uint32_t l = item;
-            float wgt = 1.f;
-            if (SAMPLED && item < nitems) {
-                const float u1 = hash_uniform(p.smp.seed, tile_id, item, 0);
-                const float u2 = hash_uniform(p.smp.seed, tile_id, item, 1);
-                float pl;
-                if (p.smp.mode == SAMPLE_UNIFORM) {
-                    l = min((uint32_t)(u1 * (float)p.L), p.L - 1);
-                    pl = 1.f / (float)p.L;
-                } else if (p.smp.mode == SAMPLE_ALIAS) {
-                    const uint32_t kk = min((uint32_t)(u1 * (float)p.L), p.L - 1);
-                    l = u2 < p.smp.prob[kk] ? kk : p.smp.alias[kk];
-                    pl = p.smp.pl[l];
-                } else {
-                    // Cluster from the tile's CDF (binary search), then uniform inside it.
-                    const float* cdf = p.smp.tile_cdf + tile_id * p.smp.G;
-                    uint32_t lo = 0, hi = p.smp.G - 1;
-                    while (lo < hi) {
-                        const uint32_t mid = (lo + hi) >> 1;
-                        if (u1 < cdf[mid]) hi = mid; else lo = mid + 1;
-                    }
-                    const float pc = cdf[lo] - (lo > 0 ? cdf[lo - 1] : 0.f);
-                    const uint32_t cs = p.smp.cluster_side, cpr = (p.smp.n_side + cs - 1) / cs;
-                    const uint32_t cx = lo % cpr, cz = lo / cpr;
-                    const uint32_t w0 = min(cs, p.smp.n_side - cx * cs), h0 = min(cs, p.smp.n_side - cz * cs);
-                    const uint32_t inner = min((uint32_t)(u2 * (float)(w0 * h0)), w0 * h0 - 1);
-                    l = (cz * cs + inner / w0) * p.smp.n_side + cx * cs + inner % w0;
-                    pl = pc / (float)(w0 * h0);
-                }
-                wgt = pl > 0.f ? 1.f / ((float)nitems * pl) : 0.f;
-            }
-            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-            int cnt = 0, src = 0, near = 0, a = 0;
-            bool skip = true;
-            if (item < nitems && l < p.L) {
-                g = p.scan[l];
-                // Nearest and farthest voxel-centre distance of the tile.
-                const float cx = fminf(fmaxf(g.x, bx0), bx1), cy = fminf(fmaxf(g.y, by0), by1),
-                            cz = fminf(fmaxf(g.z, bz0), bz1);
-                const float dmin = sqrtf((g.x - cx) * (g.x - cx) + (g.y - cy) * (g.y - cy) + (g.z - cz) * (g.z - cz));
-                const float fx = fmaxf(fabsf(g.x - bx0), fabsf(g.x - bx1)), fy = fmaxf(fabsf(g.y - by0), fabsf(g.y - by1)),
-                            fz = fmaxf(fabsf(g.z - bz0), fabsf(g.z - bz1));
-                const float dmax = sqrtf(fx * fx + fy * fy + fz * fz);
-                const float bnc = BOUNCE ? g.w : 0.f;
-                const float pmin = 2.f * dmin + neg_t0 + bnc, pmax = 2.f * dmax + neg_t0 + bnc;
-                // Paths this short make dist^2 <= EPS possible: use safeRCP's branch.
-                near = pmin < 0.0035f;
-                // Conservative bin range with a 2-bin margin for rounding.
-                const int blo = (int)fmaxf(fminf(floorf(pmin * rcp_dt), 1.0e9f), -1.0e9f) - 2;
-                const int bhi = (int)fmaxf(fminf(floorf(pmax * rcp_dt), 1.0e9f), -1.0e9f) + 2;
-                a = max(blo, 0) & ~(ALIGN - 1);
-                skip = bhi < 0 || blo >= (int)p.T;  // no bin of this tile is inside [0, T)
-                if (!skip) {
-                    if (CLAMP) a = min(a, (int)(p.row_pitch - p.slot_w));
-                    const int hi = min(bhi + 1, (int)p.row_pitch);
-                    cnt = (max(hi - a, 0) + ALIGN - 1) & ~(ALIGN - 1);
-                    if (cnt > (int)p.slot_w) {
-                        if (CLAMP) {
-                            // Capped window: bins past it map to the sentinel; only an
-                            // uncovered valid bin would be an error.
-                            if (min(bhi + 1, (int)p.T) - a > (int)p.slot_w) atomicExch(p.status, (int)FBP_ERR_DEVICE);
-                            cnt = (int)p.slot_w;
-                        } else {
-                            // The planner's span bound failed: read zeros, report.
-                            atomicExch(p.status, (int)FBP_ERR_DEVICE);
-                            skip = true;
-                            cnt = 0;
-                        }
-                    }
-                    src = a;
-                }
-            }
-            // Slot of this scan point (or the zero slot) as a shared address.
-            const uint32_t slot_elem = skip ? zero_slot : (uint32_t)(buf * CH + tid) * slot_stride;
-            uint32_t saddr = sbase + (uint32_t)slots_off + (slot_elem << SH);
-            int bias;
-            if (PATH == PATH_EXACT) {
-                bias = a;
-            } else {
-                bias = __float_as_int((float)(8388608 - a));
-                if (!CLAMP) saddr -= (0x4B000000u << SH);
-            }
-            if (item >= nitems || l >= p.L) {
-                // Beyond the last scan point: x + 0 < 2^23 lands on the sentinel
-                // (CLAMP) or, unclamped, reads the zero slot at index 0.
-                bias = PATH == PATH_EXACT ? 0x40000000 : 0;
-                saddr = sbase + (uint32_t)slots_off + (zero_slot << SH);
-                if (!CLAMP && PATH != PATH_EXACT) saddr -= (__float_as_uint(0.f) << SH);
-                g = make_float4(3.0e18f, 3.0e18f, 3.0e18f, 0.f);  // far away: x is huge
-                wgt = 0.f;
-            }
-            s_geo[buf * CHMAX + tid] = g;
-            s_meta[buf * CHMAX + tid] = make_int2(bias, (int)saddr);
-            s_cnt[buf * CHMAX + tid] = cnt;
-            s_src[buf * CHMAX + tid] = src;
-            s_row[buf * CHMAX + tid] = (int)l;
-            s_w[buf * CHMAX + tid] = wgt;
-            const unsigned any_near = __ballot_sync(CH >= 32 ? 0xffffffffu : ((1u << CH) - 1u), near);
-            if (tid == 0) s_flag[buf] = any_near != 0;
-        }
-    };
-
-    // Copy a stage's windows (all threads).
-    auto copy_chunk = [&](int buf) {
-        const uint32_t vecs_per_slot = p.slot_w / ALIGN;
-        for (uint32_t i = tid; i < CH * vecs_per_slot; i += NT) {
-            const uint32_t s = i / vecs_per_slot, j = i - s * vecs_per_slot;
-            if ((int)(j * ALIGN) < s_cnt[buf * CHMAX + s]) {
-                const uint32_t l = (uint32_t)s_row[buf * CHMAX + s];
-                const S* src = static_cast<const S*>(p.rows) + (size_t)l * p.row_pitch + s_src[buf * CHMAX + s] + j * ALIGN;
-                S* dst = s_slots + (size_t)(buf * CH + s) * slot_stride + j * ALIGN;
-                cp_async_16(dst, src);
-            }
-        }
-        cp_async_commit();
-    };
-
-    float acc[KV], ksum[KV], kcomp[KV];
-#pragma unroll
-    for (int k = 0; k < KV; ++k) acc[k] = ksum[k] = kcomp[k] = 0.f;
-
-    if (nchunks > 0) {
-        plan_chunk(0, 0);
-        __syncthreads();
-        copy_chunk(0);
-    }
-
-    for (uint32_t c = 0; c < nchunks; ++c) {
-        const int buf = c & 1;
-        __syncthreads();  // every thread is done with stage c-1, whose buffers plan(c+1) reuses
-        if (c + 1 < nchunks) plan_chunk(c + 1, buf ^ 1);
-        __syncthreads();  // plan(c+1) visible to the copy loop
-        if (c + 1 < nchunks) {
-            copy_chunk(buf ^ 1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
-        __syncthreads();  // stage c's windows visible
-
-        const float4* geo = s_geo + buf * CHMAX;
-        const int2* meta = s_meta + buf * CHMAX;
-        const float* wts = s_w + buf * CHMAX;
-        const bool safe = s_flag[buf] != 0;
-        const int nl = (int)min((uint32_t)CH, nitems - c * CH);
-        float scale = 1.f;
-        if (!safe) {
-            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, false, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
-                                                                        p.slot_w, acc);
-            if (PATH == PATH_2D) scale = 0.25f;  // w was rcp(d^2) = 4 rcp(dist^2)
-        } else {
-            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, true, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
-                                                                       p.slot_w, acc);
-        }
-
-        // Compensated (Kahan) fold of this stage's partial sums.
-#pragma unroll
-        for (int k = 0; k < KV; ++k) {
-            const float y = sub_rn(mul_rn(acc[k], scale), kcomp[k]);
-            const float t = add_rn(ksum[k], y);
-            kcomp[k] = sub_rn(sub_rn(t, ksum[k]), y);
-            ksum[k] = t;
-            acc[k] = 0.f;
-        }
-    }
-
-    if (row_ok) {
-        float* out = p.volume + ((size_t)vz * p.Vy + vy) * p.Vx + tx0;
-#pragma unroll
-        for (int k = 0; k < KV; ++k)
-            if (tx0 + k < p.Vx) out[k] = ksum[k];
-    }
-}
-
 // ------------------------------------------------------------ host driver --
 
-namespace {
-
 template <typename S>
-fbp_status prepare_rows(fbp_context* ctx, const void* cube, int layout, uint32_t L, uint32_t T, uint32_t pitch,
-                        cudaStream_t stream, S** rows_out) {
-    void* rows = nullptr;
-    FBP_TRY(workspace(ctx, WS_CUBE_ROWS, (size_t)L * pitch * sizeof(S), stream, &rows));
-    S* r = static_cast<S*>(rows);
+fbp_status prepare_rows_into(fbp_context* ctx, const void* cube, int layout, uint32_t L, uint32_t T, uint32_t pitch,
+                             S* r, cudaStream_t stream) {
     const S* c = static_cast<const S*>(cube);
     if (layout == FBP_LAYOUT_TIME_INNER) {
         const uint64_t n = (uint64_t)L * pitch;
@@ -459,8 +123,24 @@ fbp_status prepare_rows(fbp_context* ctx, const void* cube, int layout, uint32_t
             FBP_CHECK_LAUNCH(ctx, "rows_zero_tail_kernel");
         }
     }
-    *rows_out = r;
     return FBP_OK;
+}
+template fbp_status prepare_rows_into<float>(fbp_context*, const void*, int, uint32_t, uint32_t, uint32_t, float*,
+                                             cudaStream_t);
+template fbp_status prepare_rows_into<__nv_bfloat16>(fbp_context*, const void*, int, uint32_t, uint32_t, uint32_t,
+                                                     __nv_bfloat16*, cudaStream_t);
+template fbp_status prepare_rows_into<__half>(fbp_context*, const void*, int, uint32_t, uint32_t, uint32_t, __half*,
+                                              cudaStream_t);
+
+namespace {
+
+template <typename S>
+fbp_status prepare_rows(fbp_context* ctx, const void* cube, int layout, uint32_t L, uint32_t T, uint32_t pitch,
+                        cudaStream_t stream, S** rows_out) {
+    void* rows = nullptr;
+    FBP_TRY(workspace(ctx, WS_CUBE_ROWS, (size_t)L * pitch * sizeof(S), stream, &rows));
+    *rows_out = static_cast<S*>(rows);
+    return prepare_rows_into<S>(ctx, cube, layout, L, T, pitch, *rows_out, stream);
 }
 
 constexpr int kKV = 8, kWY = 2, kWZ = 4;

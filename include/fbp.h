@@ -176,6 +176,37 @@ fbp_status fbp_mis_reference_tables(fbp_context* ctx, const fbp_recon_info* info
 /* Voxel tiles of the gather / MIS sampling: tiles[0..2] along (vx, vy, vz). */
 fbp_status fbp_mis_tile_grid(const fbp_recon_info* info, uint32_t tiles[3]);
 
+/* ---- batched reconstruction ---------------------------------------------- */
+
+/* One confocal capture of a batch (all captures of a batch share `dtype`). */
+typedef struct {
+    fbp_recon_info info;    /* geometry, by value */
+    const void* cube;       /* device, L*T elements in `layout` */
+    int dtype;              /* fbp_dtype */
+    int layout;             /* fbp_layout */
+    const float* laser_xyz; /* device, L*3 */
+    float* volume;          /* device, [Vz][Vy][Vx], overwritten by each run */
+} fbp_capture_desc;
+
+typedef struct fbp_batch fbp_batch;
+
+/* Batched form of fbp_backproject_confocal for many captures of uneven sizes
+ * (the reference reconstructs one capture per run, Laser.cu:40-67).  Plans
+ * every capture once and allocates the batch's own device buffers; the
+ * descriptors (device pointers included) are copied and must stay valid. */
+fbp_status fbp_batch_create(fbp_context* ctx, uint32_t n, const fbp_capture_desc* captures, fbp_batch** out);
+/* Re-reads every capture's cube and writes every volume: one persistent
+ * launch over all (capture, voxel tile) work items, largest captures first.
+ * use_graph != 0: the launches are captured into a CUDA graph on the first
+ * call and replayed afterwards (needs a non-default stream). */
+fbp_status fbp_batch_run(fbp_batch* batch, int use_graph, void* stream);
+/* Times every voxel-tile shape on this batch and keeps the fastest (index in
+ * *chosen).  Synchronises `stream`; drops a captured graph. */
+fbp_status fbp_batch_autotune(fbp_batch* batch, void* stream, int* chosen);
+/* Selects tile shape `config` (0..2) explicitly. */
+fbp_status fbp_batch_set_config(fbp_batch* batch, int config, void* stream);
+fbp_status fbp_batch_destroy(fbp_batch* batch);
+
 /* ---- post-processing ------------------------------------------------------ */
 
 typedef enum { FBP_FILTER_NONE = 0, FBP_FILTER_LAPLACIAN = 1, FBP_FILTER_LOG = 2, FBP_FILTER_LOG_FFT = 3 } fbp_filter;

@@ -74,15 +74,22 @@ def confocal_voxel(info, cube, laser_xyz, layout=LAYOUT_TIME_INNER, bins=None) -
     return vol
 
 
-def confocal_voxel_subset(info, cube, laser_xyz, idx, layout=LAYOUT_TIME_INNER) -> np.ndarray:
+def confocal_voxel_subset(info, cube, laser_xyz, idx, layout=LAYOUT_TIME_INNER, bins=None) -> np.ndarray:
+    """FP64 values of the voxels idx; bins (len(idx) x L int32), when given,
+    replace the FP64 bin computation."""
     lib = load()
     o = to_oracle_info(info)
     cube = _f32(cube)
     lx = _f32(laser_xyz)
     idx = np.ascontiguousarray(idx, dtype=np.int64)
     out = np.empty(idx.shape[0], dtype=np.float64)
-    assert lib.oracle_confocal_voxel_subset(ctypes.byref(o), _p(cube), c_int(layout), _p(lx), _p(idx),
-                                            c_int64(idx.shape[0]), _p(out)) == 0
+    if bins is None:
+        assert lib.oracle_confocal_voxel_subset(ctypes.byref(o), _p(cube), c_int(layout), _p(lx), _p(idx),
+                                                c_int64(idx.shape[0]), _p(out)) == 0
+    else:
+        b = np.ascontiguousarray(bins, dtype=np.int32).reshape(idx.shape[0], o.num_laser_targets)
+        assert lib.oracle_confocal_voxel_subset_bins(ctypes.byref(o), _p(cube), c_int(layout), _p(lx), _p(idx),
+                                                     c_int64(idx.shape[0]), _p(b), _p(out)) == 0
     return out
 
 

@@ -66,7 +66,7 @@ static double confocal_bounce(const oracle_info* in, const double l[3]) {
 }
 
 static double confocal_voxel_value(const oracle_info* in, const float* cube, int layout, const float* laser_xyz,
-                                   const double* bounce, int64_t v, int bins_mode, const int32_t* bins) {
+                                   const double* bounce, int64_t v, int bins_mode, const int32_t* vbins) {
     const uint32_t Vx = in->voxel_res[0], Vy = in->voxel_res[1];
     const uint32_t L = in->num_laser_targets, T = in->num_time_bins;
     const uint32_t slice = Vx * Vy;
@@ -79,7 +79,7 @@ static double confocal_voxel_value(const oracle_info* in, const float* cube, int
         double lp[3];
         load3(laser_xyz + 3 * (size_t)l, lp);
         const double dist = dist3(lp, p) * 2.0 - (double)in->time_offset + bounce[l];
-        const int32_t b = bins_mode == ORACLE_BINS_GIVEN ? bins[(size_t)v * L + l] : bin_of(dist, in->time_step, T);
+        const int32_t b = bins_mode == ORACLE_BINS_GIVEN ? vbins[l] : bin_of(dist, in->time_step, T);
         if (b < 0 || (uint32_t)b >= T) continue;
         const float I = cube[confocal_index(layout, l, (uint32_t)b, L, T)];
         if (I > ORACLE_EPS) acc += (double)I * safe_rcp_d(dist * dist);
@@ -106,7 +106,8 @@ int oracle_confocal_voxel(const oracle_info* in, const float* cube, int layout, 
     if (!bounce) return 1;
 #pragma omp parallel for schedule(dynamic, 64)
     for (int64_t v = 0; v < V; ++v)
-        vol[v] = confocal_voxel_value(in, cube, layout, laser_xyz, bounce, v, bins_mode, bins);
+        vol[v] = confocal_voxel_value(in, cube, layout, laser_xyz, bounce, v, bins_mode,
+                                      bins_mode == ORACLE_BINS_GIVEN ? bins + (size_t)v * in->num_laser_targets : NULL);
     free(bounce);
     return 0;
 }
@@ -118,6 +119,19 @@ int oracle_confocal_voxel_subset(const oracle_info* in, const float* cube, int l
 #pragma omp parallel for schedule(dynamic, 8)
     for (int64_t i = 0; i < n; ++i)
         out[i] = confocal_voxel_value(in, cube, layout, laser_xyz, bounce, idx[i], ORACLE_BINS_F64, NULL);
+    free(bounce);
+    return 0;
+}
+
+int oracle_confocal_voxel_subset_bins(const oracle_info* in, const float* cube, int layout, const float* laser_xyz,
+                                      const int64_t* idx, int64_t n, const int32_t* bins, double* out) {
+    const uint32_t L = in->num_laser_targets;
+    double* bounce = confocal_bounces(in, laser_xyz);
+    if (!bounce) return 1;
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t i = 0; i < n; ++i)
+        out[i] = confocal_voxel_value(in, cube, layout, laser_xyz, bounce, idx[i], ORACLE_BINS_GIVEN,
+                                      bins + (size_t)i * L);
     free(bounce);
     return 0;
 }

@@ -59,6 +59,11 @@ int oracle_confocal_voxel(const oracle_info* info, const float* cube, int layout
 int oracle_confocal_voxel_subset(const oracle_info* info, const float* cube, int layout, const float* laser_xyz,
                                  const int64_t* idx, int64_t n, double* out);
 
+/* Same subset with given bins: bins[i*L + l] for voxel idx[i] (isolates the
+ * accumulation from the bin arithmetic at full size). */
+int oracle_confocal_voxel_subset_bins(const oracle_info* info, const float* cube, int layout, const float* laser_xyz,
+                                      const int64_t* idx, int64_t n, const int32_t* bins, double* out);
+
 /* FP32 restatement of the same kernel (reference arithmetic in float, IEEE
  * sqrt/div, one thread per voxel instead of per pair): the timed CPU baseline. */
 int oracle_confocal_voxel_f32_subset(const oracle_info* info, const float* cube, int layout, const float* laser_xyz,

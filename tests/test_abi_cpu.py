@@ -117,3 +117,34 @@ def test_bf16_bits_round_trip():
     back = scenes.from_bits_bf16(scenes.to_bits_bf16(a))
     np.testing.assert_allclose(back, a, rtol=2 ** -8)
     assert back[2] == 3.0 and back[4] == 256.0  # round to nearest even
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors have the C structs' sizes and field offsets."""
+    from fasterbackprojection_gb300 import _lib
+
+    structs = {
+        "fbp_recon_info": _lib.ReconInfo,
+        "fbp_lct_params": _lib.LctParams,
+        "fbp_mis_params": _lib.MisParams,
+        "fbp_shape_params": _lib.ShapeParams,
+        "fbp_capture_desc": _lib.CaptureDesc,
+    }
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "fbp.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        c, f, v = line.split()
+        got[(c, f)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)

@@ -192,6 +192,11 @@ def test_confocal_subset_matches_full():
     np.testing.assert_allclose(cpu.confocal_voxel_subset(o, cube, lxyz, idx), full.ravel()[idx], rtol=1e-13)
     f32 = cpu.confocal_voxel_f32_subset(o, cube, lxyz, idx)
     np.testing.assert_allclose(f32, full.ravel()[idx], rtol=1e-4)
+    # Given bins: the subset reads row i of its bins for voxel idx[i].
+    V = 6 * 5 * 7
+    bins = rng.integers(-3, T + 3, size=(V, L)).astype(np.int32)
+    full_b = cpu.confocal_voxel(o, cube, lxyz, bins=bins)
+    np.testing.assert_array_equal(cpu.confocal_voxel_subset(o, cube, lxyz, idx, bins=bins[idx]), full_b.ravel()[idx])
 
 
 def test_exhaustive_oracle_matches_python_loop():
