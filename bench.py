@@ -51,6 +51,7 @@ def parse():
                          "(profiling and plumbing checks)")
     ap.add_argument("--no-extras", action="store_true", help="skip bf16 / reference-CUDA / CPU / batched legs")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-capture batched leg")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-MIS leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     a = ap.parse_args()
     a.small = a.size != "full"
@@ -309,6 +310,8 @@ def run_ours(args):
         extras["error_vs_fp64"] = fp64_error(ctx, info, cube, lx, vol)
         if not args.no_batch:
             extras["batched"] = batched_leg(ctx, dev, 2)
+        if not args.no_learned:
+            extras["learned_mis"] = learned_mis_leg(ctx, dev, info, cube, lx)
 
     peak, peak_kind = measured_peaks()
     achieved = samples * 4 / (bp_ms / 1e3) / 1e9
@@ -481,6 +484,82 @@ def batched_leg(ctx, dev, steps):
                         for z, p in zip(sizes, per)],
         "error_sample": "128 random voxels per capture; FP64 oracle on the decoded BF16 cube (vs_fp64) and on "
                         "the FP32 cube before rounding (vs_fp32_cube, includes the storage rounding)",
+    }
+
+
+def learned_mis_leg(ctx, dev, info, cube, lx, n_train=2000, ks=(4, 8, 16, 32, 64), seeds=(0, 1)):
+    """Learned MIS on the benchmark capture in BF16: train the proposal MLP on
+    the device (2000 seeded point scenes, 64^2 x 512 x 32 ps, seeds 10000..),
+    then for K cluster samples per voxel tile (clusters of 16 x 16 scan
+    points, 256 per capture) compare learned and uniform cluster proposals
+    with the full backprojection of the same BF16 cube: rel-L2 and time.
+    Time-to-1% = wall time (CUDA events) of the smallest K reaching <= 1 %
+    rel-L2, the learned arm including its feature + MLP pass."""
+    import numpy as np
+    import torch
+
+    from fasterbackprojection_gb300 import FBP_MIS_LEARNED, Mlp, learned
+
+    n = int(round(info.num_laser_targets ** 0.5))
+    cs = n // 16
+    stream = torch.cuda.current_stream()
+    cube16 = cube.to(torch.bfloat16)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def timed(fn, reps=3):
+        fn()
+        a, b = ev(), ev()
+        a.record(stream)
+        for _ in range(reps):
+            out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b) / reps
+
+    full, full_ms = timed(lambda: ctx.backproject_confocal(info, cube16, lx))
+    full_np = full.double().cpu().numpy()
+    data = learned.build_training_set(ctx, range(10000, 10000 + n_train), vres=tuple(info.voxel_res), device=dev)
+    mlp = Mlp(ctx, seed=7)
+    losses, train_s = learned.train(ctx, mlp, data, epochs=4, batch=256, lr=2e-3)
+    cdf, prop_ms = timed(lambda: learned.proposal(ctx, mlp, info, cube16, lx, cs, n, defensive=0.1))
+
+    def rel(v):
+        d = v.double().cpu().numpy()
+        return float(np.linalg.norm(d - full_np) / np.linalg.norm(full_np))
+
+    rows = []
+    for K in ks:
+        r = {"K": K}
+        for name, tc in (("learned", cdf), ("uniform", None)):
+            errs, ms = [], []
+            for sd in seeds:
+                est, t = timed(lambda: ctx.mis_backproject(info, cube16, lx, FBP_MIS_LEARNED, K, seed=sd,
+                                                           tile_cluster_cdf=tc, cluster_side=cs, scan_side=n), reps=2)
+                errs.append(rel(est))
+                ms.append(t)
+            r[name] = {"rel_l2": float(np.mean(errs)), "ms": float(np.mean(ms))}
+        rows.append(r)
+    ctx.check_device_status()
+
+    def ttt(name, extra_ms):
+        for r in rows:
+            if r[name]["rel_l2"] <= 0.01:
+                return r[name]["ms"] + extra_ms
+        return None
+
+    t_l, t_u = ttt("learned", prop_ms), ttt("uniform", 0.0)
+    mlp.close()
+    data_s = data.seconds
+    del data
+    return {
+        "workload": "config-2 capture in BF16 (256^2 x 1024 -> 256^3); K clusters of 16x16 scan points per "
+                    "8x16x16-voxel tile, systematic sampling, whole clusters gathered",
+        "training": {"scenes": n_train, "tiles": int(n_train * 64), "epochs": 4, "losses": losses,
+                     "data_s": data_s, "train_s": train_s},
+        "full_bp_ms": full_ms, "proposal_ms": prop_ms, "per_k": rows,
+        "time_to_1pct_ms": {"learned": t_l, "uniform": t_u, "full_bp": full_ms},
+        "learned_vs_full_time": (t_l / full_ms) if t_l else None,
+        "note": "rel-L2 vs the full backprojection of the same BF16 cube; mean over MIS seeds " + str(list(seeds)),
     }
 
 

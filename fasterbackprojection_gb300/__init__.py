@@ -28,4 +28,4 @@ from ._lib import (  # noqa: F401
     ReconInfo,
     ShapeParams,
 )
-from .api import Batch, Context, make_info  # noqa: F401
+from .api import Batch, Context, Mlp, make_info  # noqa: F401

@@ -90,6 +90,7 @@ class MisParams(ctypes.Structure):
 
 
 FBP_MIS_UNIFORM, FBP_MIS_SPATIAL, FBP_MIS_LEARNED, FBP_MIS_REFERENCE = 0, 1, 2, 3
+FBP_MLP_FEATURES = 20
 
 
 class ShapeParams(ctypes.Structure):
@@ -146,6 +147,22 @@ SIGNATURES = {
                                          c_void_p, c_void_p]),
     "fbp_mis_tile_grid": (c_int, [POINTER(ReconInfo), POINTER(c_uint32)]),
     "fbp_lct": (c_int, [c_void_p, c_void_p, c_int, c_uint32, c_uint32, POINTER(LctParams), c_void_p, c_void_p]),
+    "fbp_mlp_num_params": (c_uint32, []),
+    "fbp_mlp_create": (c_int, [c_void_p, c_uint64, POINTER(c_void_p)]),
+    "fbp_mlp_destroy": (c_int, [c_void_p]),
+    "fbp_mlp_get_params": (c_int, [c_void_p, POINTER(c_float), c_uint32]),
+    "fbp_mlp_set_params": (c_int, [c_void_p, POINTER(c_float), c_uint32]),
+    "fbp_mlp_tile_count": (c_int, [POINTER(ReconInfo), POINTER(c_uint32)]),
+    "fbp_mlp_features": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_uint32, c_uint32,
+                                 c_void_p, c_uint32, c_void_p, c_void_p]),
+    "fbp_mlp_labels": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_uint32, c_uint32,
+                               c_void_p, c_uint32, c_void_p, c_void_p]),
+    "fbp_mlp_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_float, c_void_p,
+                                c_void_p]),
+    "fbp_mlp_gradients": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, c_void_p,
+                                  c_void_p]),
+    "fbp_mlp_train_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, c_float,
+                                   c_void_p, c_void_p]),
     "fbp_batch_create": (c_int, [c_void_p, c_uint32, POINTER(CaptureDesc), POINTER(c_void_p)]),
     "fbp_batch_run": (c_int, [c_void_p, c_int, c_void_p]),
     "fbp_batch_autotune": (c_int, [c_void_p, c_void_p, POINTER(c_int)]),

@@ -237,6 +237,40 @@ class Context:
         check(self._lib.fbp_lct(self._h, _ptr(data), layout, N, M, byref(prm), _ptr(out), self._stream(stream)))
         return out
 
+    # -------------------------------------------------------- learned proposal
+    def mlp_tile_count(self, info: ReconInfo) -> int:
+        n = ctypes.c_uint32()
+        check(self._lib.fbp_mlp_tile_count(byref(info), byref(n)))
+        return int(n.value)
+
+    def mlp_features(self, info: ReconInfo, cube, laser_xyz, cluster_side: int, scan_side: int, tiles=None,
+                     out=None, layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
+        """Feature rows [ntiles][G][FBP_MLP_FEATURES] of the listed tiles (int32 tensor) or of every tile."""
+        import torch
+
+        cpr = -(-scan_side // cluster_side)
+        G = cpr * cpr
+        nt = self.mlp_tile_count(info) if tiles is None else tiles.numel()
+        if out is None:
+            out = torch.empty((nt, G, _lib.FBP_MLP_FEATURES), dtype=torch.float32, device=cube.device)
+        check(self._lib.fbp_mlp_features(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout, _ptr(laser_xyz),
+                                         cluster_side, scan_side, _ptr(tiles), 0 if tiles is None else nt, _ptr(out),
+                                         self._stream(stream)))
+        return out
+
+    def mlp_labels(self, info: ReconInfo, cube, laser_xyz, cluster_side: int, scan_side: int, tiles, out=None,
+                   layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
+        import torch
+
+        cpr = -(-scan_side // cluster_side)
+        G = cpr * cpr
+        if out is None:
+            out = torch.empty((tiles.numel(), G), dtype=torch.float32, device=cube.device)
+        check(self._lib.fbp_mlp_labels(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout, _ptr(laser_xyz),
+                                       cluster_side, scan_side, _ptr(tiles), tiles.numel(), _ptr(out),
+                                       self._stream(stream)))
+        return out
+
     # ------------------------------------------------------------- end to end
     def reconstruct_shape_host(self, info: ReconInfo, cube: np.ndarray, laser_xyz: np.ndarray,
                                sensor_xyz: np.ndarray | None = None, use_fourier_filter: bool = True,
@@ -296,6 +330,63 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
             self._lib.fbp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mlp:
+    """The learned MIS proposal network (fbp_mlp_*), parameters on the device."""
+
+    def __init__(self, ctx: Context, seed: int = 0):
+        self._lib = ctx._lib
+        self._ctx = ctx
+        h = c_void_p()
+        check(self._lib.fbp_mlp_create(ctx._h, seed, byref(h)))
+        self._h = h
+        self.num_params = int(self._lib.fbp_mlp_num_params())
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, np.float32)
+        check(self._lib.fbp_mlp_get_params(self._h, out.ctypes.data_as(ctypes.POINTER(c_float)), self.num_params))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params
+        check(self._lib.fbp_mlp_set_params(self._h, p.ctypes.data_as(ctypes.POINTER(c_float)), self.num_params))
+
+    def forward(self, features, logits=True, defensive: float = 0.0, cdf=False, stream=None):
+        """(logits [ntiles][G] or None, inclusive CDF [ntiles][G] or None)."""
+        import torch
+
+        nt, G = features.shape[0], features.shape[1]
+        lo = torch.empty((nt, G), dtype=torch.float32, device=features.device) if logits else None
+        cd = torch.empty((nt, G), dtype=torch.float32, device=features.device) if cdf else None
+        check(self._lib.fbp_mlp_forward(self._ctx._h, self._h, _ptr(features), nt, G, _ptr(lo), defensive, _ptr(cd),
+                                        Context._stream(stream)))
+        return lo, cd
+
+    def gradients(self, features, labels, idx, stream=None):
+        """Gradient of the mean cross-entropy over rows idx, then the loss."""
+        import torch
+
+        out = torch.empty(self.num_params + 1, dtype=torch.float32, device=features.device)
+        check(self._lib.fbp_mlp_gradients(self._ctx._h, self._h, _ptr(features), _ptr(labels), _ptr(idx), idx.numel(),
+                                          features.shape[1], _ptr(out), Context._stream(stream)))
+        return out
+
+    def train_step(self, features, labels, idx, lr: float, loss=None, stream=None):
+        check(self._lib.fbp_mlp_train_step(self._ctx._h, self._h, _ptr(features), _ptr(labels), _ptr(idx),
+                                           idx.numel(), features.shape[1], lr, _ptr(loss), Context._stream(stream)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.fbp_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):  # pragma: no cover - best effort

@@ -24,6 +24,10 @@ __device__ __forceinline__ void cp_async_wait() {
 // 1 / (K p(l | tile)), so sum_k f(v, l_k) / (K p(l_k)) is an unbiased estimate
 // of the full backprojection sum at every voxel of the tile.
 enum SampleMode { SAMPLE_UNIFORM = 0, SAMPLE_ALIAS = 1, SAMPLE_CLUSTERS = 2 };
+// Cluster samples per tile (SAMPLE_CLUSTERS) and the static shared memory the
+// sampled gather keeps for them.
+constexpr uint32_t kMaxClusterSamples = 256;
+constexpr size_t kSampledStaticSmem = kMaxClusterSamples * 8 + 64;
 struct SampleParams {
     int mode;
     uint32_t K;              // samples per tile
@@ -31,7 +35,7 @@ struct SampleParams {
     const float* prob;       // SAMPLE_ALIAS: Vose tables over scan points
     const uint32_t* alias;
     const float* pl;         // SAMPLE_ALIAS: p(l)
-    const float* tile_cdf;   // SAMPLE_CLUSTERS: [tiles][G] inclusive CDF over clusters
+    const float* tile_cdf;   // SAMPLE_CLUSTERS: [tiles][G] inclusive CDF over clusters (null: uniform)
     uint32_t G;              // clusters
     uint32_t cluster_side;   // scan points per cluster side
     uint32_t n_side;         // scan grid side (scan point l = iz * n_side + ix)

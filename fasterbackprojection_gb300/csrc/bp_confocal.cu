@@ -185,8 +185,11 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     const double ey = (double)std::min<uint32_t>(4 * kWZ, Vz) * std::fabs(in.voxel_size[1]);
     const double ez = (double)std::min<uint32_t>(8 * kWY, Vy) * std::fabs(in.voxel_size[2]);
     WindowPlan wp;
-    FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(S), ConfocalGatherParams::meta_bytes(32), &wp,
+    // The sampled kernel also holds its cluster list in static shared memory.
+    FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(S),
+                        ConfocalGatherParams::meta_bytes(32) + (smp ? kSampledStaticSmem : 0), &wp,
                         "fbp_backproject_confocal"));
+    if (smp) wp.smem -= kSampledStaticSmem;
 
     S* rows = nullptr;
     FBP_TRY(prepare_rows<S>(ctx, cube, layout, L, T, wp.pitch, stream, &rows));

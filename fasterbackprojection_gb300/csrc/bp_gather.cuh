@@ -153,7 +153,63 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
     }
     for (uint32_t i = tid; i < slot_stride; i += NT) s_slots[zero_slot + i] = from_f32<S>(0.f);
 
-    const uint32_t nitems = SAMPLED ? p.smp.K : p.L;
+    // SAMPLE_CLUSTERS: this tile's clusters, drawn by systematic sampling from
+    // its CDF (K positions (k + u) / K), duplicates merged; each chosen
+    // cluster is gathered whole with weight hits / (K p_c).
+    uint32_t nitems = SAMPLED ? p.smp.K : p.L;
+    const uint32_t* s_clu = nullptr;
+    const float* s_cw = nullptr;
+    if constexpr (SAMPLED) {
+        __shared__ uint32_t clu[kMaxClusterSamples];
+        __shared__ float cw[kMaxClusterSamples];
+        __shared__ uint32_t ncl;
+        if (p.smp.mode == SAMPLE_CLUSTERS) {
+            const uint32_t K = p.smp.K, G = p.smp.G;
+            const float* cdf = p.smp.tile_cdf ? p.smp.tile_cdf + tile_id * G : nullptr;
+            if (warp == 0) {
+                const float u = hash_uniform(p.smp.seed, tile_id, 0xFFFFFFFFu, 2);
+                for (uint32_t k = lane; k < K; k += 32) {
+                    const float x = ((float)k + u) / (float)K;
+                    uint32_t c;
+                    if (cdf) {
+                        uint32_t lo = 0, hi = G - 1;  // first c with x < cdf[c]
+                        while (lo < hi) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (x < cdf[mid]) hi = mid; else lo = mid + 1;
+                        }
+                        c = lo;
+                    } else {
+                        c = min((uint32_t)(x * (float)G), G - 1);
+                    }
+                    clu[k] = c;
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    uint32_t n = 0;
+                    for (uint32_t k = 0; k < K; ++k) {
+                        const uint32_t c = clu[k];
+                        if (n > 0 && clu[n - 1] == c) {
+                            cw[n - 1] += 1.f;
+                        } else {
+                            clu[n] = c;
+                            cw[n] = 1.f;
+                            ++n;
+                        }
+                    }
+                    for (uint32_t j = 0; j < n; ++j) {
+                        const uint32_t c = clu[j];
+                        const float pc = cdf ? cdf[c] - (c > 0 ? cdf[c - 1] : 0.f) : 1.f / (float)G;
+                        cw[j] = pc > 0.f ? cw[j] / ((float)K * pc) : 0.f;
+                    }
+                    ncl = n;
+                }
+            }
+            __syncthreads();
+            nitems = ncl * p.smp.cluster_side * p.smp.cluster_side;
+            s_clu = clu;
+            s_cw = cw;
+        }
+    }
     const uint32_t nchunks = (nitems + CH - 1) / CH;
 
     // Plan a stage: bin window of each scan point (threads < CH, all in warp 0).
@@ -174,22 +230,17 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                     l = u2 < p.smp.prob[kk] ? kk : p.smp.alias[kk];
                     pl = p.smp.pl[l];
                 } else {
-                    // Cluster from the tile's CDF (binary search), then uniform inside it.
-                    const float* cdf = p.smp.tile_cdf + tile_id * p.smp.G;
-                    uint32_t lo = 0, hi = p.smp.G - 1;
-                    while (lo < hi) {
-                        const uint32_t mid = (lo + hi) >> 1;
-                        if (u1 < cdf[mid]) hi = mid; else lo = mid + 1;
-                    }
-                    const float pc = cdf[lo] - (lo > 0 ? cdf[lo - 1] : 0.f);
+                    // Point `inner` of the j-th chosen cluster (outside the grid
+                    // for a ragged edge cluster: skipped).
                     const uint32_t cs = p.smp.cluster_side, cpr = (p.smp.n_side + cs - 1) / cs;
-                    const uint32_t cx = lo % cpr, cz = lo / cpr;
-                    const uint32_t w0 = min(cs, p.smp.n_side - cx * cs), h0 = min(cs, p.smp.n_side - cz * cs);
-                    const uint32_t inner = min((uint32_t)(u2 * (float)(w0 * h0)), w0 * h0 - 1);
-                    l = (cz * cs + inner / w0) * p.smp.n_side + cx * cs + inner % w0;
-                    pl = pc / (float)(w0 * h0);
+                    const uint32_t j = item / (cs * cs), inner = item - j * (cs * cs);
+                    const uint32_t cl = s_clu[j];
+                    const uint32_t ix = (cl % cpr) * cs + inner % cs, iz = (cl / cpr) * cs + inner / cs;
+                    l = (ix < p.smp.n_side && iz < p.smp.n_side) ? iz * p.smp.n_side + ix : 0xFFFFFFFFu;
+                    pl = 0.f;
+                    wgt = s_cw[j];
                 }
-                wgt = pl > 0.f ? 1.f / ((float)nitems * pl) : 0.f;
+                if (p.smp.mode != SAMPLE_CLUSTERS) wgt = pl > 0.f ? 1.f / ((float)nitems * pl) : 0.f;
             }
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             int cnt = 0, src = 0, near = 0, a = 0;

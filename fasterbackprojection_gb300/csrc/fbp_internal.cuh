@@ -60,6 +60,8 @@ enum WorkspaceSlot {
     WS_HOST_STAGING_OUT,
     WS_HOST_STAGING_AUX,
     WS_HOST_STAGING_AUX2,
+    WS_MLP_PROFILES,    // learned proposal: pooled cluster profiles, centres, scale
+    WS_MLP_PARTIALS,    // learned proposal: per-CTA gradient partials
     WS_NUM_SLOTS
 };
 

@@ -13,9 +13,12 @@
 // does (Laser.cu:574).  Samples are summed in order per voxel (the reference's
 // non-atomic += races).
 //
-// FBP_MIS_UNIFORM / _SPATIAL / _LEARNED are unbiased: each voxel tile draws K
-// scan points from the proposal and the staged gather weights every pair by
-// 1/(K p(l)) (see bp_common.cuh).
+// FBP_MIS_UNIFORM / _SPATIAL are unbiased: each voxel tile draws K scan points
+// from the proposal and the staged gather weights every pair by 1/(K p(l)).
+// FBP_MIS_LEARNED draws K clusters of scan points per tile by systematic
+// sampling from the tile's cluster distribution (uniform without one) and
+// gathers each chosen cluster whole, weighted by hits / (K p_c): unbiased, as
+// the expected number of hits of cluster c is exactly K p_c.
 #include "fbp_internal.cuh"
 #include "bp_common.cuh"
 
@@ -363,9 +366,10 @@ static fbp_status mis_run(fbp_context* ctx, const fbp_recon_info& in, const void
         smp.pl = d_pl;
         FBP_TRY_CUDA(cudaStreamSynchronize(s));  // host tables are temporaries
     } else if (prm.proposal == FBP_MIS_LEARNED) {
-        if (!prm.tile_cluster_cdf || prm.cluster_side == 0 || prm.scan_side == 0 ||
-            prm.scan_side * prm.scan_side != L)
-            return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: learned proposal needs tile CDFs and a square scan grid");
+        if (prm.cluster_side == 0 || prm.scan_side == 0 || (uint64_t)prm.scan_side * prm.scan_side != L)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: cluster sampling needs a square scan grid");
+        if (smp.K > kMaxClusterSamples)
+            return set_error(FBP_ERR_UNSUPPORTED, "fbp_mis_backproject: at most 256 cluster samples per tile");
         const uint32_t cpr = (prm.scan_side + prm.cluster_side - 1) / prm.cluster_side;
         smp.mode = SAMPLE_CLUSTERS;
         smp.tile_cdf = prm.tile_cluster_cdf;

@@ -80,6 +80,33 @@ def confocal_points(n: int, T: int, dt_s: float, n_points: int = 200, depth_rang
     return Capture(cube, lx, None, step, n, T)
 
 
+def confocal_points_torch(n: int, T: int, dt_s: float, n_points: int = 200, depth_range=(0.4, 1.2), seed: int = 1,
+                          photons: float = 1e4, device="cuda", noise: bool = True) -> Capture:
+    """confocal_points generated on the device (same scene and contribution
+    rule; Poisson noise from torch's generator seeded with `seed`)."""
+    import torch
+
+    step = LIGHT_SPEED * dt_s
+    lx = torch.from_numpy(wall_grid(n)).to(device)
+    pts, alb, _ = random_points(n_points, depth_range, seed)
+    L = n * n
+    r = torch.cdist(lx.double(), torch.from_numpy(pts).to(device))  # [L, P]
+    b = torch.round(2 * r / step).to(torch.int64)
+    ok = b < T
+    val = (torch.from_numpy(alb).to(device)[None, :] / r ** 4)
+    flat = (torch.arange(L, device=device, dtype=torch.int64)[:, None] * T + b)[ok]
+    cube = torch.zeros(L * T, dtype=torch.float64, device=device)
+    cube.index_add_(0, flat, val[ok])
+    cube = cube.view(L, T)
+    if noise:
+        tot = cube.sum(dim=1).mean().item()
+        if tot > 0:
+            g = torch.Generator(device=device)
+            g.manual_seed(seed)
+            cube = torch.poisson(cube * (photons / tot), generator=g)
+    return Capture(cube.float().contiguous(), lx.contiguous(), None, step, n, T)
+
+
 def exhaustive_points(nl: int, ns: int, T: int, dt_s: float, n_points: int = 500, depth_range=(0.4, 1.4),
                       seed: int = 3, photons: float = 1e4, noise: bool = True) -> Capture:
     """Config-3 style capture: [L][S][T], albedo / (r_l^2 r_s^2) at round((r_l + r_s) / (c dt))."""

@@ -143,17 +143,19 @@ fbp_status fbp_debug_exhaustive_bins(fbp_context* ctx, const fbp_recon_info* inf
 typedef enum {
     FBP_MIS_UNIFORM = 0,   /* unbiased, scan points uniform per voxel tile */
     FBP_MIS_SPATIAL = 1,   /* unbiased, p(l) proportional to scan point l's total intensity */
-    FBP_MIS_LEARNED = 2,   /* unbiased, per-tile cluster distribution (e.g. from the MLP) */
+    FBP_MIS_LEARNED = 2,   /* unbiased, whole scan clusters drawn per tile (systematic sampling) from a
+                              per-tile cluster distribution (fbp_mlp_forward), uniform when none is given */
     FBP_MIS_REFERENCE = 3  /* the reference kernel's one-sample balance-heuristic MIS */
 } fbp_mis_proposal;
 
 typedef struct {
     int proposal;            /* fbp_mis_proposal */
-    uint32_t samples;        /* per voxel tile (unbiased modes) or per voxel (REFERENCE; 0 = L/4) */
+    uint32_t samples;        /* per voxel tile: scan points (UNIFORM, SPATIAL) or clusters (LEARNED, <= 256);
+                                per voxel (REFERENCE; 0 = L/4) */
     uint64_t seed;           /* unbiased modes: counter-based RNG seed */
     const float* noise;      /* REFERENCE: device uniform buffer (NULL: numVoxels from std::mt19937) */
     uint64_t noise_size;
-    const float* tile_cluster_cdf; /* LEARNED: device [tiles][G] inclusive CDF over scan clusters,
+    const float* tile_cluster_cdf; /* LEARNED: device [tiles][G] inclusive CDF over scan clusters (NULL: uniform),
                                       tiles in fbp_mis_tile_grid order (x fastest) */
     uint32_t cluster_side;   /* LEARNED: clusters are cluster_side^2 blocks of the scan grid */
     uint32_t scan_side;      /* LEARNED: scan grid side (L = scan_side^2, l = iz*side + ix) */
@@ -175,6 +177,55 @@ fbp_status fbp_mis_reference_tables(fbp_context* ctx, const fbp_recon_info* info
                                     int layout, float* spatial_cdf, uint32_t* alias, float* prob, void* stream);
 /* Voxel tiles of the gather / MIS sampling: tiles[0..2] along (vx, vy, vz). */
 fbp_status fbp_mis_tile_grid(const fbp_recon_info* info, uint32_t tiles[3]);
+
+/* ---- learned MIS proposal (MLP on the tensor cores) ----------------------- */
+
+/* No counterpart in the reference: its MIS proposal is the spatial alias table
+ * over scan points (Laser.cu:253-315).  Here a 19 -> 64 -> 64 -> 64 -> 1 MLP
+ * (GELU, BF16 weights and operands on tcgen05 tensor cores, FP32 accumulation
+ * in TMEM) scores every (voxel tile, scan cluster) pair; FBP_MIS_LEARNED
+ * draws whole clusters from the per-tile distribution it yields.
+ * Clusters are cluster_side^2 blocks of the scan grid (scan_side^2 points,
+ * l = iz*scan_side + ix), at most 1024 per capture.  Tiles are the gather's
+ * 8 x 16 x 16-voxel tiles in fbp_mis_tile_grid order (x fastest).
+ * Feature rows hold FBP_MLP_FEATURES floats (19 inputs + 1 pad). */
+#define FBP_MLP_FEATURES 20
+
+typedef struct fbp_mlp fbp_mlp;
+
+uint32_t fbp_mlp_num_params(void);
+/* Random initialisation (uniform +-1/sqrt(fan_in), zero biases) from `seed`. */
+fbp_status fbp_mlp_create(fbp_context* ctx, uint64_t seed, fbp_mlp** out);
+fbp_status fbp_mlp_destroy(fbp_mlp* mlp);
+/* Flat FP32 parameter vector: W1[64][32] (inputs 19..31 zero), b1[64],
+ * W2[64][64], b2, W3[64][64], b3, w4[64], b4.  set_params resets Adam. */
+fbp_status fbp_mlp_get_params(const fbp_mlp* mlp, float* host, uint32_t n);
+fbp_status fbp_mlp_set_params(fbp_mlp* mlp, const float* host, uint32_t n);
+fbp_status fbp_mlp_tile_count(const fbp_recon_info* info, uint32_t* ntiles);
+/* Feature rows [ntiles][G][FBP_MLP_FEATURES] (device) of the listed tiles
+ * (device list; NULL = every tile, ntiles ignored). */
+fbp_status fbp_mlp_features(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype, int layout,
+                            const float* laser_xyz, uint32_t cluster_side, uint32_t scan_side, const uint32_t* tiles,
+                            uint32_t ntiles, float* features, void* stream);
+/* Training targets [ntiles][G] (device): per tile, q_c proportional to
+ * sqrt(sum over the tile's voxels of F_vc^2), F_vc = cluster c's exact
+ * contribution (the reference kernel's arithmetic) to voxel v. */
+fbp_status fbp_mlp_labels(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype, int layout,
+                          const float* laser_xyz, uint32_t cluster_side, uint32_t scan_side, const uint32_t* tiles,
+                          uint32_t ntiles, float* labels, void* stream);
+/* Forward pass: logits [ntiles][G] and/or the per-tile inclusive CDF
+ * [ntiles][G] of (1 - defensive) * softmax + defensive / G (either may be NULL). */
+fbp_status fbp_mlp_forward(fbp_context* ctx, const fbp_mlp* mlp, const float* features, uint32_t ntiles, uint32_t G,
+                           float* logits, float defensive, float* tile_cdf, void* stream);
+/* Gradient of the mean softmax cross-entropy over the minibatch rows idx
+ * (device, nbatch entries indexing features/labels) into grad_loss (device,
+ * fbp_mlp_num_params() + 1 floats: the gradient, then the loss). */
+fbp_status fbp_mlp_gradients(fbp_context* ctx, const fbp_mlp* mlp, const float* features, const float* labels,
+                             const uint32_t* idx, uint32_t nbatch, uint32_t G, float* grad_loss, void* stream);
+/* One Adam step (beta 0.9 / 0.999) on that gradient; the minibatch loss is
+ * copied to `loss` (device, may be NULL). */
+fbp_status fbp_mlp_train_step(fbp_context* ctx, fbp_mlp* mlp, const float* features, const float* labels,
+                              const uint32_t* idx, uint32_t nbatch, uint32_t G, float lr, float* loss, void* stream);
 
 /* ---- batched reconstruction ---------------------------------------------- */
 

@@ -73,7 +73,7 @@ def test_unbiased_estimators_converge_to_full_backprojection(ctx, cuda, proposal
         cdf = np.cumsum(w / w.sum(1, keepdims=True), axis=1).astype(np.float32)
         cdf[:, -1] = 1.0
         kw = dict(tile_cluster_cdf=torch.from_numpy(cdf).to(cuda), cluster_side=4, scan_side=16)
-    K = 64
+    K = 4 if proposal == "clusters" else 64  # clusters of 16 scan points each
     runs = 200
     acc = torch.zeros_like(full)
     single = None

@@ -287,3 +287,35 @@ def test_alias_tables_reproduce_the_distribution():
     np.testing.assert_allclose(mass, p, atol=1e-6)
     assert cpu.build_alias(np.array([0.5, 0.4], np.float32))[0] == 1  # negative probability
     assert cpu.build_alias(np.array([0.5, 0.9], np.float32))[0] == 2  # does not sum to 1
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The oracle's backward pass (exact FP64 mode) against central differences."""
+    from oracle import mlp_ref
+
+    rng = np.random.default_rng(0)
+    p = np.zeros(mlp_ref.NPARAM)
+    p[mlp_ref.OW1:mlp_ref.OB1] = (rng.uniform(-0.3, 0.3, (64, 32)) * (np.arange(32) < 19)).ravel()
+    p[mlp_ref.OB1:] = rng.uniform(-0.2, 0.2, mlp_ref.NPARAM - mlp_ref.OB1)
+    feats = rng.normal(size=(3, 10, mlp_ref.FEAT))
+    q = rng.uniform(size=(3, 10))
+    q /= q.sum(axis=1, keepdims=True)
+    loss, grad = mlp_ref.loss_and_grad(p, feats, q, rounding=False)
+    idx = np.concatenate([rng.choice(np.arange(mlp_ref.OW1, mlp_ref.OB1).reshape(64, 32)[:, :19].ravel(), 8),
+                          rng.choice(np.arange(mlp_ref.OB1, mlp_ref.NPARAM), 24)])
+    h = 1e-6
+    for i in idx:
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (mlp_ref.loss_and_grad(pp, feats, q, rounding=False)[0] -
+              mlp_ref.loss_and_grad(pm, feats, q, rounding=False)[0]) / (2 * h)
+        assert abs(fd - grad[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, grad[i])
+
+
+def test_mlp_bf16_rounding_is_nearest_even():
+    from oracle import mlp_ref
+
+    x = np.array([1.0, 1.00390625, 1.005859375, -2.5, 3.0e-3], np.float32)
+    want = np.array([1.0, 1.0, 1.0078125, -2.5, 0.0030059814453125])
+    np.testing.assert_array_equal(mlp_ref.bf16(x), want)
