@@ -86,6 +86,7 @@ class MisParams(ctypes.Structure):
         ("tile_cluster_cdf", c_void_p),
         ("cluster_side", c_uint32),
         ("scan_side", c_uint32),
+        ("cv_side", c_uint32),
     ]
 
 

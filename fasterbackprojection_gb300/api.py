@@ -198,14 +198,14 @@ class Context:
     # -------------------------------------------------------------------- MIS
     def mis_backproject(self, info: ReconInfo, cube, laser_xyz, proposal: int, samples: int, seed: int = 0,
                         noise=None, tile_cluster_cdf=None, cluster_side: int = 0, scan_side: int = 0, out=None,
-                        layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
+                        layout=_lib.FBP_LAYOUT_TIME_INNER, cv_side: int = 0, stream=None):
         import torch
 
         vx, vy, vz = info.voxel_res
         if out is None:
             out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
         prm = MisParams(proposal, samples, seed, _ptr(noise), 0 if noise is None else noise.numel(),
-                        _ptr(tile_cluster_cdf), cluster_side, scan_side)
+                        _ptr(tile_cluster_cdf), cluster_side, scan_side, cv_side)
         check(self._lib.fbp_mis_backproject(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
                                             _ptr(laser_xyz), byref(prm), _ptr(out), self._stream(stream)))
         return out

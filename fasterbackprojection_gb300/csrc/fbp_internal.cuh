@@ -62,6 +62,7 @@ enum WorkspaceSlot {
     WS_HOST_STAGING_AUX2,
     WS_MLP_PROFILES,    // learned proposal: pooled cluster profiles, centres, scale
     WS_MLP_PARTIALS,    // learned proposal: per-CTA gradient partials
+    WS_MIS_VIRTUAL,     // cluster MIS control variate: virtual capture + two partial volumes
     WS_NUM_SLOTS
 };
 

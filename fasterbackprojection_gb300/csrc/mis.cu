@@ -264,9 +264,111 @@ static fbp_status upload(fbp_context* ctx, int slot, const std::vector<T>& h, cu
     return FBP_OK;
 }
 
+// Control variate of the cluster estimator: the capture summed over cv x cv
+// blocks of scan points (values above EPS only, as the gathers skip the
+// rest), one "virtual" scan point per block at the block's mean position.
+// vcube is time innermost [Gv][T] FP32.  Grid (Gv, ceil(T / 256)).
+template <typename S>
+__global__ void virtual_capture_kernel(const S* __restrict__ cube, int time_major, uint32_t L, uint32_t T,
+                                       uint32_t n_side, uint32_t cv, const float* __restrict__ lxyz,
+                                       float* __restrict__ vcube, float* __restrict__ vxyz) {
+    const uint32_t m = n_side / cv;
+    const uint32_t g = blockIdx.x, gx = g % m, gz = g / m;
+    const uint32_t t = blockIdx.y * blockDim.x + threadIdx.x;
+    if (t < T) {
+        float acc = 0.f;
+        for (uint32_t iz = 0; iz < cv; ++iz)
+            for (uint32_t ix = 0; ix < cv; ++ix) {
+                const uint64_t l = (uint64_t)(gz * cv + iz) * n_side + gx * cv + ix;
+                const float v = to_f32(time_major ? cube[(uint64_t)t * L + l] : cube[l * T + t]);
+                if (v > FBP_EPS) acc += v;
+            }
+        vcube[(uint64_t)g * T + t] = acc;
+    }
+    if (blockIdx.y == 0 && threadIdx.x == 0) {
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (uint32_t iz = 0; iz < cv; ++iz)
+            for (uint32_t ix = 0; ix < cv; ++ix) {
+                const uint64_t l = (uint64_t)(gz * cv + iz) * n_side + gx * cv + ix;
+                sx += lxyz[3 * l];
+                sy += lxyz[3 * l + 1];
+                sz += lxyz[3 * l + 2];
+            }
+        const float inv = 1.f / (float)(cv * cv);
+        vxyz[3 * g] = sx * inv;
+        vxyz[3 * g + 1] = sy * inv;
+        vxyz[3 * g + 2] = sz * inv;
+    }
+}
+
+// volume = volume + a - b
+__global__ void cv_combine_kernel(float* __restrict__ vol, const float* __restrict__ a, const float* __restrict__ b,
+                                  uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        vol[i] = (vol[i] + a[i]) - b[i];
+}
+
+// FBP_MIS_LEARNED: whole clusters per tile; with cv_side, the estimator is
+// BP(virtual capture) + sum over the chosen clusters of (real - virtual)
+// contributions, weighted hits / (K p_c): unbiased for the full
+// backprojection, with the variance of the residual only.
+template <typename S>
+static fbp_status mis_clusters(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int layout,
+                               const float* laser_xyz, const fbp_mis_params& prm, float* volume, cudaStream_t s) {
+    const uint32_t L = in.num_laser_targets, T = in.num_time_bins;
+    if (prm.cluster_side == 0 || prm.scan_side == 0 || (uint64_t)prm.scan_side * prm.scan_side != L)
+        return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: cluster sampling needs a square scan grid");
+    if (prm.samples == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: samples must be > 0");
+    if (prm.samples > kMaxClusterSamples)
+        return set_error(FBP_ERR_UNSUPPORTED, "fbp_mis_backproject: at most 256 cluster samples per tile");
+    const uint32_t cpr = (prm.scan_side + prm.cluster_side - 1) / prm.cluster_side;
+    SampleParams smp{};
+    smp.mode = SAMPLE_CLUSTERS;
+    smp.K = prm.samples;
+    smp.seed = prm.seed;
+    smp.tile_cdf = prm.tile_cluster_cdf;
+    smp.G = cpr * cpr;
+    smp.cluster_side = prm.cluster_side;
+    smp.n_side = prm.scan_side;
+    if (prm.cv_side == 0) return confocal_gather(ctx, in, cube, dtype_of<S>(), layout, laser_xyz, volume, s, &smp);
+
+    const uint32_t cv = prm.cv_side;
+    if (prm.scan_side % cv != 0 || prm.cluster_side % cv != 0)
+        return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: cv_side must divide scan_side and cluster_side");
+    const uint32_t m = prm.scan_side / cv, Gv = m * m;
+    const uint64_t V = (uint64_t)in.voxel_res[0] * in.voxel_res[1] * in.voxel_res[2];
+    const size_t vc_bytes = ((size_t)Gv * T * sizeof(float) + 255) & ~size_t(255);
+    const size_t vx_bytes = ((size_t)Gv * 3 * sizeof(float) + 255) & ~size_t(255);
+    const size_t vol_bytes = ((size_t)V * sizeof(float) + 255) & ~size_t(255);
+    void* ws = nullptr;
+    FBP_TRY(workspace(ctx, WS_MIS_VIRTUAL, vc_bytes + vx_bytes + 2 * vol_bytes, s, &ws));
+    float* vcube = static_cast<float*>(ws);
+    float* vxyz = reinterpret_cast<float*>(static_cast<char*>(ws) + vc_bytes);
+    float* tmp_a = reinterpret_cast<float*>(static_cast<char*>(ws) + vc_bytes + vx_bytes);
+    float* tmp_b = reinterpret_cast<float*>(static_cast<char*>(ws) + vc_bytes + vx_bytes + vol_bytes);
+    virtual_capture_kernel<S><<<dim3(Gv, cdiv(T, 256)), 256, 0, s>>>(static_cast<const S*>(cube),
+                                                                    layout == FBP_LAYOUT_TIME_MAJOR, L, T,
+                                                                    prm.scan_side, cv, laser_xyz, vcube, vxyz);
+    FBP_CHECK_LAUNCH(ctx, "virtual_capture_kernel");
+    fbp_recon_info vin = in;
+    vin.num_laser_targets = Gv;
+    vin.num_sensor_targets = Gv;
+    FBP_TRY(confocal_gather(ctx, vin, vcube, FBP_F32, FBP_LAYOUT_TIME_INNER, vxyz, volume, s, nullptr));
+    FBP_TRY(confocal_gather(ctx, in, cube, dtype_of<S>(), layout, laser_xyz, tmp_a, s, &smp));
+    SampleParams vs = smp;  // the same clusters (same seed, tiles, CDF) of the virtual grid
+    vs.cluster_side = prm.cluster_side / cv;
+    vs.n_side = m;
+    FBP_TRY(confocal_gather(ctx, vin, vcube, FBP_F32, FBP_LAYOUT_TIME_INNER, vxyz, tmp_b, s, &vs));
+    cv_combine_kernel<<<std::min<uint64_t>(cdiv(V, 256), (uint64_t)ctx->sm_count * 8), 256, 0, s>>>(volume, tmp_a,
+                                                                                                     tmp_b, V);
+    FBP_CHECK_LAUNCH(ctx, "cv_combine_kernel");
+    return FBP_OK;
+}
+
 template <typename S>
 static fbp_status mis_run(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int layout,
                           const float* laser_xyz, const fbp_mis_params& prm, float* volume, cudaStream_t s) {
+    if (prm.proposal == FBP_MIS_LEARNED) return mis_clusters<S>(ctx, in, cube, layout, laser_xyz, prm, volume, s);
     const uint32_t L = in.num_laser_targets, T = in.num_time_bins;
     const int tmaj = layout == FBP_LAYOUT_TIME_MAJOR;
     // Per-scan-point totals (device -> host): the proposal is built on the host
@@ -365,17 +467,6 @@ static fbp_status mis_run(fbp_context* ctx, const fbp_recon_info& in, const void
         smp.alias = d_alias;
         smp.pl = d_pl;
         FBP_TRY_CUDA(cudaStreamSynchronize(s));  // host tables are temporaries
-    } else if (prm.proposal == FBP_MIS_LEARNED) {
-        if (prm.cluster_side == 0 || prm.scan_side == 0 || (uint64_t)prm.scan_side * prm.scan_side != L)
-            return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: cluster sampling needs a square scan grid");
-        if (smp.K > kMaxClusterSamples)
-            return set_error(FBP_ERR_UNSUPPORTED, "fbp_mis_backproject: at most 256 cluster samples per tile");
-        const uint32_t cpr = (prm.scan_side + prm.cluster_side - 1) / prm.cluster_side;
-        smp.mode = SAMPLE_CLUSTERS;
-        smp.tile_cdf = prm.tile_cluster_cdf;
-        smp.G = cpr * cpr;
-        smp.cluster_side = prm.cluster_side;
-        smp.n_side = prm.scan_side;
     } else {
         return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: unknown proposal");
     }

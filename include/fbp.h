@@ -159,6 +159,10 @@ typedef struct {
                                       tiles in fbp_mis_tile_grid order (x fastest) */
     uint32_t cluster_side;   /* LEARNED: clusters are cluster_side^2 blocks of the scan grid */
     uint32_t scan_side;      /* LEARNED: scan grid side (L = scan_side^2, l = iz*side + ix) */
+    uint32_t cv_side;        /* LEARNED: 0, or the side of the scan-point blocks summed into the control
+                                variate (divides cluster_side and scan_side): the estimate is then the full
+                                backprojection of the block-summed capture plus the sampled clusters'
+                                real-minus-block-summed contributions (still unbiased) */
 } fbp_mis_params;
 
 /* Sampled confocal backprojection.  Replaces Laser::reconstructAABBConfocalMIS

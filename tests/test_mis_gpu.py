@@ -53,7 +53,7 @@ def test_reference_mis_many_samples_is_deterministic(ctx, cuda):
     assert torch.equal(a, b) and float(a.abs().max()) > 0
 
 
-@pytest.mark.parametrize("proposal", ["uniform", "spatial", "clusters"])
+@pytest.mark.parametrize("proposal", ["uniform", "spatial", "clusters", "clusters_cv"])
 def test_unbiased_estimators_converge_to_full_backprojection(ctx, cuda, proposal):
     import torch
     from fasterbackprojection_gb300 import FBP_MIS_LEARNED, FBP_MIS_SPATIAL, FBP_MIS_UNIFORM
@@ -64,16 +64,18 @@ def test_unbiased_estimators_converge_to_full_backprojection(ctx, cuda, proposal
     lx = torch.from_numpy(cap.laser_xyz).to(cuda)
     full = ctx.backproject_confocal(info, cube, lx).double()
     kw = {}
-    mode = {"uniform": FBP_MIS_UNIFORM, "spatial": FBP_MIS_SPATIAL, "clusters": FBP_MIS_LEARNED}[proposal]
-    if proposal == "clusters":
+    mode = {"uniform": FBP_MIS_UNIFORM, "spatial": FBP_MIS_SPATIAL, "clusters": FBP_MIS_LEARNED,
+            "clusters_cv": FBP_MIS_LEARNED}[proposal]
+    if proposal.startswith("clusters"):
         tiles = mis_tile_grid(info)
         G = 16  # 4 x 4 clusters of 4 x 4 scan points
         rng = np.random.default_rng(0)
         w = rng.uniform(0.2, 1.0, (int(np.prod(tiles)), G))
         cdf = np.cumsum(w / w.sum(1, keepdims=True), axis=1).astype(np.float32)
         cdf[:, -1] = 1.0
-        kw = dict(tile_cluster_cdf=torch.from_numpy(cdf).to(cuda), cluster_side=4, scan_side=16)
-    K = 4 if proposal == "clusters" else 64  # clusters of 16 scan points each
+        kw = dict(tile_cluster_cdf=torch.from_numpy(cdf).to(cuda), cluster_side=4, scan_side=16,
+                  cv_side=2 if proposal == "clusters_cv" else 0)
+    K = 4 if proposal.startswith("clusters") else 64  # clusters of 16 scan points each
     runs = 200
     acc = torch.zeros_like(full)
     single = None
@@ -98,3 +100,42 @@ def test_more_samples_lower_error(ctx, cuda):
     errs = [rel_l2(ctx.mis_backproject(info, cube, lx, FBP_MIS_SPATIAL, K, seed=3).cpu().numpy(), full)
             for K in (16, 64, 256)]
     assert errs[0] > errs[1] > errs[2]
+
+
+def test_control_variate_with_every_cluster_is_the_full_backprojection(ctx, cuda):
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_LEARNED
+
+    cap, info = _case(seed=19)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    full = ctx.backproject_confocal(info, cube, lx).cpu().numpy()
+    # K = G = 16 uniform: every cluster once, the control variate cancels.
+    got = ctx.mis_backproject(info, cube, lx, FBP_MIS_LEARNED, 16, seed=3, cluster_side=4, scan_side=16, cv_side=2)
+    ctx.check_device_status()
+    assert rel_l2(got.cpu().numpy(), full) < 1e-5
+
+
+def test_control_variate_lowers_the_error(ctx, cuda):
+    """Dense scan (64^2 points, 3.1 cm pitch): the 2 x 2-point block sums
+    track the real contributions, so the residual estimator beats plain
+    cluster sampling at the same 8 of 64 clusters per tile."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_LEARNED, make_info, scenes
+
+    n = 64
+    cap = scenes.confocal_points(n, 512, 32e-12, n_points=60, seed=23)
+    hmin, vs = scenes.volume_geometry((32, 32, 32), depth_range=(0.0, 1.5))
+    info = make_info(num_laser_targets=n * n, num_time_bins=512, time_step=cap.time_step, voxel_res=(32, 32, 32),
+                     hidden_min=hmin, voxel_size=vs)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    full = ctx.backproject_confocal(info, cube, lx).cpu().numpy()
+    plain, cv = [], []
+    for seed in range(6):
+        plain.append(rel_l2(ctx.mis_backproject(info, cube, lx, FBP_MIS_LEARNED, 8, seed=seed, cluster_side=8,
+                                                scan_side=n).cpu().numpy(), full))
+        cv.append(rel_l2(ctx.mis_backproject(info, cube, lx, FBP_MIS_LEARNED, 8, seed=seed, cluster_side=8,
+                                             scan_side=n, cv_side=2).cpu().numpy(), full))
+    ctx.check_device_status()
+    assert np.mean(cv) < 0.7 * np.mean(plain), (np.mean(cv), np.mean(plain))
