@@ -85,3 +85,48 @@ def proposal(ctx: Context, mlp: Mlp, info, cube, laser_xyz, cluster_side: int, s
     f = ctx.mlp_features(info, cube, laser_xyz, cluster_side, scan_side, layout=layout, stream=stream)
     _, cdf = mlp.forward(f, logits=False, defensive=defensive, cdf=True, stream=stream)
     return cdf
+
+
+def main(argv=None) -> int:
+    """Train the proposal on point scenes and evaluate it on a seeded
+    256^2 x 1024 patch capture (BF16):
+    python -m fasterbackprojection_gb300.learned --scenes 2000 --out w.npy"""
+    import argparse
+    import json
+
+    import torch
+
+    from . import FBP_MIS_LEARNED
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scenes", type=int, default=2000)
+    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--samples", type=int, default=8, help="clusters per voxel tile")
+    ap.add_argument("--scan", type=int, default=256)
+    ap.add_argument("--out", default=None, help="save the trained parameters (.npy)")
+    a = ap.parse_args(argv)
+    dev = torch.device("cuda", 0)
+    ctx = Context(0)
+    vres = (a.scan, a.scan, a.scan)
+    data = build_training_set(ctx, range(10000, 10000 + a.scenes), vres=vres, device=dev)
+    mlp = Mlp(ctx, seed=7)
+    losses, train_s = train(ctx, mlp, data, epochs=a.epochs)
+    if a.out:
+        np.save(a.out, mlp.get_params())
+    cap = scenes.confocal_patches_torch(a.scan, 1024, 16e-12, seed=2, device=dev)
+    info = point_scene_info(a.scan, 1024, cap.time_step, vres)
+    cube = cap.cube.to(torch.bfloat16)
+    full = ctx.backproject_confocal(info, cube, cap.laser_xyz).double()
+    cs = a.scan // 16
+    cdf = proposal(ctx, mlp, info, cube, cap.laser_xyz, cs, a.scan)
+    est = ctx.mis_backproject(info, cube, cap.laser_xyz, FBP_MIS_LEARNED, a.samples, seed=0, tile_cluster_cdf=cdf,
+                              cluster_side=cs, scan_side=a.scan, cv_side=max(1, cs // 4)).double()
+    ctx.check_device_status()
+    err = float(torch.linalg.vector_norm(est - full) / torch.linalg.vector_norm(full))
+    print(json.dumps({"scenes": a.scenes, "losses": losses, "train_s": train_s, "data_s": data.seconds,
+                      "samples": a.samples, "rel_l2_vs_full": err}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
