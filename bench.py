@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip bf16 / reference-CUDA / CPU / batched legs")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-capture batched leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-MIS leg")
+    ap.add_argument("--no-configs", action="store_true", help="skip the LCT / exhaustive / filter legs")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     a = ap.parse_args()
     a.small = a.size != "full"
@@ -312,6 +313,11 @@ def run_ours(args):
             extras["batched"] = batched_leg(ctx, dev, 2)
         if not args.no_learned:
             extras["learned_mis"] = learned_mis_leg(ctx, dev, info, cube, lx)
+        if not args.no_configs:
+            pk = measured_peaks()[0]
+            extras["filters"] = filters_leg(ctx, dev, vol, cube, info.time_step, pk)
+            extras["lct"] = lct_leg(ctx, dev, pk)
+            extras["exhaustive"] = exhaustive_leg(ctx, dev)
 
     peak, peak_kind = measured_peaks()
     achieved = samples * 4 / (bp_ms / 1e3) / 1e9
@@ -485,6 +491,125 @@ def batched_leg(ctx, dev, steps):
         "error_sample": "128 random voxels per capture; FP64 oracle on the decoded BF16 cube (vs_fp64) and on "
                         "the FP32 cube before rounding (vs_fp32_cube, includes the storage rounding)",
     }
+
+
+def timed_ms(fn, reps=5, stream=None):
+    """Mean CUDA-event time of fn() over reps calls after one warm-up call."""
+    import torch
+
+    stream = stream or torch.cuda.current_stream()
+    fn()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        out = fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return out, a.elapsed_time(b) / reps
+
+
+def lct_leg(ctx, dev, peak):
+    """LCT of the 64^2 x 512 x 32 ps point capture (200 points) into 64x64x512,
+    against the oracle's FP64 restatement of python/lct.py, which is also
+    timed on the host cores (the reference's lct.py cannot run here: it
+    needs the Stanford .mat captures; its steps are restated)."""
+    import numpy as np
+    import torch
+
+    from fasterbackprojection_gb300 import scenes
+    from oracle import numpy_ref
+
+    N, M = 64, 512
+    cap = scenes.confocal_points(N, M, 32e-12, n_points=200, seed=1)
+    data = cap.cube.reshape(N, N, M).transpose(2, 0, 1).copy()  # [M][N][N]
+    d = torch.from_numpy(data).to(dev)
+    t0 = time.perf_counter()
+    first = ctx.lct(d, 1.0, cap.time_step, 0.8, True)
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    vol, ms = timed_ms(lambda: ctx.lct(d, 1.0, cap.time_step, 0.8, True))
+    bytes_run = 4 * M * N * N * 2 + 2 * 2 * 8 * (2 * M) * (2 * N) ** 2
+    # CPU: the FP64 NumPy restatement, timed step by step on all host cores.
+    t0 = time.perf_counter()
+    psf = numpy_ref.define_psf(N, M, 1.0 / (M * cap.time_step))
+    t_psf = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mtx, mtxi = numpy_ref.resampling_operator(M)
+    t_res = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    want = numpy_ref.lct(data.astype(np.float64), 1.0, cap.time_step, 0.8, True, psf=psf, mtx=mtx, mtxi=mtxi)
+    t_steps = time.perf_counter() - t0
+    got = vol.cpu().numpy()
+    return {
+        "workload": "LCT, 64^2 scan x 512 bins of 32 ps, 200 points -> 64x64x512 (diffuse, snr 0.8)",
+        "gpu_ms": ms, "gpu_first_call_s": first_s,
+        "roofline": {"bound": "hbm", "bytes_per_run": bytes_run, "achieved_gbs": bytes_run / (ms / 1e3) / 1e9,
+                     "peak_gbs": peak, "frac": bytes_run / (ms / 1e3) / 1e9 / peak},
+        "rel_l2_vs_fp64": float(np.linalg.norm(got - want) / np.linalg.norm(want)),
+        "cpu": {"kind": "port", "cores": os.cpu_count(), "define_psf_s": t_psf, "resampling_operator_s": t_res,
+                "steps_1_4_s": t_steps, "total_s": t_psf + t_res + t_steps,
+                "sample": "full run of the FP64 NumPy restatement of python/lct.py (numpy FFT, sparse operator)"},
+        "speedup_vs_cpu_steps": t_steps / (ms / 1e3),
+    }
+
+
+def exhaustive_leg(ctx, dev):
+    """Exhaustive backprojection: 16^2 lasers x 32^2 SPADs, 1024 bins of
+    16 ps, FP16, 500 points -> 128^3; error vs FP64 on 128 voxels."""
+    import numpy as np
+    import torch
+
+    from fasterbackprojection_gb300 import FBP_EXHAUSTIVE, make_info, scenes
+    from oracle import cpu
+
+    cap = scenes.exhaustive_points_torch(16, 32, 1024, 16e-12, n_points=500, seed=3, device=dev)
+    vres = (128, 128, 128)
+    hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 1.5))
+    L, S = 256, 1024
+    info = make_info(num_laser_targets=L, num_sensor_targets=S, num_time_bins=1024, time_step=cap.time_step,
+                     voxel_res=vres, hidden_min=hmin, voxel_size=vs, capture_system=FBP_EXHAUSTIVE)
+    cube16 = cap.cube.to(torch.float16).contiguous()
+    del cap.cube
+    vol, ms = timed_ms(lambda: ctx.backproject_exhaustive(info, cube16, cap.laser_xyz, cap.sensor_xyz), reps=3)
+    triples = 128 ** 3 * L * S
+    idx = np.sort(np.random.default_rng(3).choice(128 ** 3, 128, replace=False)).astype(np.int64)
+    want = cpu.exhaustive_voxel_subset(info, cube16.float().cpu().numpy().reshape(L * S, 1024),
+                                       cap.laser_xyz.cpu().numpy(), cap.sensor_xyz.cpu().numpy(), idx)
+    got = vol.reshape(-1)[torch.from_numpy(idx).to(dev)].double().cpu().numpy()
+    return {
+        "workload": "exhaustive 16^2 x 32^2 x 1024 (16 ps) FP16 -> 128^3, 500 points",
+        "ms": ms, "value": triples / (ms / 1e3), "unit": "voxel-samples/s (voxel, laser, SPAD)",
+        "achieved_gbs_2B_per_sample": triples * 2 / (ms / 1e3) / 1e9,
+        "rel_l2_vs_fp64": float(np.linalg.norm(got - want) / np.linalg.norm(want)), "error_voxels": 128,
+        "reference_cuda": {"unavailable": "the reference kernel splits the pair index by L (l = ls/L, "
+                                          "s = ls%L) and reads laserTargets out of bounds when L != S"},
+    }
+
+
+def filters_leg(ctx, dev, vol, cube, time_step, peak):
+    """LoG (k=5, sigma 1), min-max normalisation and filter_H on the
+    benchmark volume / capture: HBM rooflines (LoG 8 B per voxel, normalise
+    12 B per voxel, filter_H 8 B per bin)."""
+    import torch
+
+    from fasterbackprojection_gb300 import FBP_FILTER_LOG
+
+    V = vol.numel()
+    out = torch.empty_like(vol)
+    _, log_ms = timed_ms(lambda: ctx.postfilter(FBP_FILTER_LOG, vol, 5, 1.0, out=out))
+    tmp = out.clone()
+    _, norm_ms = timed_ms(lambda: ctx.normalize_(tmp))
+    res = {"log": {"ms": log_ms, "bytes": 8 * V, "achieved_gbs": 8 * V / (log_ms / 1e3) / 1e9,
+                   "frac": 8 * V / (log_ms / 1e3) / 1e9 / peak},
+           "normalize": {"ms": norm_ms, "bytes": 12 * V, "achieved_gbs": 12 * V / (norm_ms / 1e3) / 1e9,
+                         "frac": 12 * V / (norm_ms / 1e3) / 1e9 / peak}}
+    c = cube.clone()
+    nb = c.numel()
+    _, fh_ms = timed_ms(lambda: ctx.filter_h_(c, time_step))
+    res["filter_h"] = {"ms": fh_ms, "bytes": 8 * nb, "achieved_gbs": 8 * nb / (fh_ms / 1e3) / 1e9,
+                       "frac": 8 * nb / (fh_ms / 1e3) / 1e9 / peak,
+                       "workload": "256^2 series x 1024 bins, wavelength 10 bins (taps over 1106 padded bins)"}
+    return res
 
 
 def learned_mis_leg(ctx, dev, info, cube, lx, n_train=2000, ks=(4, 8, 16, 32, 64), seeds=(0, 1)):

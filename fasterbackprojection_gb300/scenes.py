@@ -130,6 +130,39 @@ def exhaustive_points(nl: int, ns: int, T: int, dt_s: float, n_points: int = 500
     return Capture(cube.reshape(L, S, T), lx, sx, step, nl, T)
 
 
+def exhaustive_points_torch(nl: int, ns: int, T: int, dt_s: float, n_points: int = 500, depth_range=(0.4, 1.4),
+                            seed: int = 3, photons: float = 1e4, device="cuda", noise: bool = True) -> Capture:
+    """exhaustive_points generated on the device: cube [L][S][T] float32."""
+    import torch
+
+    step = LIGHT_SPEED * dt_s
+    lx = torch.from_numpy(wall_grid(nl)).to(device)
+    sx = torch.from_numpy(wall_grid(ns)).to(device)
+    pts, alb, _ = random_points(n_points, depth_range, seed)
+    L, S = nl * nl, ns * ns
+    P = torch.from_numpy(pts).to(device)
+    A = torch.from_numpy(alb).to(device)
+    rl_all = torch.cdist(lx.double(), P)  # [L, P]
+    rs_all = torch.cdist(sx.double(), P)  # [S, P]
+    cube = torch.zeros(L * S * T, dtype=torch.float64, device=device)
+    base = (torch.arange(L, device=device, dtype=torch.int64)[:, None] * S +
+            torch.arange(S, device=device, dtype=torch.int64)[None, :]) * T
+    for pi in range(n_points):
+        rl = rl_all[:, pi][:, None]
+        rs = rs_all[:, pi][None, :]
+        b = torch.round((rl + rs) / step).to(torch.int64)
+        ok = b < T
+        cube.index_add_(0, (base + b)[ok], (A[pi] / (rl ** 2 * rs ** 2)).expand(L, S)[ok])
+    cube = cube.view(L * S, T)
+    if noise:
+        tot = cube.sum(dim=1).mean().item()
+        if tot > 0:
+            g = torch.Generator(device=device)
+            g.manual_seed(seed)
+            cube = torch.poisson(cube * (photons / tot), generator=g)
+    return Capture(cube.float().view(L, S, T).contiguous(), lx.contiguous(), sx.contiguous(), step, nl, T)
+
+
 def patch_points(n_patches: int, depth_range, seed: int, sample: float = 0.004):
     """Config-2 scene: planar patches (edge U[0.1, 0.4] m, normal uniform on
     the hemisphere facing the wall) sampled every `sample` metres."""
