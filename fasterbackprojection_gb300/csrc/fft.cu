@@ -37,30 +37,125 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// In-place radix-2 DIT over C lines of n points held bit-reversed in x.
+// Stockham auto-sort FFT over C lines of n points in shared memory, natural
+// order in and out (the radix-R formulation of Govindaraju et al., "High
+// performance discrete Fourier transforms on graphics processors", SC 2008):
+// a pass with stride Ns reads the R inputs x[j + r n/R] of butterfly j,
+// multiplies input r by w^(r (j mod Ns) n / (Ns R)) (w = exp(-2 pi i / n)),
+// takes an R-point DFT in registers and writes output k to
+// x[(j / Ns) Ns R + (j mod Ns) + k Ns]; Ns grows by R per pass.  Radix-8
+// passes, then one radix-4 or radix-2 pass.  Every thread holds at most 32
+// complex values (C * n <= 8192 with 256 threads).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// a * (-i) forward, a * (+i) inverse
 template <bool INV>
-__device__ __forceinline__ void fft_stages(float2* x, const float2* tw, int log2n, int C) {
-    const int n = 1 << log2n, half_n = n >> 1;
-    for (int s = 0; s < log2n; ++s) {
-        const int half = 1 << s;
-        for (int b = threadIdx.x; b < C * half_n; b += blockDim.x) {
-            const int line = b >> (log2n - 1);
-            const int bb = b & (half_n - 1);
-            const int pos = bb & (half - 1);
-            const int i0 = ((bb >> s) << (s + 1)) + pos;
-            float2 w = tw[pos << (log2n - 1 - s)];
-            if (INV) w.y = -w.y;
-            float2* xl = x + line * n;
-            const float2 u = xl[i0];
-            const float2 v = cmul(xl[i0 + half], w);
-            xl[i0] = make_float2(u.x + v.x, u.y + v.y);
-            xl[i0 + half] = make_float2(u.x - v.x, u.y - v.y);
-        }
-        __syncthreads();
-    }
+__device__ __forceinline__ float2 rot_mi(float2 a) { return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x); }
+
+template <bool INV>
+__device__ __forceinline__ void dft2(float2& a, float2& b) {
+    const float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
 }
 
-__device__ __forceinline__ int bitrev(int j, int log2n) { return (int)(__brev((unsigned)j) >> (32 - log2n)); }
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a, float2& b, float2& c, float2& d) {
+    const float2 s0 = cadd(a, c), d0 = csub(a, c), s1 = cadd(b, d), d1 = rot_mi<INV>(csub(b, d));
+    a = cadd(s0, s1);
+    c = csub(s0, s1);
+    b = cadd(d0, d1);
+    d = csub(d0, d1);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft8(float2* v) {
+    // Even and odd halves, then the radix-2 combination with w8^k.
+    dft4<INV>(v[0], v[2], v[4], v[6]);
+    dft4<INV>(v[1], v[3], v[5], v[7]);
+    constexpr float h = 0.70710678118654752f;  // sqrt(2) / 2
+    const float2 o1 = INV ? make_float2(h * (v[3].x - v[3].y), h * (v[3].x + v[3].y))
+                          : make_float2(h * (v[3].x + v[3].y), h * (v[3].y - v[3].x));
+    const float2 o2 = rot_mi<INV>(v[5]);
+    const float2 o3 = INV ? make_float2(-h * (v[7].x + v[7].y), h * (v[7].x - v[7].y))
+                          : make_float2(h * (v[7].y - v[7].x), -h * (v[7].x + v[7].y));
+    const float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6], o0 = v[1];
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+}
+
+// w^k for k in [0, n) from the half table tw[k] = exp(-2 pi i k / n), k < n/2.
+template <bool INV>
+__device__ __forceinline__ float2 twiddle(const float2* tw, int k, int half_n) {
+    float2 w = k < half_n ? tw[k] : make_float2(-tw[k - half_n].x, -tw[k - half_n].y);
+    if (INV) w.y = -w.y;
+    return w;
+}
+
+// Shared-memory layout of a line: element j at pidx(j) = j + j/16 (one pad
+// slot per 128 bytes breaks the power-of-two strides of the Stockham writes
+// into different banks); lines are line_stride(n) = n + n/16 + 1 apart so the
+// C lines of a strided-axis load land in different banks too.
+__device__ __forceinline__ int pidx(int j) { return j + (j >> 4); }
+__host__ __device__ __forceinline__ int line_stride(int n) { return n + (n >> 4) + 1; }
+
+template <int R, bool INV>
+__device__ __forceinline__ void stockham_pass(float2* x, const float2* tw, int log2n, int ns_log, int C) {
+    constexpr int U = 32 / R;
+    constexpr int RL = R == 8 ? 3 : (R == 4 ? 2 : 1);
+    const int n = 1 << log2n, lb = log2n - RL, nb_line = 1 << lb, nb = C << lb;
+    const int Ns = 1 << ns_log, LS = line_stride(n);
+    const int tshift = log2n - ns_log - RL;  // n / (Ns R) = 2^tshift
+    float2 v[U][R];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int b = threadIdx.x + u * (int)blockDim.x;
+        if (b < nb) {
+            const int line = b >> lb, j = b & (nb_line - 1);
+            const float2* xl = x + line * LS;
+            const int jm = j & (Ns - 1);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                float2 a = xl[pidx(j + r * nb_line)];
+                if (r > 0 && jm > 0) a = cmul(a, twiddle<INV>(tw, (r * jm) << tshift, n >> 1));
+                v[u][r] = a;
+            }
+            if (R == 8) dft8<INV>(v[u]);
+            else if (R == 4) dft4<INV>(v[u][0], v[u][1], v[u][2], v[u][3]);
+            else dft2<INV>(v[u][0], v[u][1]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int b = threadIdx.x + u * (int)blockDim.x;
+        if (b < nb) {
+            const int line = b >> lb, j = b & (nb_line - 1);
+            float2* xl = x + line * LS;
+            const int d = ((j >> ns_log) << (ns_log + RL)) + (j & (Ns - 1));
+#pragma unroll
+            for (int r = 0; r < R; ++r) xl[pidx(d + r * Ns)] = v[u][r];
+        }
+    }
+    __syncthreads();
+}
+
+template <bool INV>
+__device__ __forceinline__ void fft_stages(float2* x, const float2* tw, int log2n, int C) {
+    int done = 0;
+    while (log2n - done >= 3) {
+        stockham_pass<8, INV>(x, tw, log2n, done, C);
+        done += 3;
+    }
+    if (log2n - done == 2) stockham_pass<4, INV>(x, tw, log2n, done, C);
+    else if (log2n - done == 1) stockham_pass<2, INV>(x, tw, log2n, done, C);
+}
 
 // buildLoGKernel3D (transient_postprocessing.cuh:116-148) at full-grid index (x, y, z).
 __device__ __forceinline__ float log_response(int x, int y, int z, int nx, int ny, int nz, float sigma) {
@@ -73,84 +168,139 @@ __device__ __forceinline__ float log_response(int x, int y, int z, int nx, int n
     return -4.0f * pi * pi * k2 * expf(-2.0f * pi * pi * sigma * sigma * k2);
 }
 
+// Element j of line i of this CTA's group.
+__device__ __forceinline__ long long fft_offset(const FftLineParams& p, long long base, int i, int j) {
+    return base + (long long)i * p.line_step + (long long)j * p.elem_stride;
+}
+
 template <int MODE, int LOAD, int STORE, int MUL>
-__global__ void __launch_bounds__(kFftThreads) fft_lines_kernel(FftLineParams p) {
+__global__ void __launch_bounds__(kFftThreads, 3) fft_lines_kernel(FftLineParams p) {
     extern __shared__ float2 sh[];
-    const int log2n = p.log2n, n = 1 << log2n, C = p.lines;
-    float2* x = sh;                 // [C][n]
-    float2* tw = sh + (size_t)C * n;  // [n/2]
+    constexpr int EMAX = kFftSmemElems / kFftThreads;  // elements per thread
+    const int log2n = p.log2n, n = 1 << log2n, C = p.lines, log2c = p.log2c, total = C * n;
+    const int LS = line_stride(n);
+    const int nv = p.n_valid > 0 ? p.n_valid : n;  // elements j >= nv are zero (not read)
+    const int nst = p.n_store > 0 ? p.n_store : n; // elements j >= nst are not stored
+    float2* x = sh;                    // [C][LS], padded lines
+    float2* tw = sh + (size_t)C * LS;  // [n/2]
     for (int k = threadIdx.x; k < n / 2; k += blockDim.x) tw[k] = p.tw[k];
     const long long base = (long long)blockIdx.y * p.outer_stride + (long long)blockIdx.x * C * p.line_step;
     const bool contig = p.elem_stride == 1;
 
-    // Load (bit-reversed placement).
-    for (int idx = threadIdx.x; idx < C * n; idx += blockDim.x) {
-        const int i = contig ? idx / n : idx % C;
-        const int j = contig ? idx % n : idx / C;
-        const long long off = base + (long long)i * p.line_step + (long long)j * p.elem_stride;
-        float2 v;
-        if (LOAD == LOAD_COMPLEX) {
-            v = p.data[off];
-        } else if (LOAD == LOAD_REAL) {
-            v = make_float2(p.real_in[off], 0.f);
-        } else {  // LOAD_RESAMPLE: row z' = blockIdx.y, y = blockIdx.x * C + i
-            v = make_float2(0.f, 0.f);
-            const int zp = blockIdx.y, y = blockIdx.x * C + i;
-            if (j < p.n_valid && y < p.rs_ns) {
-                float acc = 0.f;
-                for (int k = p.rs_rowptr[zp]; k < p.rs_rowptr[zp + 1]; ++k) {
-                    const int z = p.rs_col[k];
-                    float g = 1.f;
-                    if (p.rs_power > 0) {
-                        const int gi = p.rs_grid_tiled ? (int)(((long long)z * p.rs_ns + y) % p.rs_m) : z;
-                        const float lin = p.rs_m > 1 ? (float)((double)gi / (double)(p.rs_m - 1)) : 0.f;
-                        const float l2 = lin * lin;
-                        g = p.rs_power == 4 ? l2 * l2 : l2;
+    // Load: every thread first issues all its loads (registers), then fills
+    // shared memory, so the loads of a thread are in flight together.
+    if (LOAD == LOAD_RESAMPLE) {
+        // Row z' = blockIdx.y of the operator is the same for the whole CTA:
+        // stage its entries, then accumulate every element term by term
+        // (all of a term's source loads in flight together).
+        constexpr int KMAX = 128;
+        __shared__ int s_col[KMAX];
+        __shared__ float s_val[KMAX];
+        const int zp = blockIdx.y;
+        const int k0 = p.rs_rowptr[zp], nk = p.rs_rowptr[zp + 1] - k0;
+        for (int t = threadIdx.x; t < min(nk, KMAX); t += blockDim.x) {
+            s_col[t] = p.rs_col[k0 + t];
+            s_val[t] = p.rs_val[k0 + t];
+        }
+        __syncthreads();
+        constexpr int EG = 8;  // elements per accumulation group
+        for (int e0 = 0; e0 < EMAX; e0 += EG) {
+            float acc[EG];
+#pragma unroll
+            for (int e = 0; e < EG; ++e) acc[e] = 0.f;
+            for (int k = 0; k < nk; ++k) {
+                const int z = k < KMAX ? s_col[k] : p.rs_col[k0 + k];
+                const float vk = k < KMAX ? s_val[k] : p.rs_val[k0 + k];
+#pragma unroll
+                for (int e = 0; e < EG; ++e) {
+                    const int idx = threadIdx.x + (e0 + e) * kFftThreads;
+                    const int i = contig ? idx >> log2n : idx & (C - 1);
+                    const int j = contig ? idx & (n - 1) : idx >> log2c;
+                    const int y = blockIdx.x * C + i;
+                    if (idx < total && j < nv && y < p.rs_ns) {
+                        const float g = p.rs_power > 0 ? p.rs_gtab[p.rs_grid_tiled ? (z * p.rs_ns + y) % p.rs_m : z]
+                                                       : 1.f;
+                        acc[e] = fmaf(vk * g, p.rs_src[z * p.rs_sz + y * p.rs_sy + j * p.rs_sx], acc[e]);
                     }
-                    acc = fmaf(p.rs_val[k] * g, p.rs_src[z * p.rs_sz + y * p.rs_sy + j * p.rs_sx], acc);
                 }
-                v.x = acc;
+            }
+#pragma unroll
+            for (int e = 0; e < EG; ++e) {
+                const int idx = threadIdx.x + (e0 + e) * kFftThreads;
+                if (idx < total) {
+                    const int i = contig ? idx >> log2n : idx & (C - 1);
+                    const int j = contig ? idx & (n - 1) : idx >> log2c;
+                    x[i * LS + pidx(j)] = make_float2(acc[e], 0.f);
+                }
             }
         }
-        x[i * n + bitrev(j, log2n)] = v;
+    } else {
+        float2 r[EMAX];
+#pragma unroll
+        for (int e = 0; e < EMAX; ++e) {
+            const int idx = threadIdx.x + e * kFftThreads;
+            r[e] = make_float2(0.f, 0.f);
+            if (idx < total) {
+                const int i = contig ? idx >> log2n : idx & (C - 1);
+                const int j = contig ? idx & (n - 1) : idx >> log2c;
+                if (j < nv) {
+                    if (LOAD == LOAD_COMPLEX) r[e] = p.data[fft_offset(p, base, i, j)];
+                    else r[e] = make_float2(p.real_in[fft_offset(p, base, i, j)], 0.f);
+                }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < EMAX; ++e) {
+            const int idx = threadIdx.x + e * kFftThreads;
+            if (idx < total) {
+                const int i = contig ? idx >> log2n : idx & (C - 1);
+                const int j = contig ? idx & (n - 1) : idx >> log2c;
+                x[i * LS + pidx(j)] = r[e];
+            }
+        }
     }
     __syncthreads();
     fft_stages<MODE == FFT_INVERSE>(x, tw, log2n, C);
 
     if (MODE == FFT_FWD_MUL_INV) {
-        for (int idx = threadIdx.x; idx < C * n; idx += blockDim.x) {
-            const int i = idx / n, j = idx % n;
-            const long long off = base + (long long)i * p.line_step + (long long)j * p.elem_stride;
-            float2 m;
-            if (MUL == MUL_ARRAY) {
-                m = p.mul[off];
-            } else {
-                // Position of this element in the nx*ny*nz grid (x fastest).
-                const long long e = off;
-                const int gx = (int)(e % p.nx), gy = (int)((e / p.nx) % p.ny), gz = (int)(e / ((long long)p.nx * p.ny));
-                m = make_float2(log_response(gx, gy, gz, p.nx, p.ny, p.nz, p.sigma), 0.f);
+        float2 m[EMAX];
+#pragma unroll
+        for (int e = 0; e < EMAX; ++e) {
+            const int idx = threadIdx.x + e * kFftThreads;
+            m[e] = make_float2(0.f, 0.f);
+            if (idx < total) {
+                const int i = contig ? idx >> log2n : idx & (C - 1);
+                const int j = contig ? idx & (n - 1) : idx >> log2c;
+                const long long off = fft_offset(p, base, i, j);
+                if (MUL == MUL_ARRAY) {
+                    m[e] = p.mul[off];
+                } else {
+                    // Position of this element in the nx*ny*nz grid (x fastest).
+                    const int gx = (int)(off % p.nx), gy = (int)((off / p.nx) % p.ny),
+                              gz = (int)(off / ((long long)p.nx * p.ny));
+                    m[e] = make_float2(log_response(gx, gy, gz, p.nx, p.ny, p.nz, p.sigma), 0.f);
+                }
             }
-            x[idx] = cmul(x[idx], m);
         }
-        __syncthreads();
-        // Back to bit-reversed order for the inverse transform.
-        for (int idx = threadIdx.x; idx < C * n; idx += blockDim.x) {
-            const int i = idx / n, j = idx % n, r = bitrev(j, log2n);
-            if (j < r) {
-                const float2 t = x[i * n + j];
-                x[i * n + j] = x[i * n + r];
-                x[i * n + r] = t;
+#pragma unroll
+        for (int e = 0; e < EMAX; ++e) {
+            const int idx = threadIdx.x + e * kFftThreads;
+            if (idx < total) {
+                const int i = contig ? idx >> log2n : idx & (C - 1);
+                const int j = contig ? idx & (n - 1) : idx >> log2c;
+                x[i * LS + pidx(j)] = cmul(x[i * LS + pidx(j)], m[e]);
             }
         }
         __syncthreads();
         fft_stages<true>(x, tw, log2n, C);
     }
 
-    for (int idx = threadIdx.x; idx < C * n; idx += blockDim.x) {
-        const int i = contig ? idx / n : idx % C;
-        const int j = contig ? idx % n : idx / C;
-        const long long off = base + (long long)i * p.line_step + (long long)j * p.elem_stride;
-        const float2 v = x[i * n + j];
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int i = contig ? idx >> log2n : idx & (C - 1);
+        const int j = contig ? idx & (n - 1) : idx >> log2c;
+        if (j >= nst) continue;
+        const long long off = fft_offset(p, base, i, j);
+        const float2 v = x[i * LS + pidx(j)];
         if (STORE == STORE_COMPLEX) p.data[off] = make_float2(v.x * p.scale, v.y * p.scale);
         else p.real_out[off] = v.x * p.scale;
     }
@@ -159,10 +309,15 @@ __global__ void __launch_bounds__(kFftThreads) fft_lines_kernel(FftLineParams p)
 template <int MODE, int LOAD, int STORE, int MUL>
 static fbp_status fft_go(fbp_context* ctx, const FftLineParams& p, unsigned gx, unsigned gy, cudaStream_t stream) {
     const int n = 1 << p.log2n;
-    const size_t smem = ((size_t)p.lines * n + n / 2) * sizeof(float2);
+    if (p.lines < 1 || (p.lines & (p.lines - 1)) || (size_t)p.lines * n > (size_t)kFftSmemElems)
+        return set_error(FBP_ERR_UNSUPPORTED, "FFT: lines per CTA must be a power of two within the tile");
+    FftLineParams q = p;
+    q.log2c = 0;
+    while ((1 << q.log2c) < p.lines) ++q.log2c;
+    const size_t smem = ((size_t)p.lines * line_stride(n) + n / 2) * sizeof(float2);
     auto k = fft_lines_kernel<MODE, LOAD, STORE, MUL>;
     FBP_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<dim3(gx, gy), kFftThreads, smem, stream>>>(p);
+    k<<<dim3(gx, gy), kFftThreads, smem, stream>>>(q);
     FBP_CHECK_LAUNCH(ctx, "fft_lines_kernel");
     return FBP_OK;
 }

@@ -26,7 +26,8 @@ struct FftLineParams {
     const float2* tw;        // n/2 twiddles exp(-2 pi i k / n)
     const float2* mul;       // MUL_ARRAY: multiplier with the same indexing as data
     int log2n;
-    int lines;               // lines per CTA (C)
+    int lines;               // lines per CTA (C, a power of two)
+    int log2c;               // log2(lines), set by the launcher
     long long elem_stride, line_step, outer_stride;
     float scale;             // applied on store
     // LOAD_RESAMPLE (LCT): element j < n_valid of row (z', y) is
@@ -42,7 +43,9 @@ struct FftLineParams {
     int rs_m;                // M (bins)
     int rs_power;            // radiometric exponent (2 or 4; 0 for none)
     int rs_grid_tiled;       // 1: python/lct.py tiling grid[(z*N + y) % M], 0: grid[z]
-    int n_valid;
+    const float* rs_gtab;    // [M] grid^power per grid index (rs_power > 0)
+    int n_valid;             // elements j >= n_valid are zero and not read (<= 0: n)
+    int n_store;             // elements j >= n_store are not written (<= 0: n)
     // MUL_LOG: frequency response of buildLoGKernel3D over an nx*ny*nz grid
     int nx, ny, nz;
     float sigma;

@@ -134,6 +134,7 @@ void build_resampling(uint32_t M, std::vector<int>& rp, std::vector<int>& ci, st
 struct LctOperator {
     const int *rp, *ci, *rpt, *cit;
     const float *v, *vt;
+    const float *g2, *g4;  // [M] radiometric scales grid^2, grid^4 (grid = linspace(0, 1, M))
 };
 
 }  // namespace
@@ -158,7 +159,7 @@ static fbp_status lct_plan(fbp_context* ctx, uint32_t N, uint32_t M, double slop
     const size_t nnz = ctx->lct_nnz;
     const size_t hdr = 256;
     const size_t bytes_ops = hdr + (2 * (M + 1) + 2 * nnz) * sizeof(int) + 2 * nnz * sizeof(float);
-    const size_t bytes_aux = 256 + (X + Z) * sizeof(double);
+    const size_t bytes_aux = 256 + (X + Z) * sizeof(double) + 2 * (size_t)M * sizeof(float);
     FBP_TRY(workspace(ctx, WS_LCT_OPERATOR, bytes_ops + bytes_aux, s, &o));
     char* base = static_cast<char*>(o);
     int* d_rp = reinterpret_cast<int*>(base + hdr);
@@ -171,7 +172,10 @@ static fbp_status lct_plan(fbp_context* ctx, uint32_t N, uint32_t M, double slop
     unsigned long long* d_count = reinterpret_cast<unsigned long long*>(aux);
     double* d_gx = reinterpret_cast<double*>(aux + 256);
     double* d_gz = d_gx + X;
+    float* d_g2 = reinterpret_cast<float*>(d_gz + Z);
+    float* d_g4 = d_g2 + M;
     op->rp = d_rp; op->ci = d_ci; op->rpt = d_rpt; op->cit = d_cit; op->v = d_v; op->vt = d_vt;
+    op->g2 = d_g2; op->g4 = d_g4;
     *invpsf = static_cast<float2*>(b);
     if (same) return FBP_OK;
 
@@ -182,6 +186,17 @@ static fbp_status lct_plan(fbp_context* ctx, uint32_t N, uint32_t M, double slop
     FBP_TRY_CUDA(cudaMemcpyAsync(d_cit, cit.data(), nnz * sizeof(int), cudaMemcpyHostToDevice, s));
     FBP_TRY_CUDA(cudaMemcpyAsync(d_v, v.data(), nnz * sizeof(float), cudaMemcpyHostToDevice, s));
     FBP_TRY_CUDA(cudaMemcpyAsync(d_vt, vt.data(), nnz * sizeof(float), cudaMemcpyHostToDevice, s));
+    // Radiometric scales: lin = gi / (M - 1) rounded to float, then squared
+    // (and squared again) in float.
+    std::vector<float> g2(M), g4(M);
+    for (uint32_t gi = 0; gi < M; ++gi) {
+        const float lin = M > 1 ? (float)((double)gi / (double)(M - 1)) : 0.f;
+        const float l2 = lin * lin;
+        g2[gi] = l2;
+        g4[gi] = l2 * l2;
+    }
+    FBP_TRY_CUDA(cudaMemcpyAsync(d_g2, g2.data(), M * sizeof(float), cudaMemcpyHostToDevice, s));
+    FBP_TRY_CUDA(cudaMemcpyAsync(d_g4, g4.data(), M * sizeof(float), cudaMemcpyHostToDevice, s));
     const std::vector<double> gx = np_linspace(-1.0, 1.0, X), gz = np_linspace(0.0, 2.0, Z);
     FBP_TRY_CUDA(cudaMemcpyAsync(d_gx, gx.data(), X * sizeof(double), cudaMemcpyHostToDevice, s));
     FBP_TRY_CUDA(cudaMemcpyAsync(d_gz, gz.data(), Z * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -236,8 +251,9 @@ fbp_status lct_run(fbp_context* ctx, const float* data, int layout, uint32_t N, 
     const size_t nfull = (size_t)Z * X * X;
     FBP_TRY(workspace(ctx, WS_FFT_A, nfull * sizeof(float2), s, &a));
     float2* buf = static_cast<float2*>(a);
-    // Rows (z' < M, y >= N) and planes z' >= M are zero padding.
-    FBP_TRY_CUDA(cudaMemsetAsync(buf, 0, nfull * sizeof(float2), s));
+    // Rows (z' < M, y >= N) and planes z' >= M are zero padding: never
+    // written, and every pass treats them as zero instead of reading them
+    // (n_valid); passes store only what later passes read (n_store).
 
     const int lx = ln + 1, lz = lm + 1;
     FftLineParams p{};
@@ -256,29 +272,40 @@ fbp_status lct_run(fbp_context* ctx, const float* data, int layout, uint32_t N, 
     }
     p.rs_ns = (int)N; p.rs_m = (int)M;
     p.rs_power = prm.diffuse ? 4 : 2;
+    p.rs_gtab = prm.diffuse ? op.g4 : op.g2;
     p.rs_grid_tiled = prm.grid_mode == FBP_LCT_GRID_REFERENCE;
     p.n_valid = (int)N;
+    p.n_store = X;
     FBP_TRY(fft_launch(ctx, p, FFT_FORWARD, LOAD_RESAMPLE, STORE_COMPLEX, MUL_NONE, cdiv(N, p.lines), M, s));
-    // 2. y-FFT of planes z' < M.
+    // 2. y-FFT of planes z' < M (rows y >= N are zero).
     p.lines = std::min(fft_lines_per_cta(lx), X);
     p.elem_stride = X; p.line_step = 1; p.outer_stride = (long long)X * X;
+    p.n_valid = (int)N;
+    p.n_store = X;
     FBP_TRY(fft_launch(ctx, p, FFT_FORWARD, LOAD_COMPLEX, STORE_COMPLEX, MUL_NONE, cdiv(X, p.lines), M, s));
-    // 3. z: forward, Wiener filter, inverse, every (y, x) line.
+    // 3. z: forward (planes z' >= M are zero), Wiener filter, inverse, every
+    //    (y, x) line; only z < M is kept.
     p.log2n = lz;
     p.lines = std::min(fft_lines_per_cta(lz), X);
     FBP_TRY(fft_twiddles(ctx, lz, s, &p.tw));
     p.elem_stride = (long long)X * X; p.line_step = 1; p.outer_stride = X;
     p.mul = invpsf;
+    p.n_valid = (int)M;
+    p.n_store = (int)M;
     FBP_TRY(fft_launch(ctx, p, FFT_FWD_MUL_INV, LOAD_COMPLEX, STORE_COMPLEX, MUL_ARRAY, cdiv(X, p.lines), X, s));
-    // 4. inverse y-FFT of planes z < M (only they are kept).
+    // 4. inverse y-FFT of planes z < M; only rows y < N are kept.
     p.log2n = lx;
     p.lines = std::min(fft_lines_per_cta(lx), X);
     FBP_TRY(fft_twiddles(ctx, lx, s, &p.tw));
     p.elem_stride = X; p.line_step = 1; p.outer_stride = (long long)X * X;
+    p.n_valid = X;
+    p.n_store = (int)N;
     FBP_TRY(fft_launch(ctx, p, FFT_INVERSE, LOAD_COMPLEX, STORE_COMPLEX, MUL_NONE, cdiv(X, p.lines), M, s));
-    // 5. inverse x-FFT of rows (z < M, y < N).
+    // 5. inverse x-FFT of rows (z < M, y < N); only x < N is kept.
     p.lines = std::min(fft_lines_per_cta(lx), (int)N);
     p.elem_stride = 1; p.line_step = X; p.outer_stride = (long long)X * X;
+    p.n_valid = X;
+    p.n_store = (int)N;
     FBP_TRY(fft_launch(ctx, p, FFT_INVERSE, LOAD_COMPLEX, STORE_COMPLEX, MUL_NONE, cdiv(N, p.lines), M, s));
     // 6. unpad, inverse resample (mtxi = mtx^T), normalise the inverse FFT, clamp.
     const size_t nout = (size_t)M * N * N;
