@@ -316,7 +316,14 @@ static fbp_status fft_go(fbp_context* ctx, const FftLineParams& p, unsigned gx, 
     while ((1 << q.log2c) < p.lines) ++q.log2c;
     const size_t smem = ((size_t)p.lines * line_stride(n) + n / 2) * sizeof(float2);
     auto k = fft_lines_kernel<MODE, LOAD, STORE, MUL>;
-    FBP_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // The largest tile any launch uses, set once per variant and device.
+    static thread_local int attr_device = -1;
+    if (attr_device != ctx->device) {
+        const size_t most = ((size_t)kFftSmemElems * 17 / 16 + kFftSmemElems + kFftSmemElems / 2) * sizeof(float2);
+        FBP_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
+        attr_device = ctx->device;
+    }
+    (void)smem;
     k<<<dim3(gx, gy), kFftThreads, smem, stream>>>(q);
     FBP_CHECK_LAUNCH(ctx, "fft_lines_kernel");
     return FBP_OK;

@@ -19,36 +19,94 @@
 namespace fbp {
 
 constexpr int kMaxTaps = 2048;
-__constant__ float c_filter_taps[kMaxTaps];
+// Taps by value (kernel parameters): concurrent calls share no state.
+struct FilterTaps {
+    float w[kMaxTaps];
+};
 
 // One CTA filters one series at a time (grid-stride over series).  Shared
 // memory holds the padded period P[k] = h_ext[k - pad], k < n, extended
 // circularly by R on both sides: S[i] = P[(i - R) mod n], i < n + 2R, so
 //     out[t] = sum_{j=0}^{2R} taps[j] * S[t + pad + 2R - j]
 // is the circular correlation the padded FFTs compute.
-__global__ void filter_h_kernel(float* __restrict__ data, uint64_t nseries, uint32_t T, int n, int R, int pad,
-                                int edge) {
-    extern __shared__ float sh[];  // n + 2R floats
-    const int E = n + 2 * R;
+// Every thread produces Q = 8 consecutive outputs.  It keeps the 2Q values
+// S[b0 - j - Q .. b0 - j + Q) of the current block of Q taps in registers
+// (indices fixed at compile time), loads the next Q once per block, and adds
+// tap j + s to output q from register Q - s + q: one shared-memory load per
+// tap for Q FMAs.  Each output still sums its taps in order j = 0..2R.  The
+// series is stored Q-way interleaved (element e at (e % Q) * QS + e / Q), so
+// the loads of consecutive threads, Q elements apart, hit consecutive words.
+constexpr int kFilterQ = 8;
+
+__device__ __forceinline__ float sld(const float* sh, int qs, int e) {
+    return sh[(e & (kFilterQ - 1)) * qs + (e >> 3)];
+}
+
+__global__ void __launch_bounds__(128) filter_h_kernel(float* __restrict__ data, uint64_t nseries, uint32_t T, int n,
+                                                       int R, int pad, int edge,
+                                                       const __grid_constant__ FilterTaps taps) {
+    constexpr int Q = kFilterQ;
+    extern __shared__ float sh[];  // taps, then Q interleaved parts of QS floats
+    const int E = n + 2 * R, QS = (E + 2 * Q - 1) / Q + 1;
+    const int ntaps = 2 * R + 1;
+    float* s_taps = sh;
+    float* sser = sh + ((ntaps + 3) & ~3);
+    for (int j = threadIdx.x; j < ntaps; j += blockDim.x) s_taps[j] = taps.w[j];
     for (uint64_t s = blockIdx.x; s < nseries; s += gridDim.x) {
         float* h = data + s * T;
         const float first = h[0], last = h[T - 1];
-        for (int i = threadIdx.x; i < E; i += blockDim.x) {
-            int k = (i - R) % n;
-            if (k < 0) k += n;
-            const int u = k - pad;  // signal index
-            float v;
-            if (u >= 0 && u < (int)T) v = h[u];
-            else if (edge) v = u < 0 ? first : last;
-            else v = 0.f;
-            sh[i] = v;
+        // Fill in batches of 8 per thread, the batch's loads in flight together
+        // (the slots past E, read only for discarded outputs, are zero).
+        for (int i0 = threadIdx.x; i0 < Q * QS; i0 += 8 * blockDim.x) {
+            float v[8];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const int i = i0 + b * blockDim.x;
+                int k = i - R;  // circular index in [0, n); i - R >= -R > -n
+                if (k < 0) k += n;
+                while (k >= n) k -= n;
+                const int u = k - pad;  // signal index
+                if (i >= E) v[b] = 0.f;
+                else if (u >= 0 && u < (int)T) v[b] = h[u];
+                else if (edge) v[b] = u < 0 ? first : last;
+                else v[b] = 0.f;
+            }
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                const int i = i0 + b * blockDim.x;
+                if (i < Q * QS) sser[(i & (Q - 1)) * QS + (i >> 3)] = v[b];
+            }
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < (int)T; t += blockDim.x) {
-            float acc = 0.f;
-            const float* hp = sh + t + pad + 2 * R;
-            for (int j = 0; j <= 2 * R; ++j) acc = fmaf(hp[-j], c_filter_taps[j], acc);
-            h[t] = acc;
+        for (int t0 = threadIdx.x * Q; t0 < (int)T; t0 += blockDim.x * Q) {
+            // out[t0 + q] = sum_j taps[j] * S[b0 - j + q], b0 = t0 + pad + 2R (>= Q - 1 + ...)
+            const int b0 = t0 + pad + 2 * R;
+            float buf[2 * Q], acc[Q];
+#pragma unroll
+            for (int m = 0; m < 2 * Q; ++m) buf[m] = (b0 - Q + m >= 0) ? sld(sser, QS, b0 - Q + m) : 0.f;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) acc[q] = 0.f;
+            for (int j = 0; j < ntaps; j += Q) {
+#pragma unroll
+                for (int st = 0; st < Q; ++st) {
+                    if (j + st < ntaps) {
+                        const float t = s_taps[j + st];
+#pragma unroll
+                        for (int q = 0; q < Q; ++q) acc[q] = fmaf(buf[Q - st + q], t, acc[q]);
+                    }
+                }
+                // Next block: S[b0 - j - 2Q .. b0 - j).
+#pragma unroll
+                for (int m = 0; m < Q; ++m) buf[Q + m] = buf[m];
+#pragma unroll
+                for (int m = 0; m < Q; ++m) {
+                    const int e = b0 - j - 2 * Q + m;
+                    buf[m] = e >= 0 ? sld(sser, QS, e) : 0.f;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (t0 + q < (int)T) h[t0 + q] = acc[q];
         }
         __syncthreads();
     }
@@ -102,13 +160,14 @@ fbp_status filter_h_device(fbp_context* ctx, float* data, uint64_t nseries, uint
     std::vector<float> taps;
     int R = 0, pad = 0, n = 0;
     FBP_TRY(filter_h_taps(T, delta_t, wl_mean, wl_sigma, taps, R, pad, n));
-    FBP_TRY_CUDA(cudaMemcpyToSymbolAsync(c_filter_taps, taps.data(), taps.size() * sizeof(float), 0,
-                                         cudaMemcpyHostToDevice, stream));
-    const size_t smem = (size_t)(n + 2 * R) * sizeof(float);
+    FilterTaps tp{};
+    for (size_t j = 0; j < taps.size(); ++j) tp.w[j] = taps[j];
+    const size_t smem = ((size_t)((2 * R + 1 + 3) & ~3) +
+                         (size_t)kFilterQ * ((n + 2 * R + 2 * kFilterQ - 1) / kFilterQ + 1)) * sizeof(float);
     if (smem > (size_t)ctx->smem_optin) return set_error(FBP_ERR_UNSUPPORTED, "filter_H: series too long for one CTA");
     FBP_TRY_CUDA(cudaFuncSetAttribute(filter_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const unsigned blocks = (unsigned)std::min<uint64_t>(nseries, (uint64_t)ctx->sm_count * 8);
-    filter_h_kernel<<<blocks, 256, smem, stream>>>(data, nseries, T, n, R, pad, border == FBP_BORDER_EDGE);
+    const unsigned blocks = (unsigned)std::min<uint64_t>(nseries, (uint64_t)ctx->sm_count * 16);
+    filter_h_kernel<<<blocks, 128, smem, stream>>>(data, nseries, T, n, R, pad, border == FBP_BORDER_EDGE, tp);
     FBP_CHECK_LAUNCH(ctx, "filter_h_kernel");
     return FBP_OK;
 }

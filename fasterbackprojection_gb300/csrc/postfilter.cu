@@ -126,24 +126,42 @@ fbp_status normalize_device(fbp_context* ctx, float* v, uint64_t n, cudaStream_t
 // ------------------------------------------------------------- LoG filter --
 
 constexpr int kLogMaxK = 15;
-__constant__ float c_log_weights[kLogMaxK * kLogMaxK * kLogMaxK];
+
+// LoG taps passed by value (kernel parameters, so concurrent calls with
+// different kernels do not share state): ksize^3 weights, ksize = 2H+1 or 2H+2.
+template <int H>
+struct LogTaps {
+    float w[(2 * H + 2) * (2 * H + 2) * (2 * H + 2)];
+};
 
 // Output tile 8x8x8 per CTA, halo tile (8 + 2h)^3 in shared memory.
 // Taps in the reference's order (kz, ky, kx innermost), sum = fma(v, w, sum)
 // (LoGFilter, transient_postprocessing.cuh:52-83).
 template <int H>
 __global__ void __launch_bounds__(512) log_filter_kernel(const float* __restrict__ in, float* __restrict__ out,
-                                                         uint32_t nx, uint32_t ny, uint32_t nz, int ksize) {
+                                                         uint32_t nx, uint32_t ny, uint32_t nz, int ksize,
+                                                         const __grid_constant__ LogTaps<H> taps) {
     constexpr int E = 8 + 2 * H;
     extern __shared__ float tile[];  // [E][E][E]
     const int x0 = blockIdx.x * 8, y0 = blockIdx.y * 8, z0 = blockIdx.z * 8;
     const int tid = threadIdx.x + 8 * (threadIdx.y + 8 * threadIdx.z);
-    for (int i = tid; i < E * E * E; i += 512) {
-        const int lx = i % E, ly = (i / E) % E, lz = i / (E * E);
-        const int gx = min(max(x0 + lx - H, 0), (int)nx - 1);
-        const int gy = min(max(y0 + ly - H, 0), (int)ny - 1);
-        const int gz = min(max(z0 + lz - H, 0), (int)nz - 1);
-        tile[i] = in[((size_t)gz * ny + gy) * nx + gx];
+    constexpr int NE = E * E * E, B = 4;
+    for (int i0 = tid; i0 < NE; i0 += B * 512) {
+        float v[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int i = i0 + u * 512;
+            if (i < NE) {
+                const int lx = i % E, ly = (i / E) % E, lz = i / (E * E);
+                const int gx = min(max(x0 + lx - H, 0), (int)nx - 1);
+                const int gy = min(max(y0 + ly - H, 0), (int)ny - 1);
+                const int gz = min(max(z0 + lz - H, 0), (int)nz - 1);
+                v[u] = in[((size_t)gz * ny + gy) * nx + gx];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (i0 + u * 512 < NE) tile[i0 + u * 512] = v[u];
     }
     __syncthreads();
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y, z = z0 + threadIdx.z;
@@ -152,11 +170,76 @@ __global__ void __launch_bounds__(512) log_filter_kernel(const float* __restrict
     for (int kz = -H; kz <= H; ++kz)
         for (int ky = -H; ky <= H; ++ky) {
             const float* row = tile + ((threadIdx.z + H + kz) * E + (threadIdx.y + H + ky)) * E + threadIdx.x + H;
-            const float* wrow = c_log_weights + ((kz + H) * ksize + (ky + H)) * ksize + H;
+            const float* wrow = taps.w + ((kz + H) * ksize + (ky + H)) * ksize + H;
 #pragma unroll
             for (int kx = -H; kx <= H; ++kx) sum = fma_rn(row[kx], wrow[kx], sum);
         }
     out[((size_t)z * ny + y) * nx + x] = sum;
+}
+
+// The same filter for odd ksize = 2H+1 with H <= 2, register-blocked along
+// z: a thread owns one (x, y) column of TZ outputs and walks the input planes
+// once.  It keeps the K = 2H+1 outputs a plane reaches in a rotating window
+// of accumulators: output zo = pl - 2H + k sits in acc[k] and takes tap
+// kz = 2H - k of plane pl; after the plane acc[0] is complete and the window
+// shifts.  Every output still receives its terms in the reference's order
+// (plane = kz ascending, then ky, then kx), so the result is bitwise that of
+// log_filter_kernel.  Tile 32 x 4 x 32 outputs, 128 threads.
+template <int H>
+__global__ void __launch_bounds__(128) log_filter_zblock_kernel(const float* __restrict__ in, float* __restrict__ out,
+                                                                uint32_t nx, uint32_t ny, uint32_t nz,
+                                                                const __grid_constant__ LogTaps<H> taps) {
+    constexpr int K = 2 * H + 1, TX = 32, TY = 4, TZ = 32;
+    constexpr int EX = TX + 2 * H, EY = TY + 2 * H, EZ = TZ + 2 * H;
+    __shared__ float tile[EZ][EY][EX];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    // Fill in batches: a thread's loads of a batch are in flight together.
+    constexpr int NT = TX * TY, NE = EX * EY * EZ, B = 8;
+    for (int i0 = tid; i0 < NE; i0 += B * NT) {
+        float v[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int i = i0 + u * NT;
+            if (i < NE) {
+                const int lx = i % EX, ly = (i / EX) % EY, lz = i / (EX * EY);
+                const int gx = min(max(x0 + lx - H, 0), (int)nx - 1);
+                const int gy = min(max(y0 + ly - H, 0), (int)ny - 1);
+                const int gz = min(max(z0 + lz - H, 0), (int)nz - 1);
+                v[u] = in[((size_t)gz * ny + gy) * nx + gx];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (i0 + u * NT < NE) (&tile[0][0][0])[i0 + u * NT] = v[u];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool col_ok = x < (int)nx && y < (int)ny;
+    float acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0.f;
+#pragma unroll 1
+    for (int pl = 0; pl < EZ; ++pl) {
+#pragma unroll
+        for (int ky = 0; ky < K; ++ky) {
+            float r[K];
+#pragma unroll
+            for (int kx = 0; kx < K; ++kx) r[kx] = tile[pl][ty + ky][tx + kx];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int kz = 2 * H - k;
+#pragma unroll
+                for (int kx = 0; kx < K; ++kx) acc[k] = fma_rn(r[kx], taps.w[(kz * K + ky) * K + kx], acc[k]);
+            }
+        }
+        const int zo = pl - 2 * H;  // acc[0] is complete
+        if (zo >= 0 && col_ok && z0 + zo < (int)nz) out[((size_t)(z0 + zo) * ny + y) * nx + x] = acc[0];
+#pragma unroll
+        for (int k = 0; k < K - 1; ++k) acc[k] = acc[k + 1];
+        acc[K - 1] = 0.f;
+    }
 }
 
 // ------------------------------------------------------- Laplacian filter --
@@ -235,12 +318,22 @@ fbp_status log_weights_host(int size, float std1, float* w_final) {
 
 template <int H>
 static fbp_status log_h(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz, int ksize,
-                        cudaStream_t stream) {
+                        const float* w, cudaStream_t stream) {
+    LogTaps<H> taps{};
+    for (int i = 0; i < ksize * ksize * ksize; ++i) taps.w[i] = w[i];
+    if constexpr (H >= 1 && H <= 2) {
+        if (ksize == 2 * H + 1) {
+            dim3 grid(cdiv(nx, 32), cdiv(ny, 4), cdiv(nz, 32));
+            log_filter_zblock_kernel<H><<<grid, dim3(32, 4), 0, stream>>>(in, out, nx, ny, nz, taps);
+            FBP_CHECK_LAUNCH(ctx, "log_filter_zblock_kernel");
+            return FBP_OK;
+        }
+    }
     constexpr int E = 8 + 2 * H;
     const size_t smem = sizeof(float) * E * E * E;
     FBP_TRY_CUDA(cudaFuncSetAttribute(log_filter_kernel<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(cdiv(nx, 8), cdiv(ny, 8), cdiv(nz, 8));
-    log_filter_kernel<H><<<grid, dim3(8, 8, 8), smem, stream>>>(in, out, nx, ny, nz, ksize);
+    log_filter_kernel<H><<<grid, dim3(8, 8, 8), smem, stream>>>(in, out, nx, ny, nz, ksize, taps);
     FBP_CHECK_LAUNCH(ctx, "log_filter_kernel");
     return FBP_OK;
 }
@@ -263,18 +356,16 @@ fbp_status launch_log(fbp_context* ctx, const float* in, float* out, uint32_t nx
         return set_error(FBP_ERR_UNSUPPORTED, "LoG filter: kernel size must be in [1, 15]");
     std::vector<float> w((size_t)ksize * ksize * ksize);
     FBP_TRY(log_weights_host(ksize, sigma, w.data()));
-    FBP_TRY_CUDA(cudaMemcpyToSymbolAsync(c_log_weights, w.data(), w.size() * sizeof(float), 0,
-                                         cudaMemcpyHostToDevice, stream));
     // The reference's kernelHalf = (k - 1) / 2 (PostprocessingFilters.cu:25).
     switch ((ksize - 1) / 2) {
-        case 0: return log_h<0>(ctx, in, out, nx, ny, nz, ksize, stream);
-        case 1: return log_h<1>(ctx, in, out, nx, ny, nz, ksize, stream);
-        case 2: return log_h<2>(ctx, in, out, nx, ny, nz, ksize, stream);
-        case 3: return log_h<3>(ctx, in, out, nx, ny, nz, ksize, stream);
-        case 4: return log_h<4>(ctx, in, out, nx, ny, nz, ksize, stream);
-        case 5: return log_h<5>(ctx, in, out, nx, ny, nz, ksize, stream);
-        case 6: return log_h<6>(ctx, in, out, nx, ny, nz, ksize, stream);
-        default: return log_h<7>(ctx, in, out, nx, ny, nz, ksize, stream);
+        case 0: return log_h<0>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
+        case 1: return log_h<1>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
+        case 2: return log_h<2>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
+        case 3: return log_h<3>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
+        case 4: return log_h<4>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
+        case 5: return log_h<5>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
+        case 6: return log_h<6>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
+        default: return log_h<7>(ctx, in, out, nx, ny, nz, ksize, w.data(), stream);
     }
 }
 
