@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-capture batched leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-MIS leg")
     ap.add_argument("--no-configs", action="store_true", help="skip the LCT / exhaustive / filter legs")
+    ap.add_argument("--mode", choices=["weak", "slabs"], default="weak",
+                    help="multi-GPU: weak = one capture per rank; slabs = the same capture split into depth slabs "
+                         "(strong scaling; each rank uploads only its slab's bin window in the e2e leg)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     a = ap.parse_args()
     a.small = a.size != "full"
@@ -216,6 +219,8 @@ def run_ours(args):
     ws, rank, local = dist_setup("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.mode == "slabs":
+        return run_slabs(args, ws, rank, local, dev)
     cap, info = make_workload(dev, 2 + rank, args.size)
     L = info.num_laser_targets
     V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
@@ -341,6 +346,79 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(info, cube, lx)
         line.update(extras)
     line["clocks"] = clk.summary()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_slabs(args, ws, rank, local, dev):
+    """Strong scaling: every rank reconstructs its depth slab of the same
+    capture (backprojection only; the LoG would need halos across slabs).
+    value = all ranks' voxel-samples / max-over-ranks time.  e2e: each rank
+    copies only its slab's bin window from pinned host memory and reads its
+    slab back."""
+    import torch
+
+    from fasterbackprojection_gb300 import Context, slabs
+
+    cap, info = make_workload(dev, 2, args.size)
+    ctx = Context(local)
+    L = info.num_laser_targets
+    vx, vy, vz = info.voxel_res
+    z0, z1 = slabs.plan(info, ws)[rank]
+    cube, lx = cap.cube.contiguous(), cap.laser_xyz.contiguous()
+    slab = torch.empty((max(z1 - z0, 0), vy, vx), device=dev)
+
+    def step():
+        if z1 > z0:
+            ctx.backproject_confocal_slab(info, cube, lx, z0, z1, out=slab)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    stream = torch.cuda.current_stream()
+    launches0 = ctx.launches
+    with ClockSampler(local) as clk:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            step()
+        b.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    launches = ctx.launches - launches0
+    ms = max_over_ranks(a.elapsed_time(b), ws, dev) / args.steps
+    total = vx * vy * vz * L
+    e2e = None
+    if not args.no_e2e:
+        host_cube = torch.empty(cube.shape, dtype=cube.dtype, pin_memory=True)
+        host_cube.copy_(cube)
+        host_lx = lx.cpu().numpy()
+        host_slab = torch.empty(tuple(slab.shape), dtype=torch.float32, pin_memory=True)
+        h2d = 0
+        for _ in range(max(1, args.warmup)):
+            s, _, h2d = slabs.reconstruct_rank(ctx, info, host_cube, host_lx, rank, ws, dev)
+            host_slab.copy_(s)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s, _, h2d = slabs.reconstruct_rank(ctx, info, host_cube, host_lx, rank, ws, dev)
+            host_slab.copy_(s)
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(time.perf_counter() - t0, ws, dev)
+        e2e = {"value": total * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(host_slab.numel() * 4), "note": "rank 0's bytes"}
+    line = {
+        "metric": METRIC, "value": total / (ms / 1e3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 8-patch scene), generated on device",
+        "config": {"workload": "confocal_bp_slabs_" + WORKLOAD, "volume": list(info.voxel_res),
+                   "slabs": slabs.plan(info, ws), "postfilter": "none (slab mode)",
+                   "l2": "inputs larger than L2 (cube 256 MiB)"},
+        "e2e": e2e, "gpu_launches": launches, "clocks": clk.summary(),
+    }
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

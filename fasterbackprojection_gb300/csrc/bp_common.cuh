@@ -90,6 +90,9 @@ fbp_status plan_window(const fbp_context* ctx, double ex, double ey, double ez, 
 
 // The confocal gather over all scan points (smp == nullptr) or over K sampled
 // scan points per tile (the unbiased MIS estimator).
+fbp_status confocal_gather_slab(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype, int layout,
+                                const float* laser_xyz, uint32_t z_begin, uint32_t z_end, float* volume,
+                                cudaStream_t s);
 fbp_status confocal_gather(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype, int layout,
                            const float* laser_xyz, float* volume, cudaStream_t s, const SampleParams* smp);
 void confocal_tile_grid(const fbp_recon_info& in, uint32_t out[3]);

@@ -173,11 +173,18 @@ fbp_status dispatch_confocal(fbp_context* ctx, const ConfocalGatherParams& p, di
     return go_confocal<S, PATH_FAST, false, SAMPLED, false>(ctx, p, grid, smem, stream);
 }
 
+// Depth slices [z_begin, z_end) of the volume (the whole volume by default)
+// into `volume` ([z_end - z_begin][Vy][Vx]).  The window plan and the voxel
+// tables are those of the whole volume, so with z_begin a multiple of the
+// tile depth a slab is bitwise the same rows of the full result.
 template <typename S>
 fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int layout,
-                           const float* laser_xyz, float* volume, cudaStream_t stream, const SampleParams* smp) {
+                           const float* laser_xyz, float* volume, cudaStream_t stream, const SampleParams* smp,
+                           uint32_t z_begin = 0, uint32_t z_end = 0xFFFFFFFFu) {
     const uint32_t L = in.num_laser_targets, T = in.num_time_bins;
     const uint32_t Vx = in.voxel_res[0], Vy = in.voxel_res[1], Vz = in.voxel_res[2];
+    if (z_end > Vz) z_end = Vz;
+    if (z_begin >= z_end) return FBP_OK;
     constexpr int ALIGN = 16 / sizeof(S);
 
     // World extents of the largest tile (clamped to the volume).
@@ -199,14 +206,15 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     p.rows = rows;
     p.volume = volume;
     p.status = ctx->status_dev;
-    p.Vx = Vx; p.Vy = Vy; p.Vz = Vz; p.L = L; p.T = T;
+    p.ys += z_begin;
+    p.Vx = Vx; p.Vy = Vy; p.Vz = z_end - z_begin; p.L = L; p.T = T;
     p.t0 = in.time_offset;
     p.dt = in.time_step;
     p.row_pitch = wp.pitch;
     p.slot_w = wp.slot_w;
     p.ch = wp.ch;
     if (smp) p.smp = *smp;
-    dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(Vz, 4 * kWZ));
+    dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(z_end - z_begin, 4 * kWZ));
     const bool bounce = in.discard_first_last_bounces == 0;
     if (smp) return dispatch_confocal<S, true>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
     return dispatch_confocal<S, false>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
@@ -227,6 +235,18 @@ fbp_status confocal_gather(fbp_context* ctx, const fbp_recon_info& in, const voi
         case FBP_F32: return launch_confocal<float>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
         case FBP_BF16: return launch_confocal<__nv_bfloat16>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
         case FBP_F16: return launch_confocal<__half>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
+        default: return set_error(FBP_ERR_INVALID_ARG, "unknown dtype");
+    }
+}
+
+fbp_status confocal_gather_slab(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype, int layout,
+                                const float* laser_xyz, uint32_t z_begin, uint32_t z_end, float* volume,
+                                cudaStream_t s) {
+    switch (dtype) {
+        case FBP_F32: return launch_confocal<float>(ctx, in, cube, layout, laser_xyz, volume, s, nullptr, z_begin, z_end);
+        case FBP_BF16:
+            return launch_confocal<__nv_bfloat16>(ctx, in, cube, layout, laser_xyz, volume, s, nullptr, z_begin, z_end);
+        case FBP_F16: return launch_confocal<__half>(ctx, in, cube, layout, laser_xyz, volume, s, nullptr, z_begin, z_end);
         default: return set_error(FBP_ERR_INVALID_ARG, "unknown dtype");
     }
 }

@@ -182,6 +182,29 @@ fbp_status fbp_mis_reference_tables(fbp_context* ctx, const fbp_recon_info* info
 /* Voxel tiles of the gather / MIS sampling: tiles[0..2] along (vx, vy, vz). */
 fbp_status fbp_mis_tile_grid(const fbp_recon_info* info, uint32_t tiles[3]);
 
+/* ---- depth-slab partition across ranks ------------------------------------ */
+
+/* No counterpart in the reference (it runs on one GPU).  Voxels are
+ * independent, so ranks reconstruct contiguous ranges of depth slices of the
+ * same capture with no collective on the data path; the slabs are gathered
+ * afterwards.
+ * fbp_plan_slabs: z_bounds[0..nranks] (nranks + 1 entries), slab r is
+ * [z_bounds[r], z_bounds[r+1]); boundaries are multiples of 16 (the gather's
+ * tile depth) except the last (= voxel_res[2]); balanced by tile rows. */
+fbp_status fbp_plan_slabs(const fbp_recon_info* info, uint32_t nranks, uint32_t* z_bounds);
+/* Bins [*bin_lo, *bin_hi] that any voxel of slices [z_begin, z_end) can reach
+ * from any scan point (FP64 box distances, 2 bins of margin, clamped to
+ * [0, T-1]; *bin_lo > *bin_hi if none).  laser_xyz: HOST array, L*3.  A rank
+ * may copy only these bins of the capture to its GPU (zeros elsewhere). */
+fbp_status fbp_slab_bin_window(const fbp_recon_info* info, const float* laser_xyz, uint32_t z_begin, uint32_t z_end,
+                               uint32_t* bin_lo, uint32_t* bin_hi);
+/* fbp_backproject_confocal restricted to slices [z_begin, z_end) into
+ * volume_slab[z_end - z_begin][Vy][Vx]; with z_begin a multiple of 16 the
+ * slab is bitwise the same rows of the full volume. */
+fbp_status fbp_backproject_confocal_slab(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
+                                         int layout, const float* laser_xyz, uint32_t z_begin, uint32_t z_end,
+                                         float* volume_slab, void* stream);
+
 /* ---- learned MIS proposal (MLP on the tensor cores) ----------------------- */
 
 /* No counterpart in the reference: its MIS proposal is the spatial alias table
