@@ -32,12 +32,16 @@ struct ExhaustiveGatherParams {
     int ch;
 
     __host__ __device__ static constexpr size_t meta_bytes(int ch) {
-        return ((size_t)2 * ch * (2 * sizeof(float4) + sizeof(float) + 3 * sizeof(int)) + 2 * sizeof(int) + 15) &
+        return ((size_t)2 * ch * (2 * sizeof(float4) + sizeof(float) + 4 * sizeof(int)) + 2 * sizeof(int) + 15) &
                ~size_t(15);
     }
 };
 
-template <typename S, int KV, int WY, int WZ, bool BOUNCE, bool EXACT_TRUNC>
+// LB = 4: pairs are walked as (laser block of 4, SPAD, laser in block), so
+// the SPAD-to-voxel distance is computed once per SPAD for 4 lasers (the 4
+// laser distances are kept per block); requires L % 4 == 0 and ch % 4 == 0.
+// LB = 1: pairs in (laser, SPAD) order.
+template <typename S, int KV, int WY, int WZ, bool BOUNCE, bool EXACT_TRUNC, int LB>
 __global__ void __launch_bounds__(32 * WY * WZ)
 exhaustive_gather_kernel(ExhaustiveGatherParams p) {
     constexpr int NT = 32 * WY * WZ;
@@ -54,7 +58,8 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
     int* s_cnt = reinterpret_cast<int*>(s_cl + 2 * CHMAX);
     int* s_src = s_cnt + 2 * CHMAX;
     int* s_lid = s_src + 2 * CHMAX;
-    int* s_flag = s_lid + 2 * CHMAX;
+    int* s_row = s_lid + 2 * CHMAX;
+    int* s_flag = s_row + 2 * CHMAX;
     S* s_slots = reinterpret_cast<S*>(smem_raw + ExhaustiveGatherParams::meta_bytes(CHMAX));
 
     const int tid = threadIdx.x;
@@ -98,9 +103,18 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
             const uint64_t ls = c * CH + tid;
             float4 lg = make_float4(0.f, 0.f, 0.f, 0.f), sg = lg;
             float cl = 0.f;
-            int cnt = 0, src = 0, near = 0, lid = -1;
+            int cnt = 0, src = 0, near = 0, lid = -1, row = 0;
             if (ls < npairs) {
-                const uint32_t l = (uint32_t)(ls / p.S), s = (uint32_t)(ls % p.S);
+                uint32_t l, s;
+                if (LB == 1) {
+                    l = (uint32_t)(ls / p.S);
+                    s = (uint32_t)(ls % p.S);
+                } else {
+                    const uint64_t grp = ls / LB;
+                    l = (uint32_t)(grp / p.S) * LB + (uint32_t)(ls % LB);
+                    s = (uint32_t)(grp % p.S);
+                }
+                row = (int)(l * p.S + s);
                 lg = p.lscan[l];
                 sg = p.sscan[s];
                 lid = (int)l;
@@ -136,6 +150,7 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
             s_cnt[buf * CHMAX + tid] = cnt;
             s_src[buf * CHMAX + tid] = src;
             s_lid[buf * CHMAX + tid] = lid;
+            s_row[buf * CHMAX + tid] = row;
             const unsigned any_near = __ballot_sync(CH >= 32 ? 0xffffffffu : ((1u << CH) - 1u), near);
             if (tid == 0) s_flag[buf] = any_near != 0;
         }
@@ -146,18 +161,58 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
         for (uint32_t i = tid; i < CH * vecs; i += NT) {
             const uint32_t s = i / vecs, j = i - s * vecs;
             if ((int)(j * ALIGN) < s_cnt[buf * CHMAX + s]) {
-                const uint64_t ls = c * CH + s;
-                const S* src = static_cast<const S*>(p.rows) + ls * p.row_pitch + s_src[buf * CHMAX + s] + j * ALIGN;
+                const uint64_t row = (uint32_t)s_row[buf * CHMAX + s];
+                const S* src = static_cast<const S*>(p.rows) + row * p.row_pitch + s_src[buf * CHMAX + s] + j * ALIGN;
                 cp_async_16(s_slots + (size_t)(buf * CH + s) * slot_stride + j * ALIGN, src);
             }
         }
         cp_async_commit();
     };
 
-    float acc[KV], ksum[KV], kcomp[KV], dl[KV];
+    float acc[KV], ksum[KV], kcomp[KV], dl[LB][KV];
 #pragma unroll
-    for (int k = 0; k < KV; ++k) acc[k] = ksum[k] = kcomp[k] = dl[k] = 0.f;
+    for (int k = 0; k < KV; ++k) acc[k] = ksum[k] = kcomp[k] = 0.f;
+#pragma unroll
+    for (int li = 0; li < LB; ++li)
+#pragma unroll
+        for (int k = 0; k < KV; ++k) dl[li][k] = 0.f;
     int cur_l = -1;
+    int buf_cur = 0;  // buffer of the stage being accumulated
+
+    // Triples of pair i of the stage in buffer buf with the laser distances
+    // dl[li] and the SPAD distances ds (transient_reconstruction.cuh:155-162).
+    auto pair_terms = [&](int i, int li, const float (&ds)[KV], bool safe) {
+        const float4 lg = s_lg[buf_cur * CHMAX + i];
+        const float4 sg = s_sg[buf_cur * CHMAX + i];
+        const float cl = s_cl[buf_cur * CHMAX + i];
+        const S* slot = s_slots + (size_t)(buf_cur * CH + i) * slot_stride;
+        const float bnc = BOUNCE ? add_rn(lg.w, sg.w) : 0.f;
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+            float dist = sub_rn(add_rn(dl[li][k], ds[k]), p.t0);
+            if (BOUNCE) dist = add_rn(dist, bnc);
+            const float x = ref_bin_ratio(dist, rcp_dt);
+            uint32_t idx;
+            if (EXACT_TRUNC) {
+                idx = min((uint32_t)(__float2int_rz(x) - __float_as_int(cl)), p.slot_w);
+            } else {
+                idx = min(__float_as_uint(add_rz(x, cl)) - 0x4B000000u, p.slot_w);
+            }
+            const float I = to_f32(slot[idx]);
+            const float dd = mul_rn(dist, dist);
+            const float w = safe ? ref_safe_rcp(dd) : rcp_approx(dd);
+            acc[k] = fmaf(I, w, acc[k]);
+        }
+    };
+    auto point_dist = [&](const float4& g, float (&d)[KV]) {
+        const float ddy = sub_rn(py, g.y), ddz = sub_rn(pz, g.z);
+        const float ddy2 = mul_rn(ddy, ddy);
+#pragma unroll
+        for (int k = 0; k < KV; ++k) {
+            const float dx = sub_rn(px[k], g.x);
+            d[k] = sqrt_approx(fma_rn(ddz, ddz, fma_rn(dx, dx, ddy2)));
+        }
+    };
 
     if (nchunks > 0) {
         plan_chunk(0, 0);
@@ -166,6 +221,7 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
     }
     for (uint64_t c = 0; c < nchunks; ++c) {
         const int buf = (int)(c & 1);
+        buf_cur = buf;
         __syncthreads();  // every thread is done with chunk c-1, whose buffer plan(c+1) reuses
         if (c + 1 < nchunks) plan_chunk(c + 1, buf ^ 1);
         __syncthreads();  // plan(c+1) visible to the copy loop
@@ -179,43 +235,29 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
 
         const bool safe = s_flag[buf] != 0;
         const int np = (int)min((uint64_t)CH, npairs - c * CH);
-        for (int i = 0; i < np; ++i) {
-            const float4 lg = s_lg[buf * CHMAX + i];
-            const float4 sg = s_sg[buf * CHMAX + i];
-            const float cl = s_cl[buf * CHMAX + i];
-            const int lid = s_lid[buf * CHMAX + i];
-            const S* slot = s_slots + (size_t)(buf * CH + i) * slot_stride;
-            if (lid != cur_l) {  // uniform across the CTA
-                cur_l = lid;
-                const float ldy = sub_rn(py, lg.y), ldz = sub_rn(pz, lg.z);
-                const float ldy2 = mul_rn(ldy, ldy);
-#pragma unroll
-                for (int k = 0; k < KV; ++k) {
-                    const float dx = sub_rn(px[k], lg.x);
-                    dl[k] = sqrt_approx(fma_rn(ldz, ldz, fma_rn(dx, dx, ldy2)));
+        if (LB == 1) {
+            for (int i = 0; i < np; ++i) {
+                const int lid = s_lid[buf * CHMAX + i];
+                if (lid != cur_l) {  // uniform across the CTA
+                    cur_l = lid;
+                    point_dist(s_lg[buf * CHMAX + i], dl[0]);
                 }
+                float ds[KV];
+                point_dist(s_sg[buf * CHMAX + i], ds);
+                pair_terms(i, 0, ds, safe);
             }
-            const float sdy = sub_rn(py, sg.y), sdz = sub_rn(pz, sg.z);
-            const float sdy2 = mul_rn(sdy, sdy);
-            const float bnc = BOUNCE ? add_rn(lg.w, sg.w) : 0.f;
+        } else {
+            for (int g = 0; g < np; g += LB) {
+                const int lb = s_lid[buf * CHMAX + g] / LB;
+                if (lb != cur_l) {  // a new block of LB lasers (uniform across the CTA)
+                    cur_l = lb;
 #pragma unroll
-            for (int k = 0; k < KV; ++k) {
-                const float dx = sub_rn(px[k], sg.x);
-                const float ds = sqrt_approx(fma_rn(sdz, sdz, fma_rn(dx, dx, sdy2)));
-                // transient_reconstruction.cuh:155-157
-                float dist = sub_rn(add_rn(dl[k], ds), p.t0);
-                if (BOUNCE) dist = add_rn(dist, bnc);
-                const float x = ref_bin_ratio(dist, rcp_dt);
-                uint32_t idx;
-                if (EXACT_TRUNC) {
-                    idx = min((uint32_t)(__float2int_rz(x) - __float_as_int(cl)), p.slot_w);
-                } else {
-                    idx = min(__float_as_uint(add_rz(x, cl)) - 0x4B000000u, p.slot_w);
+                    for (int li = 0; li < LB; ++li) point_dist(s_lg[buf * CHMAX + g + li], dl[li]);
                 }
-                const float I = to_f32(slot[idx]);
-                const float dd = mul_rn(dist, dist);
-                const float w = safe ? ref_safe_rcp(dd) : rcp_approx(dd);
-                acc[k] = fmaf(I, w, acc[k]);
+                float ds[KV];
+                point_dist(s_sg[buf * CHMAX + g], ds);  // the group's SPAD
+#pragma unroll
+                for (int li = 0; li < LB; ++li) pair_terms(g + li, li, ds, safe);
             }
         }
 #pragma unroll
@@ -319,12 +361,20 @@ fbp_status launch_exhaustive(fbp_context* ctx, const fbp_recon_info& in, const v
         FBP_CHECK_LAUNCH(ctx, "exhaustive_gather_kernel");
         return FBP_OK;
     };
-    if (bounce) {
-        if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, true>);
-        return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, false>);
+    if (L % 4 == 0 && wp.ch % 4 == 0) {
+        if (bounce) {
+            if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, true, 4>);
+            return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, false, 4>);
+        }
+        if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, true, 4>);
+        return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, false, 4>);
     }
-    if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, true>);
-    return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, false>);
+    if (bounce) {
+        if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, true, 1>);
+        return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, true, false, 1>);
+    }
+    if (exact) return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, true, 1>);
+    return go(exhaustive_gather_kernel<S, kKV, kWY, kWZ, false, false, 1>);
 }
 
 }  // namespace
