@@ -319,6 +319,7 @@ def run_ours(args):
         if not args.no_learned:
             extras["learned_mis"] = learned_mis_leg(ctx, dev, info, cube, lx)
         if not args.no_configs:
+            extras["reference_kernels"] = reference_kernels_leg(ctx, dev, info, cube, lx, vol)
             pk = measured_peaks()[0]
             extras["filters"] = filters_leg(ctx, dev, vol, cube, info.time_step, pk)
             extras["lct"] = lct_leg(ctx, dev, pk)
@@ -456,6 +457,87 @@ def reference_cuda_rate(info, cube, lx, dev):
     del cube_tm
     return {"kernel": "backprojectConfocalVoxel (reference, sm_103a, fast math)", "value": samples / (ms / 1e3),
             "unit": UNIT, "sample": f"{nz} of {info.voxel_res[2]} depth slices", "ms": ms}
+
+
+def reference_kernels_leg(ctx, dev, info, cube, lx, vol):
+    """Our kernels next to the reference's own kernels (compiled from its
+    sources, oracle/_ref) on the same GPU and data: LoG (k=5), Laplacian (k=5)
+    and min-max normalisation on the 256^3 volume, the one-sample-per-voxel
+    MIS kernel, depth-plane backprojection (64^2 x 512, 200 planes) and the
+    exhaustive kernel on an L == S capture (16^2 x 16^2, the only shape it
+    indexes correctly).  Each entry: ours_ms, reference_ms, speedup, and
+    whether the outputs are bitwise equal (where the arithmetic is the
+    reference's)."""
+    import numpy as np
+    import torch
+
+    from fasterbackprojection_gb300 import (FBP_EXHAUSTIVE, FBP_FILTER_LAPLACIAN, FBP_FILTER_LOG, FBP_MIS_REFERENCE,
+                                            make_info, scenes)
+    from fasterbackprojection_gb300.api import linear_space, log_weights
+
+    try:
+        from oracle import harness
+    except Exception as e:  # pragma: no cover
+        return {"unavailable": f"harness import failed: {e}"}
+    if not harness.available():
+        return {"unavailable": "reference kernels not built (needs the reference sources at build time)"}
+    harness.load()
+    out = {}
+
+    def both(name, ours, ref, reps=3, compare=True):
+        o, o_ms = timed_ms(ours, reps)
+        r, r_ms = timed_ms(ref, reps)
+        e = {"ours_ms": o_ms, "reference_ms": r_ms, "speedup": r_ms / o_ms}
+        if compare:
+            e["bitwise_equal"] = bool(torch.equal(o, r))
+            e["rel_l2"] = float(torch.linalg.vector_norm((o - r).double()) /
+                                max(float(torch.linalg.vector_norm(r.double())), 1e-30))
+        out[name] = e
+
+    w5 = torch.from_numpy(log_weights(5, 1.0)).to(dev)
+    both("log_k5_256^3", lambda: ctx.postfilter(FBP_FILTER_LOG, vol, 5, 1.0), lambda: harness.log_filter(vol, w5, 5))
+    both("laplacian_k5_256^3", lambda: ctx.postfilter(FBP_FILTER_LAPLACIAN, vol, 5),
+         lambda: harness.laplacian_filter(vol, 5))
+    a, b = vol.clone(), vol.clone()
+    both("normalize_256^3", lambda: ctx.normalize_(a.copy_(vol)), lambda: harness.normalize_(b.copy_(vol)))
+    # MIS (the reference's one-sample balance-heuristic kernel): 64 samples per
+    # voxel over the whole 256^3 volume.  Ours includes the per-call proposal
+    # tables (scan totals on the GPU, Vose alias on the host, as the
+    # reference's host code builds them); the reference column is its kernel
+    # alone.  With more than one sample the reference's += races, so only
+    # the one-sample case is compared bitwise (tests).
+    V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
+    noise = torch.rand(V, generator=torch.Generator().manual_seed(5)).to(dev)
+    cdf, alias, prob = ctx.mis_reference_tables(info, cube)
+    cdf_t, alias_t, prob_t = (torch.from_numpy(cdf).to(dev), torch.from_numpy(alias.astype(np.int32)).to(dev),
+                              torch.from_numpy(prob).to(dev))
+    cube_tm = cube.t().contiguous()
+    both("mis_reference_64_samples_256^2x1024_to_256^3",
+         lambda: ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE, 64, noise=noise),
+         lambda: harness.confocal_voxel_mis(info, cube_tm, lx, cdf_t, noise, alias_t, prob_t, 64), reps=2,
+         compare=False)
+    del cube_tm
+    # Depth planes (confocal, 64^2 x 512, 200 planes around 0.8 m).
+    cap = scenes.confocal_points(64, 512, 32e-12, n_points=200, seed=1)
+    dinfo = make_info(num_laser_targets=4096, num_time_bins=512, time_step=cap.time_step, voxel_res=(1, 1, 1),
+                      hidden_min=(0, 0, 0), voxel_size=(1, 1, 1))
+    dc = torch.from_numpy(cap.cube).to(dev)
+    dlx = torch.from_numpy(cap.laser_xyz).to(dev)
+    depths = torch.from_numpy(linear_space(0.7, 0.9, 200)).to(dev)
+    dtm = dc.t().contiguous()
+    both("depth_planes_64^2x512_200", lambda: ctx.backproject_depths(dinfo, dc, dlx, depths),
+         lambda: harness.depth_confocal(dinfo, dtm, dlx, depths))
+    # Exhaustive on L == S = 16^2, 8 of 128 depth slices.
+    ecap = scenes.exhaustive_points(16, 16, 1024, 16e-12, n_points=100, seed=3)
+    hmin, vs = scenes.volume_geometry((128, 128, 128), depth_range=(0.0, 1.5))
+    einfo = make_info(num_laser_targets=256, num_sensor_targets=256, num_time_bins=1024, time_step=ecap.time_step,
+                      voxel_res=(128, 128, 8), hidden_min=hmin, voxel_size=vs, capture_system=FBP_EXHAUSTIVE)
+    ec = torch.from_numpy(ecap.cube).to(dev)
+    elx, esx = torch.from_numpy(ecap.laser_xyz).to(dev), torch.from_numpy(ecap.sensor_xyz).to(dev)
+    both("exhaustive_16^2x16^2x1024_8_slices", lambda: ctx.backproject_exhaustive(einfo, ec, elx, esx),
+         lambda: harness.exhaustive_voxel(einfo, ec, elx, esx))
+    ctx.check_device_status()
+    return out
 
 
 def fp64_error(ctx, info, cube, lx, vol, nvox=512, seed=5):
