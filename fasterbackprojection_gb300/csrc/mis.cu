@@ -100,37 +100,56 @@ __global__ void mis_reference_kernel(MisRefParams p) {
     const float invL = ref_safe_rcp((float)p.L);
     const S* rows = static_cast<const S*>(p.rows);
     float ksum = 0.f, kcomp = 0.f, acc = 0.f;
-    for (uint32_t s = 0; s < p.samples; ++s) {
-        uint32_t state = (uint32_t)(slice * vz + vs + s);  // transient_reconstruction.cuh:209
-        uint32_t l;
-        float pdf, gpdf;
-        if (noise_next(p.noise, p.noise_size, state) < 0.5f) {
-            const float r1 = noise_next(p.noise, p.noise_size, state);
-            const float r2 = noise_next(p.noise, p.noise_size, state);
-            const uint32_t k = min((uint32_t)(r1 * (float)p.L), p.L - 1);
-            l = r2 < p.prob[k] ? k : p.alias[k];
-            pdf = l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l];
-            gpdf = pdf + 1.0f * invL;
-        } else {
-            l = min((uint32_t)(noise_next(p.noise, p.noise_size, state) * (float)p.L), p.L - 1);
-            pdf = 1.0f * invL;
-            gpdf = pdf + (l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l]);
+    // U samples at a time: their dependent load chains (noise, alias, scan
+    // point, cube) are independent of each other and run concurrently; the
+    // terms are still added in sample order.
+    constexpr int U = 4;
+    for (uint32_t s0 = 0; s0 < p.samples; s0 += U) {
+        float a[U], w[U], I[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            a[u] = 0.f;
+            w[u] = 0.f;
+            I[u] = 0.f;
+            const uint32_t s = s0 + u;
+            if (s >= p.samples) continue;
+            uint32_t state = (uint32_t)(slice * vz + vs + s);  // transient_reconstruction.cuh:209
+            uint32_t l;
+            float pdf, gpdf;
+            if (noise_next(p.noise, p.noise_size, state) < 0.5f) {
+                const float r1 = noise_next(p.noise, p.noise_size, state);
+                const float r2 = noise_next(p.noise, p.noise_size, state);
+                const uint32_t k = min((uint32_t)(r1 * (float)p.L), p.L - 1);
+                l = r2 < p.prob[k] ? k : p.alias[k];
+                pdf = l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l];
+                gpdf = pdf + 1.0f * invL;
+            } else {
+                l = min((uint32_t)(noise_next(p.noise, p.noise_size, state) * (float)p.L), p.L - 1);
+                pdf = 1.0f * invL;
+                gpdf = pdf + (l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l]);
+            }
+            const float4 g = p.scan[l];
+            float dist = fma_rn(sqrt_approx(ref_dot3(sub_rn(px, g.x), sub_rn(py, g.y), sub_rn(pz, g.z))), 2.f, -p.t0);
+            if (p.bounce) dist = add_rn(dist, g.w);
+            a[u] = pdf * ref_safe_rcp(gpdf);  // the balance weight
+            const int b = __float2int_rz(ref_bin_ratio(dist, rcp_dt));
+            if (b >= 0 && b < (int)p.T) {
+                I[u] = to_f32(rows[(uint64_t)l * p.pitch + b]);
+                w[u] = ref_safe_rcp(mul_rn(dist, dist));
+            }
         }
-        const float4 g = p.scan[l];
-        float dist = fma_rn(sqrt_approx(ref_dot3(sub_rn(px, g.x), sub_rn(py, g.y), sub_rn(pz, g.z))), 2.f, -p.t0);
-        if (p.bounce) dist = add_rn(dist, g.w);
-        const float mis = pdf * ref_safe_rcp(gpdf);
-        const int b = __float2int_rz(ref_bin_ratio(dist, rcp_dt));
-        if (b >= 0 && b < (int)p.T) {
-            const float I = to_f32(rows[(uint64_t)l * p.pitch + b]);
-            if (I > FBP_EPS) acc += mis * I * ref_safe_rcp(mul_rn(dist, dist));
-        }
-        if ((s & 63) == 63 || s + 1 == p.samples) {
-            const float y = sub_rn(acc, kcomp);
-            const float t = add_rn(ksum, y);
-            kcomp = sub_rn(sub_rn(t, ksum), y);
-            ksum = t;
-            acc = 0.f;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t s = s0 + u;
+            if (s >= p.samples) break;
+            if (I[u] > FBP_EPS) acc = fmaf(a[u] * I[u], w[u], acc);
+            if ((s & 63) == 63 || s + 1 == p.samples) {
+                const float y = sub_rn(acc, kcomp);
+                const float t = add_rn(ksum, y);
+                kcomp = sub_rn(sub_rn(t, ksum), y);
+                ksum = t;
+                acc = 0.f;
+            }
         }
     }
     p.volume[v] = ksum;
