@@ -148,6 +148,8 @@ SIGNATURES = {
                                          c_void_p, c_void_p]),
     "fbp_mis_tile_grid": (c_int, [POINTER(ReconInfo), POINTER(c_uint32)]),
     "fbp_lct": (c_int, [c_void_p, c_void_p, c_int, c_uint32, c_uint32, POINTER(LctParams), c_void_p, c_void_p]),
+    "fbp_backproject_confocal_scatter": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p,
+                                                 c_void_p, c_void_p]),
     "fbp_plan_slabs": (c_int, [POINTER(ReconInfo), c_uint32, POINTER(c_uint32)]),
     "fbp_slab_bin_window": (c_int, [POINTER(ReconInfo), c_void_p, c_uint32, c_uint32, POINTER(c_uint32),
                                     POINTER(c_uint32)]),

@@ -66,6 +66,7 @@ struct ConfocalGatherParams {
     int ch;              // scan points per pipeline stage (<= 32)
     const void* rows;    // [L][row_pitch] of the storage type
     SampleParams smp;    // used by the sampled (MIS) variant only
+    float vs[3];         // voxel size (the voxel-scattering variant's extent)
 
     // Bytes of per-chunk metadata in front of the window slots (16-byte aligned).
     __host__ __device__ static constexpr size_t meta_bytes(int ch) {
@@ -86,10 +87,13 @@ struct WindowPlan {
     size_t smem;
 };
 fbp_status plan_window(const fbp_context* ctx, double ex, double ey, double ez, double time_step, uint32_t T, int align,
-                       size_t elem_bytes, size_t meta_bytes, WindowPlan* out, const char* who);
+                       size_t elem_bytes, size_t meta_bytes, WindowPlan* out, const char* who,
+                       double extra_path = 0.0);
 
 // The confocal gather over all scan points (smp == nullptr) or over K sampled
 // scan points per tile (the unbiased MIS estimator).
+fbp_status confocal_gather_scatter(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype,
+                                   int layout, const float* laser_xyz, float* volume, cudaStream_t s);
 fbp_status confocal_gather_slab(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype, int layout,
                                 const float* laser_xyz, uint32_t z_begin, uint32_t z_end, float* volume,
                                 cudaStream_t s);

@@ -180,7 +180,7 @@ fbp_status dispatch_confocal(fbp_context* ctx, const ConfocalGatherParams& p, di
 template <typename S>
 fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int layout,
                            const float* laser_xyz, float* volume, cudaStream_t stream, const SampleParams* smp,
-                           uint32_t z_begin = 0, uint32_t z_end = 0xFFFFFFFFu) {
+                           uint32_t z_begin = 0, uint32_t z_end = 0xFFFFFFFFu, bool scatter = false) {
     const uint32_t L = in.num_laser_targets, T = in.num_time_bins;
     const uint32_t Vx = in.voxel_res[0], Vy = in.voxel_res[1], Vz = in.voxel_res[2];
     if (z_end > Vz) z_end = Vz;
@@ -193,9 +193,15 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     const double ez = (double)std::min<uint32_t>(8 * kWY, Vy) * std::fabs(in.voxel_size[2]);
     WindowPlan wp;
     // The sampled kernel also holds its cluster list in static shared memory.
+    // The voxel-scattering variant reads every bin of dist -/+ half the voxel
+    // diagonal, one step past the end.
+    const double vdiag = std::sqrt((double)in.voxel_size[0] * in.voxel_size[0] +
+                                   (double)in.voxel_size[1] * in.voxel_size[1] +
+                                   (double)in.voxel_size[2] * in.voxel_size[2]);
+    const double extra = scatter ? 1.02 * vdiag + 2.0 * std::fabs((double)in.time_step) : 0.0;
     FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(S),
                         ConfocalGatherParams::meta_bytes(32) + (smp ? kSampledStaticSmem : 0), &wp,
-                        "fbp_backproject_confocal"));
+                        "fbp_backproject_confocal", extra));
     if (smp) wp.smem -= kSampledStaticSmem;
 
     S* rows = nullptr;
@@ -213,9 +219,14 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     p.row_pitch = wp.pitch;
     p.slot_w = wp.slot_w;
     p.ch = wp.ch;
+    for (int k = 0; k < 3; ++k) p.vs[k] = in.voxel_size[k];
     if (smp) p.smp = *smp;
     dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(z_end - z_begin, 4 * kWZ));
     const bool bounce = in.discard_first_last_bounces == 0;
+    if (scatter) {
+        if (bounce) return go_confocal<S, PATH_SCATTER, true, false, true>(ctx, p, grid, wp.smem, stream);
+        return go_confocal<S, PATH_SCATTER, false, false, true>(ctx, p, grid, wp.smem, stream);
+    }
     if (smp) return dispatch_confocal<S, true>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
     return dispatch_confocal<S, false>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
 }
@@ -235,6 +246,18 @@ fbp_status confocal_gather(fbp_context* ctx, const fbp_recon_info& in, const voi
         case FBP_F32: return launch_confocal<float>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
         case FBP_BF16: return launch_confocal<__nv_bfloat16>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
         case FBP_F16: return launch_confocal<__half>(ctx, in, cube, layout, laser_xyz, volume, s, smp);
+        default: return set_error(FBP_ERR_INVALID_ARG, "unknown dtype");
+    }
+}
+
+fbp_status confocal_gather_scatter(fbp_context* ctx, const fbp_recon_info& in, const void* cube, int dtype,
+                                   int layout, const float* laser_xyz, float* volume, cudaStream_t s) {
+    const uint32_t all = 0xFFFFFFFFu;
+    switch (dtype) {
+        case FBP_F32: return launch_confocal<float>(ctx, in, cube, layout, laser_xyz, volume, s, nullptr, 0, all, true);
+        case FBP_BF16:
+            return launch_confocal<__nv_bfloat16>(ctx, in, cube, layout, laser_xyz, volume, s, nullptr, 0, all, true);
+        case FBP_F16: return launch_confocal<__half>(ctx, in, cube, layout, laser_xyz, volume, s, nullptr, 0, all, true);
         default: return set_error(FBP_ERR_INVALID_ARG, "unknown dtype");
     }
 }
@@ -278,10 +301,11 @@ fbp_status build_tables(fbp_context* ctx, const fbp_recon_info& in, const float*
 }
 
 fbp_status plan_window(const fbp_context* ctx, double ex, double ey, double ez, double time_step, uint32_t T, int align,
-                       size_t elem_bytes, size_t meta_bytes, WindowPlan* out, const char* who) {
+                       size_t elem_bytes, size_t meta_bytes, WindowPlan* out, const char* who, double extra_path) {
     const double diag = std::sqrt(ex * ex + ey * ey + ez * ez);
-    // Round trip across the tile, a 2-bin margin on each side, alignment slack.
-    const double span = 2.0 * diag / std::fabs(time_step) + 8.0 + align;
+    // Round trip across the tile (plus any extra path range), a 2-bin margin
+    // on each side, alignment slack.
+    const double span = (2.0 * diag + extra_path) / std::fabs(time_step) + 8.0 + align;
     const uint32_t t_round = (T + align - 1) / align * align;
     const uint32_t cap = t_round + align;
     uint32_t slot_w = span < (double)cap ? ((uint32_t)std::ceil(span) + align - 1) / align * align : cap;
@@ -323,6 +347,21 @@ fbp_status validate_info(const fbp_recon_info* info, bool need_sensors, const ch
 }  // namespace fbp
 
 using namespace fbp;
+
+extern "C" fbp_status fbp_backproject_confocal_scatter(fbp_context* ctx, const fbp_recon_info* info,
+                                                       const void* cube, int dtype, int layout,
+                                                       const float* laser_xyz, float* volume, void* stream) {
+    clear_error();
+    FBP_TRY(check_ctx(ctx));
+    FBP_TRY(validate_info(info, false, "fbp_backproject_confocal_scatter"));
+    if (!cube || !laser_xyz || !volume)
+        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal_scatter: null buffer");
+    if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
+        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal_scatter: unknown layout");
+    if (!(info->time_step > 1e-4f))
+        return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_confocal_scatter: time_step must exceed 0.1 mm");
+    return confocal_gather_scatter(ctx, *info, cube, dtype, layout, laser_xyz, volume, (cudaStream_t)stream);
+}
 
 extern "C" fbp_status fbp_backproject_confocal(fbp_context* ctx, const fbp_recon_info* info, const void* cube,
                                                int dtype, int layout, const float* laser_xyz, float* volume,

@@ -15,7 +15,11 @@ namespace fbp {
 // In PATH_2D / PATH_FAST the bin is floor(x) - a via a round-toward-zero add of
 // 2^23 - a; without CLAMP the window planner guarantees every bin of the tile
 // lies inside its window, so the -2^23 bias folds into the shared-memory base.
-enum { PATH_2D = 0, PATH_FAST = 1, PATH_EXACT = 2 };
+//   PATH_SCATTER the reference's ACCUMULATE_VOXEL_SCATTERING variant
+//               (transient_reconstruction.cuh:112-126): every bin of the
+//               path range dist -/+ the voxel's half diagonal, stepped by
+//               (dt + EPS) in float like the reference, bins by conversion.
+enum { PATH_2D = 0, PATH_FAST = 1, PATH_EXACT = 2, PATH_SCATTER = 3 };
 
 template <typename S>
 __device__ __forceinline__ float lds_elem(uint32_t addr);
@@ -49,9 +53,43 @@ template <typename S, int KV, int PATH, bool BOUNCE, bool CLAMP, bool SAFE, bool
 __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, const int2* __restrict__ meta,
                                                const float* __restrict__ wts, int nl, const float (&px)[KV], float py,
                                                float pz, float neg_t0, float rcp_dt, uint32_t slot_w,
-                                               float (&acc)[KV]) {
+                                               float (&acc)[KV], float ext = 0.f, float step = 0.f) {
     constexpr int SH = ElemShift<S>::value;
     const float rcp2 = 2.f * rcp_dt;  // exact
+    if constexpr (PATH == PATH_SCATTER) {
+        const int max_it = (int)(2.f * ext / step) + 4;
+        for (int i = 0; i < nl; ++i) {
+            const float4 g = geo[i];
+            const int2 m = meta[i];  // (window start bin a, slot shared address)
+            const float wl = WEIGHTED ? wts[i] : 1.f;
+            const float dy = sub_rn(py, g.y), dz = sub_rn(pz, g.z);
+            const float dy2 = mul_rn(dy, dy);
+#pragma unroll
+            for (int k = 0; k < KV; ++k) {
+                const float dx = sub_rn(px[k], g.x);
+                const float d = sqrt_approx(fma_rn(dz, dz, fma_rn(dx, dx, dy2)));
+                float dist = fma_rn(d, 2.f, neg_t0);
+                if (BOUNCE) dist = add_rn(dist, g.w);
+                const float w = SAFE ? ref_safe_rcp(mul_rn(dist, dist)) : rcp_approx(mul_rn(dist, dist));
+                float dd = fmaxf(0.f, sub_rn(dist, ext));
+                const float dmax = add_rn(dist, ext);
+                float a = acc[k];
+                // The reference adds I * w per bin with an atomic: one rounding
+                // for the product, one for the sum, in bin order.  The count
+                // bound only matters where dist is so large that adding the
+                // step no longer changes it (no such path reaches a bin).
+                for (int it = 0; dd < dmax && it < max_it; ++it) {
+                    const int b = __float2int_rz(ref_bin_ratio(dd, rcp_dt));
+                    float I = lds_elem<S>((uint32_t)m.y + (min((uint32_t)(b - m.x), slot_w) << SH));
+                    if (WEIGHTED) I *= wl;
+                    a = add_rn(a, mul_rn(I, w));
+                    dd = add_rn(dd, step);
+                }
+                acc[k] = a;
+            }
+        }
+        return;
+    }
 #pragma unroll 2
     for (int i = 0; i < nl; ++i) {
         const float4 g = geo[i];
@@ -145,6 +183,10 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
 
     const float rcp_dt = rcp_approx(p.dt);
     const float neg_t0 = -p.t0;
+    // PATH_SCATTER: length(voxelSize) / 2 and the step timeStep + EPS, in the
+    // reference's FP32 arithmetic (transient_reconstruction.cuh:113-125).
+    const float scat_ext = PATH == PATH_SCATTER ? mul_rn(0.5f, sqrt_approx(ref_dot3(p.vs[0], p.vs[1], p.vs[2]))) : 0.f;
+    const float scat_step = PATH == PATH_SCATTER ? add_rn(p.dt, FBP_EPS) : 0.f;
 
     // Sentinels of every slot and the whole zero slot.
     for (int i = tid; i < 2 * CH * ALIGN; i += NT) {
@@ -255,7 +297,11 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                             fz = fmaxf(fabsf(g.z - bz0), fabsf(g.z - bz1));
                 const float dmax = sqrtf(fx * fx + fy * fy + fz * fz);
                 const float bnc = BOUNCE ? g.w : 0.f;
-                const float pmin = 2.f * dmin + neg_t0 + bnc, pmax = 2.f * dmax + neg_t0 + bnc;
+                float pmin = 2.f * dmin + neg_t0 + bnc, pmax = 2.f * dmax + neg_t0 + bnc;
+                if (PATH == PATH_SCATTER) {  // the bins of dist -/+ ext, stepped past dist + ext
+                    pmin = fmaxf(0.f, pmin - 1.01f * scat_ext);
+                    pmax = pmax + 1.01f * scat_ext + scat_step;
+                }
                 // Paths this short make dist^2 <= EPS possible: use safeRCP's branch.
                 near = pmin < 0.0035f;
                 // Conservative bin range with a 2-bin margin for rounding.
@@ -287,7 +333,7 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
             const uint32_t slot_elem = skip ? zero_slot : (uint32_t)(buf * CH + tid) * slot_stride;
             uint32_t saddr = sbase + (uint32_t)slots_off + (slot_elem << SH);
             int bias;
-            if (PATH == PATH_EXACT) {
+            if (PATH == PATH_EXACT || PATH == PATH_SCATTER) {
                 bias = a;
             } else {
                 bias = __float_as_int((float)(8388608 - a));
@@ -296,7 +342,7 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
             if (item >= nitems || l >= p.L) {
                 // Beyond the last scan point: x + 0 < 2^23 lands on the sentinel
                 // (CLAMP) or, unclamped, reads the zero slot at index 0.
-                bias = PATH == PATH_EXACT ? 0x40000000 : 0;
+                bias = (PATH == PATH_EXACT || PATH == PATH_SCATTER) ? 0x40000000 : 0;
                 saddr = sbase + (uint32_t)slots_off + (zero_slot << SH);
                 if (!CLAMP && PATH != PATH_EXACT) saddr -= (__float_as_uint(0.f) << SH);
                 g = make_float4(3.0e18f, 3.0e18f, 3.0e18f, 0.f);  // far away: x is huge
@@ -359,11 +405,11 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
         float scale = 1.f;
         if (!safe) {
             confocal_stage<S, KV, PATH, BOUNCE, CLAMP, false, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
-                                                                        p.slot_w, acc);
+                                                                        p.slot_w, acc, scat_ext, scat_step);
             if (PATH == PATH_2D) scale = 0.25f;  // w was rcp(d^2) = 4 rcp(dist^2)
         } else {
             confocal_stage<S, KV, PATH, BOUNCE, CLAMP, true, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
-                                                                       p.slot_w, acc);
+                                                                       p.slot_w, acc, scat_ext, scat_step);
         }
 
         // Compensated (Kahan) fold of this stage's partial sums.

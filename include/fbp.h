@@ -182,6 +182,15 @@ fbp_status fbp_mis_reference_tables(fbp_context* ctx, const fbp_recon_info* info
 /* Voxel tiles of the gather / MIS sampling: tiles[0..2] along (vx, vy, vz). */
 fbp_status fbp_mis_tile_grid(const fbp_recon_info* info, uint32_t tiles[3]);
 
+/* The reference's ACCUMULATE_VOXEL_SCATTERING build of backprojectConfocalVoxel
+ * (transient_reconstruction.cuh:112-126, a compile-time option there): each
+ * (voxel, scan point) pair adds I(bin) * safeRCP(dist^2) for every bin of
+ * d = max(0, dist - e), d += timeStep + 1e-5 while d < dist + e, with e half
+ * the voxel diagonal, in the reference's FP32 arithmetic and order.
+ * time_step must exceed 1e-4 m. */
+fbp_status fbp_backproject_confocal_scatter(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
+                                            int layout, const float* laser_xyz, float* volume, void* stream);
+
 /* ---- depth-slab partition across ranks ------------------------------------ */
 
 /* No counterpart in the reference (it runs on one GPU).  Voxels are

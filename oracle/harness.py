@@ -15,6 +15,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 LOADER = HERE / "_build" / "libref_loader.so"
 CUBIN = HERE / "_ref" / "ref_kernels.cubin"
+CUBIN_SCATTER = HERE / "_ref" / "ref_kernels_scatter.cubin"  # ACCUMULATE_VOXEL_SCATTERING build
 
 _lib = None
 
@@ -36,6 +37,10 @@ def load():
                  "refk_laplacian_filter", "refk_normalize"]:
         getattr(lib, name).restype = c_int
     lib.refk_load.argtypes = [c_char_p]
+    lib.refk_load_variant.argtypes = [c_char_p]
+    lib.refk_load_variant.restype = c_int
+    lib.refk_select.argtypes = [c_int]
+    lib.refk_select.restype = c_int
     lib.refk_set_state.argtypes = [c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
     lib.refk_set_mis_state.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
     lib.refk_confocal_voxel.argtypes = [c_void_p, c_uint, c_uint, c_uint, c_uint, c_void_p]
@@ -161,3 +166,18 @@ def confocal_voxel_mis(info, cube_time_major, laser_xyz, spatial_sum, noise, ali
     _chk(lib.refk_confocal_voxel_mis(_ptr(spatial_sum), _ptr(vol), _ptr(noise), _ptr(alias), _ptr(prob), vx, vy, vz,
                                      num_samples, noise.numel(), _stream()))
     return vol
+
+
+def scatter_available() -> bool:
+    return available() and CUBIN_SCATTER.exists()
+
+
+def confocal_voxel_scatter(info, cube_time_major, laser_xyz):
+    """backprojectConfocalVoxel of the ACCUMULATE_VOXEL_SCATTERING build."""
+    lib = load()
+    _chk(lib.refk_load_variant(str(CUBIN_SCATTER).encode()))
+    _chk(lib.refk_select(1))
+    try:
+        return confocal_voxel(info, cube_time_major, laser_xyz)
+    finally:
+        _chk(lib.refk_select(0))

@@ -31,6 +31,9 @@
 
 namespace {
 
+// Two builds of the reference kernels: [0] as shipped, [1] with
+// ACCUMULATE_VOXEL_SCATTERING; g_lib is the selected one.
+cudaLibrary_t g_libs[2] = {nullptr, nullptr};
 cudaLibrary_t g_lib = nullptr;
 std::string g_err;
 
@@ -78,9 +81,25 @@ const char* refk_last_error(void) { return g_err.c_str(); }
 
 // Load the cubin built from the reference sources.
 int refk_load(const char* cubin_path) {
-    if (g_lib) return 0;
-    cudaError_t e = cudaLibraryLoadFromFile(&g_lib, cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0);
-    if (e != cudaSuccess) { g_lib = nullptr; return fail("cudaLibraryLoadFromFile", e); }
+    if (g_libs[0]) return 0;
+    cudaError_t e = cudaLibraryLoadFromFile(&g_libs[0], cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) { g_libs[0] = nullptr; return fail("cudaLibraryLoadFromFile", e); }
+    g_lib = g_libs[0];
+    return 0;
+}
+
+// Load the ACCUMULATE_VOXEL_SCATTERING build as variant 1.
+int refk_load_variant(const char* cubin_path) {
+    if (g_libs[1]) return 0;
+    cudaError_t e = cudaLibraryLoadFromFile(&g_libs[1], cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) { g_libs[1] = nullptr; return fail("cudaLibraryLoadFromFile", e); }
+    return 0;
+}
+
+// Select the build the next calls use (0: as shipped, 1: voxel scattering).
+int refk_select(int which) {
+    if (which < 0 || which > 1 || !g_libs[which]) { g_err = "refk_select: build not loaded"; return 1; }
+    g_lib = g_libs[which];
     return 0;
 }
 

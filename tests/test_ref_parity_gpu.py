@@ -191,3 +191,49 @@ def test_normalize_bitwise(ctx, harness, cuda):
     ref = harness.normalize_(v.clone())
     got = ctx.normalize_(v.clone())
     assert torch.equal(ref, got)
+
+
+@pytest.mark.parametrize("mode", ["plain", "bounces", "t0"])
+def test_voxel_scattering_single_scan_bitwise(ctx, harness, cuda, mode):
+    """The ACCUMULATE_VOXEL_SCATTERING build: with one scan point each voxel's
+    bins are added by one reference thread in bin order, so the volume must
+    match bit for bit (ext, step and every visited bin included)."""
+    import torch
+
+    if not harness.scatter_available():
+        pytest.skip("voxel-scattering build of the reference kernels not present")
+    rng = np.random.default_rng({"plain": 11, "bounces": 12, "t0": 13}[mode])
+    T = 2048
+    cube = torch.from_numpy((2.0 ** (np.arange(T) % 3)).astype(np.float32)).to(cuda)
+    mismatch = total = 0
+    for trial in range(8):
+        info = _rand_geometry(rng, 32, T, 0 if mode == "bounces" else 1, 0.6 if mode == "t0" else 0.0,
+                              res=(32, 24, 40))
+        lxyz = torch.tensor([[rng.uniform(-1, 1), 0.0, rng.uniform(-1, 1)]], dtype=torch.float32, device=cuda)
+        ref = harness.confocal_voxel_scatter(info, cube, lxyz)
+        got = ctx.backproject_confocal_scatter(info, cube.view(1, T), lxyz)
+        torch.cuda.synchronize()
+        mismatch += int((ref.view(torch.int32) != got.view(torch.int32)).sum())
+        total += ref.numel()
+    ctx.check_device_status()
+    assert mismatch == 0, f"{mismatch} of {total} voxels differ from the reference kernel"
+
+
+def test_voxel_scattering_multi_scan_matches_reference(ctx, harness, cuda):
+    import torch
+    from fasterbackprojection_gb300 import make_info, scenes
+
+    if not harness.scatter_available():
+        pytest.skip("voxel-scattering build of the reference kernels not present")
+    cap = scenes.confocal_points(12, 512, 32e-12, n_points=30, seed=23)
+    L, T = cap.cube.shape
+    hmin, vs = scenes.volume_geometry((24, 20, 28), depth_range=(0.0, 2.4))
+    info = make_info(num_laser_targets=L, num_time_bins=T, time_step=cap.time_step, voxel_res=(24, 20, 28),
+                     hidden_min=hmin, voxel_size=vs)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lxyz = torch.from_numpy(cap.laser_xyz).to(cuda)
+    ref = harness.confocal_voxel_scatter(info, cube.t().contiguous(), lxyz)
+    got = ctx.backproject_confocal_scatter(info, cube, lxyz)
+    plain = ctx.backproject_confocal(info, cube, lxyz)
+    assert rel_l2(got.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+    assert float(got.sum()) > float(plain.sum())  # several bins per pair
