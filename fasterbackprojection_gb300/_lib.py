@@ -150,6 +150,8 @@ SIGNATURES = {
     "fbp_lct": (c_int, [c_void_p, c_void_p, c_int, c_uint32, c_uint32, POINTER(LctParams), c_void_p, c_void_p]),
     "fbp_backproject_confocal_scatter": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p,
                                                  c_void_p, c_void_p]),
+    "fbp_splat_backproject": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_uint32,
+                                      c_uint32, c_uint32, c_void_p, c_void_p]),
     "fbp_plan_slabs": (c_int, [POINTER(ReconInfo), c_uint32, POINTER(c_uint32)]),
     "fbp_slab_bin_window": (c_int, [POINTER(ReconInfo), c_void_p, c_uint32, c_uint32, POINTER(c_uint32),
                                     POINTER(c_uint32)]),

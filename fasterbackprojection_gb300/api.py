@@ -141,6 +141,19 @@ class Context:
                                                          _ptr(laser_xyz), _ptr(out), self._stream(stream)))
         return out
 
+    def splat_backproject(self, info: ReconInfo, cube, laser_xyz, max_bins: int = 700, grid=(256, 256), out=None,
+                          layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
+        """Scatter-form (rasterised ellipsoid) backprojection, volume [Vz][Vy][Vx]."""
+        import torch
+
+        vx, vy, vz = info.voxel_res
+        if out is None:
+            out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
+        check(self._lib.fbp_splat_backproject(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
+                                              _ptr(laser_xyz), max_bins, grid[0], grid[1], _ptr(out),
+                                              self._stream(stream)))
+        return out
+
     def backproject_confocal_slab(self, info: ReconInfo, cube, laser_xyz, z_begin: int, z_end: int, out=None,
                                   layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
         """Depth slices [z_begin, z_end) of the confocal volume: [z_end - z_begin][Vy][Vx]."""

@@ -191,6 +191,19 @@ fbp_status fbp_mis_tile_grid(const fbp_recon_info* info, uint32_t tiles[3]);
 fbp_status fbp_backproject_confocal_scatter(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
                                             int layout, const float* laser_xyz, float* volume, void* stream);
 
+/* Scatter-form backprojection: the reference's rasterised ellipsoid splat
+ * (DrawEllipsoids.cpp:12-114, 332-440, shaders backprojection-vs/fs.glsl, an
+ * OpenGL path) on CUDA.  Every (scan point, bin < max_bins) with intensity
+ * above FLT_EPSILON is a hemisphere towards -y of radius
+ * (bin * time_step + time_offset [- bounces]) / 2 around the scan point,
+ * sampled at a grid_w x grid_h grid of pixel centres over the volume's x / z
+ * extent; each sample adds the intensity to the voxel it falls in (FP32
+ * atomics, like imageAtomicAdd).  max_bins 0 = all bins (the reference uses
+ * 700).  The volume is overwritten. */
+fbp_status fbp_splat_backproject(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype, int layout,
+                                 const float* laser_xyz, uint32_t max_bins, uint32_t grid_w, uint32_t grid_h,
+                                 float* volume, void* stream);
+
 /* ---- depth-slab partition across ranks ------------------------------------ */
 
 /* No counterpart in the reference (it runs on one GPU).  Voxels are

@@ -132,3 +132,53 @@ def lct(data_tmajor: np.ndarray, width: float, bin_length: float, snr: float = 0
     tvol = np.fft.ifftn(np.fft.fftn(tdata) * invpsf)[:M, :N, :N]
     vol = (mtxi @ tvol.reshape(M, N * N)).reshape(M, N, N)
     return np.maximum(np.real(vol), 0)
+
+
+# ------------------------------------------------------------ ellipsoid splat
+
+def splat_backproject(info, cube, laser_xyz, max_bins=700, grid=(256, 256)) -> np.ndarray:
+    """The rasterised ellipsoid splat (FasterBackprojection/DrawEllipsoids.cpp:
+    12-114, 332-440; backprojection-vs/fs.glsl) as fasterbackprojection_gb300's
+    fbp_splat_backproject samples it: exact hemispheres towards -y at a grid of
+    pixel centres over the volume's x / z extent, every operation in IEEE
+    float32 in the same order (so voxel indices are the GPU's), sums in FP64.
+    Bounce terms are not supported here (discard_first_last_bounces = 1).
+    cube: [L][T] (time innermost).  Returns vol[Vz][Vy][Vx] float64."""
+    f = np.float32
+    cube = np.asarray(cube, dtype=np.float32)
+    L, T = cube.shape
+    nb = min(T, max_bins) if max_bins else T
+    Vx, Vy, Vz = (int(v) for v in info.voxel_res)
+    vs = [f(v) for v in info.voxel_size]
+    hm = [f(v) for v in info.hidden_min]
+    gw, gh = grid
+    px = f(vs[0] * f(Vx)) / f(gw)
+    pz = f(vs[2] * f(Vy)) / f(gh)
+    x0 = f(hm[0] + f(f(0.5) * px))
+    z0 = f(hm[2] + f(f(0.5) * pz))
+    xs = (x0 + np.arange(gw, dtype=np.float32) * px).astype(np.float32)
+    zs = (z0 + np.arange(gh, dtype=np.float32) * pz).astype(np.float32)
+    X, Z = np.meshgrid(xs, zs, indexing="xy")
+    vol = np.zeros((Vz, Vy, Vx), dtype=np.float64)
+    ls, ts = np.nonzero(cube[:, :nb] > f(1.1920929e-7))
+    lx = np.asarray(laser_xyz, dtype=np.float32)
+    for l, t in zip(ls, ts):
+        path = f(f(f(t) * f(info.time_step)) + f(info.time_offset))
+        r = f(f(0.5) * path)
+        if not r > 0:
+            continue
+        c = lx[l]
+        dx = (X - c[0]).astype(np.float32)
+        dz = (Z - c[2]).astype(np.float32)
+        h2 = ((f(r * r) - (dx * dx).astype(np.float32)).astype(np.float32) - (dz * dz).astype(np.float32))
+        h2 = h2.astype(np.float32)
+        ok = h2 >= 0
+        y = (c[1] - np.sqrt(np.where(ok, h2, f(0)))).astype(np.float32)
+        fx = ((X - hm[0]).astype(np.float32) / vs[0]).astype(np.float32)
+        fy = ((y - hm[1]).astype(np.float32) / vs[1]).astype(np.float32)
+        fz = ((Z - hm[2]).astype(np.float32) / vs[2]).astype(np.float32)
+        ok &= (fx >= 0) & (fy >= 0) & (fz >= 0)
+        vx, vz, vy = fx.astype(np.int64), fy.astype(np.int64), fz.astype(np.int64)
+        ok &= (vx < Vx) & (vy < Vy) & (vz < Vz)
+        np.add.at(vol, (vz[ok], vy[ok], vx[ok]), float(cube[l, t]))
+    return vol

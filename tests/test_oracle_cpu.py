@@ -319,3 +319,20 @@ def test_mlp_bf16_rounding_is_nearest_even():
     x = np.array([1.0, 1.00390625, 1.005859375, -2.5, 3.0e-3], np.float32)
     want = np.array([1.0, 1.0, 1.0078125, -2.5, 0.0030059814453125])
     np.testing.assert_array_equal(mlp_ref.bf16(x), want)
+
+
+def test_splat_oracle_known_answer():
+    """One scan point at the origin, one bin of path 1 m: a hemisphere of
+    radius 0.5 below the wall; the pixel straight below the scan point lands
+    at depth 0.5 m."""
+    from types import SimpleNamespace
+
+    info = SimpleNamespace(voxel_res=(5, 5, 10), voxel_size=(0.2, 0.1, 0.2), hidden_min=(-0.5, -1.0, -0.5),
+                           time_step=0.25, time_offset=0.0)
+    cube = np.zeros((1, 8), np.float32)
+    cube[0, 4] = 3.0  # bin 4: path 1.0 m, radius 0.5 m
+    vol = numpy_ref.splat_backproject(info, cube, np.zeros((1, 3), np.float32), grid=(5, 5))
+    # Pixel (2, 2) is the centre (x = z = 0): y = -0.5 -> depth index (−0.5 + 1.0) / 0.1 = 5.
+    assert vol[5, 2, 2] == pytest.approx(3.0)
+    assert vol.sum() == pytest.approx(3.0 * np.count_nonzero(vol > 0) * 1.0)  # each fragment adds 3
+    assert np.count_nonzero(vol) >= 5
