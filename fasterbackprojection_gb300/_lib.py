@@ -152,6 +152,11 @@ SIGNATURES = {
                                                  c_void_p, c_void_p]),
     "fbp_splat_backproject": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_uint32,
                                       c_uint32, c_uint32, c_void_p, c_void_p]),
+    "fbp_transient_images": (c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint64, c_uint64, c_uint32,
+                                     c_uint32, c_int, c_void_p, c_void_p]),
+    "fbp_write_png": (c_int, [c_char_p, c_void_p, c_uint32, c_uint32]),
+    "fbp_save_transient_images": (c_int, [c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_uint64, c_uint64,
+                                          c_uint32, c_uint32, c_int, c_char_p, c_void_p]),
     "fbp_plan_slabs": (c_int, [POINTER(ReconInfo), c_uint32, POINTER(c_uint32)]),
     "fbp_slab_bin_window": (c_int, [POINTER(ReconInfo), c_void_p, c_uint32, c_uint32, POINTER(c_uint32),
                                     POINTER(c_uint32)]),

@@ -191,6 +191,39 @@ class Context:
                                                self._stream(stream)))
         return out
 
+    def transient_images(self, data, width: int, height: int, num_planes: int, pixel_stride: int,
+                         plane_stride: int, size=None, normalize: bool = False, out=None, stream=None):
+        """RGBA8 images [planes][out_h][out_w][4] (TransientImage::save per
+        plane); pixel idx of plane p is data[p*plane_stride + idx*pixel_stride];
+        size = (out_w, out_h), default the plane's own size."""
+        import torch
+
+        ow, oh = size if size is not None else (width, height)
+        if out is None:
+            out = torch.empty((num_planes, oh, ow, 4), dtype=torch.uint8, device=data.device)
+        check(self._lib.fbp_transient_images(self._h, _ptr(data), width, height, num_planes, pixel_stride,
+                                             plane_stride, ow, oh, int(normalize), _ptr(out), self._stream(stream)))
+        return out
+
+    def depth_plane_images(self, activation, width: int, height: int, size=None, normalize: bool = False,
+                           out=None, stream=None):
+        """The images of every depth plane of an [width*height][D] activation."""
+        D = int(activation.shape[-1])
+        return self.transient_images(activation, width, height, D, D, 1, size, normalize, out, stream)
+
+    def save_transient_images(self, data, width: int, height: int, num_planes: int, pixel_stride: int,
+                              plane_stride: int, prefix: str, size=None, normalize: bool = False, stream=None):
+        """Writes "<prefix>transient_<p>.png" for every plane."""
+        ow, oh = size if size is not None else (width, height)
+        check(self._lib.fbp_save_transient_images(self._h, _ptr(data), width, height, num_planes, pixel_stride,
+                                                  plane_stride, ow, oh, int(normalize), prefix.encode(),
+                                                  self._stream(stream)))
+
+    def save_depth_planes(self, activation, width: int, height: int, prefix: str, size=None, normalize: bool = False,
+                          stream=None):
+        D = int(activation.shape[-1])
+        self.save_transient_images(activation, width, height, D, D, 1, prefix, size, normalize, stream)
+
     def debug_confocal_bins(self, info: ReconInfo, laser_xyz, voxel_idx, stream=None):
         import torch
 
@@ -450,3 +483,19 @@ def linear_space(lo: float, hi: float, n: int) -> np.ndarray:
     out = np.empty(n, dtype=np.float64)
     check(load().fbp_linear_space(lo, hi, n, out.ctypes.data_as(ctypes.POINTER(c_double))))
     return out
+
+
+def write_png(path: str, rgba: np.ndarray) -> None:
+    """PNG file of an RGBA8 host image [h][w][4] (rows top first)."""
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    if a.ndim != 3 or a.shape[2] != 4:
+        raise ValueError("write_png: expected an [h][w][4] uint8 image")
+    check(load().fbp_write_png(str(path).encode(), a.ctypes.data_as(c_void_p), a.shape[1], a.shape[0]))
+
+
+def depth_image_size(side: int, exhaustive: bool = False) -> tuple[int, int]:
+    """Output size of the depth-plane images: side * (256 // side) below 256
+    for confocal captures (Laser.cu:420-422), 4 * side for exhaustive ones
+    (Laser.cu:473)."""
+    s = side * 4 if exhaustive else side * (256 // side if side < 256 else 1)
+    return (s, s)

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <fstream>
@@ -162,6 +163,20 @@ bool NLosData::saveBinaryFile(const std::string& filename) const {
     return static_cast<bool>(f);
 }
 
+void NLosData::saveImages(const std::string& outPath) {
+    if (_dims.size() > 3) throw std::runtime_error("NLosData: Invalid dimensions for saving images.");
+    if (_dims.size() < 3 || _dims[0] == 0) throw std::runtime_error("NLosData: no [rows][cols][T] data to save");
+    make_dirs(outPath);
+    const size_t slice = _data.size() / _dims[0];
+    if (slice != _dims[1] * _dims[2]) throw std::runtime_error("NLosData: dims do not match the data size");
+    float* d = device_upload(_data.data(), _data.size());
+    const fbp_status st = fbp_save_transient_images(fbp_default_context(), d, (uint32_t)_dims[1], (uint32_t)_dims[2],
+                                                    (uint32_t)_dims[0], 1, slice, (uint32_t)_dims[1],
+                                                    (uint32_t)_dims[2], 1, outPath.c_str(), nullptr);
+    cudaFree(d);
+    check(st, "NLosData::saveImages");
+}
+
 void NLosData::toGpu(ReconstructionInfo& in, ReconstructionBuffers& buf, const TransientParameters& tp) {
     std::memset(&in, 0, sizeof(in));
     buf._intensity = device_upload(_data.data(), _data.size());
@@ -310,17 +325,32 @@ void Laser::reconstructShape(const TransientParameters& tp) {
     const double focus = std::fabs((in.hidden_min[1] + in.hidden_max[1]) * 0.5f);
     std::vector<double> depths = linearSpace(focus - 0.1f, focus + 0.1f, (int)tp._numReconstructionDepths);
     double* ddep = device_upload(depths.data(), depths.size());
-    const size_t npix = (size_t)in.num_laser_targets * depths.size();
+    // The activation has num_sensor_targets rows (Laser.cu:389, 441); rows
+    // past the laser targets stay zero.
+    const uint32_t D = (uint32_t)depths.size();
+    const size_t rows = std::max(in.num_laser_targets, in.num_sensor_targets);
+    const size_t npix = rows * D;
     float* act = nullptr;
     check_cuda(cudaMalloc(&act, npix * sizeof(float)), "cudaMalloc");
-    fbp_status st = fbp_backproject_depths(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
-                                           reinterpret_cast<float*>(buf._laserTargets),
-                                           reinterpret_cast<float*>(buf._sensorTargets), ddep,
-                                           (uint32_t)depths.size(), act, nullptr);
+    fbp_status st = FBP_OK;
+    if (rows > in.num_laser_targets)
+        check_cuda(cudaMemset(act, 0, npix * sizeof(float)), "cudaMemset");
+    st = fbp_backproject_depths(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
+                                reinterpret_cast<float*>(buf._laserTargets),
+                                reinterpret_cast<float*>(buf._sensorTargets), ddep, D, act, nullptr);
     if (st == FBP_OK) st = fbp_normalize_minmax(ctx, act, npix, nullptr);
     _lastVolume.resize(npix);
     if (st == FBP_OK)
         check_cuda(cudaMemcpy(_lastVolume.data(), act, npix * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
+    // Laser.cu:410-424, 462-476: one image per depth of side sqrt(num_sensor_targets),
+    // enlarged to 256 (confocal, when smaller) or 4x (exhaustive).
+    const uint32_t side = (uint16_t)std::sqrt((float)in.num_sensor_targets);
+    const bool confocal = in.capture_system == FBP_CONFOCAL;
+    const uint32_t out = confocal ? side * (side < 256u ? 256u / side : 1u) : side * 4u;
+    if (st == FBP_OK && side > 0) {
+        make_dirs(tp._outputFolder);
+        st = fbp_save_transient_images(ctx, act, side, side, D, D, 1, out, out, 0, tp._outputFolder.c_str(), nullptr);
+    }
     cudaFree(act);
     cudaFree(ddep);
     check(st, "depth reconstruction");

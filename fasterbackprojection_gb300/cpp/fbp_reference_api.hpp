@@ -105,6 +105,11 @@ public:
 
     bool loadBinaryFile(const std::string& filename);
     bool saveBinaryFile(const std::string& filename) const;
+    // NLosData.cpp:161-180: "<outPath>transient_<row>.png" per scan row, the
+    // [cols][T] slice normalised by its maximum; the directory is created
+    // when missing.  Unlike the reference, _data itself is left unchanged
+    // (its normalizeImage divides the host slice in place).
+    void saveImages(const std::string& outPath);
 };
 
 // PostprocessingFilters.h:5-39.  compute() replaces `input` with a new device
@@ -141,7 +146,8 @@ public:
 
     // Laser.cu:40-67: filter_H, upload, AABB or depth-plane reconstruction,
     // post-filter, normalisation, "<outputFolder>aabb.cube" (AABB mode) or
-    // "<outputFolder>depths.raw" (depth mode: float32 [L][D]).
+    // "<outputFolder>depths.raw" (depth mode: float32 [L][D]) plus the depth
+    // planes as "<outputFolder>transient_<d>.png" (Laser.cu:409-424, 461-476).
     void reconstructShape(const TransientParameters& transientParams);
     // Laser.cu:526-611 with the unbiased estimator (see fbp.h); `volume` is a
     // device buffer of Vx*Vy*Vz floats.

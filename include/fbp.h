@@ -124,6 +124,35 @@ fbp_status fbp_backproject_depths(fbp_context* ctx, const fbp_recon_info* info, 
                                   int layout, const float* laser_xyz, const float* sensor_xyz,
                                   const double* depths, uint32_t num_depths, float* activation, void* stream);
 
+/* Transient images: the output step of the depth-plane reconstruction
+ * (Laser::reconstructDepthConfocal / Exhaustive, Laser.cu:409-424, 461-476) and
+ * of NLosData::saveImages (NLosData.cpp:161-180), for num_planes planes at once.
+ * Pixel idx (row-major, idx < width*height) of plane p is
+ * data[p*plane_stride + idx*pixel_stride] (device): pixel_stride D, plane_stride 1
+ * for the depth planes of an [L][D] activation; 1 and width*height for
+ * contiguous slices.  Each plane becomes TransientImage::save's image
+ * (TransientImage.cpp:46-64): grey RGBA8 clamp(uint(v*255), 0, 255), rows flipped
+ * (Image.h:160-178), bilinearly resized to out_width x out_height when that
+ * differs (Image.h:45-66, 92-138), in the reference's FP32 expression order.
+ * rgba: device [num_planes][out_height][out_width][4], PNG row order.  normalize
+ * != 0 divides each plane by max(0, its maximum) first (the reference divides
+ * the first width*height floats of its pointer: the same plane for contiguous
+ * slices).  Sizes 1..65535; a resized image is at least 2 x 2. */
+fbp_status fbp_transient_images(fbp_context* ctx, const float* data, uint32_t width, uint32_t height,
+                                uint32_t num_planes, uint64_t pixel_stride, uint64_t plane_stride, uint32_t out_width,
+                                uint32_t out_height, int normalize, uint8_t* rgba, void* stream);
+
+/* PNG file (8-bit RGBA) of a host image, rows top first; replaces the SOIL2
+ * SOIL_save_image call of TransientImage::save (TransientImage.cpp:63).  Host function. */
+fbp_status fbp_write_png(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height);
+
+/* fbp_transient_images, then "<prefix>transient_<p>.png" for every plane
+ * (Laser.cu:416-424, NLosData.cpp:172-178).  Synchronises the stream. */
+fbp_status fbp_save_transient_images(fbp_context* ctx, const float* data, uint32_t width, uint32_t height,
+                                     uint32_t num_planes, uint64_t pixel_stride, uint64_t plane_stride,
+                                     uint32_t out_width, uint32_t out_height, int normalize, const char* prefix,
+                                     void* stream);
+
 /* Laser::linearSpace (Laser.cu:69-78) and the depth set reconstructShapeDepths
  * uses (Laser.cu:365-377): out[i] = min + i*(max-min)/n.  Host function. */
 fbp_status fbp_linear_space(double min_value, double max_value, int n, double* out);

@@ -182,3 +182,57 @@ def splat_backproject(info, cube, laser_xyz, max_bins=700, grid=(256, 256)) -> n
         ok &= (vx < Vx) & (vy < Vy) & (vz < Vz)
         np.add.at(vol, (vz[ok], vy[ok], vx[ok]), float(cube[l, t]))
     return vol
+
+
+def transient_image(slice_, width, height, size, stride=1, offset=0, normalize=False) -> np.ndarray:
+    """TransientImage::save (FasterBackprojection/TransientImage.cpp:46-64) of
+    one plane: grey RGBA8 clamp(uint(v * 255), 0, 255) of
+    slice[offset + idx * stride], rows flipped (Image.h:160-178), then the
+    bilinear Image::resize (Image.h:45-66, 92-138) to size = (w, h) when it
+    differs, every operation in IEEE float32 in the reference's order.
+    normalize divides the plane by max(0, its maximum) (the reference divides
+    the first width * height floats, the same plane for stride 1, offset 0).
+    Negative or NaN products become 0.  Returns uint8 [h][w][4], rows top first."""
+    f = np.float32
+    s = np.asarray(slice_, dtype=np.float32)
+    n = width * height
+    v = s[offset + np.arange(n, dtype=np.int64) * stride].astype(np.float32)
+    if normalize:
+        m = f(max(0.0, float(np.nanmax(v)) if np.any(~np.isnan(v)) else 0.0))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            v = (v / m).astype(np.float32)
+    with np.errstate(invalid="ignore", over="ignore"):
+        p = (v * f(255.0)).astype(np.float32)
+        p = np.where(np.isnan(p) | (p < 0), f(0), np.minimum(np.trunc(p), f(255)))
+    grey = p.reshape(height, width)[::-1].astype(np.float32)  # flipped, values 0..255
+    ow, oh = size
+    if (ow, oh) == (width, height):
+        out = np.empty((height, width, 4), np.uint8)
+        out[..., :3] = grey.astype(np.uint8)[..., None]
+        out[..., 3] = 255
+        return out
+    xr = f(f(width - 1) / f(ow - 1))
+    yr = f(f(height - 1) / f(oh - 1))
+    xs = (np.arange(ow, dtype=np.float32) * xr).astype(np.float32)
+    ys = (np.arange(oh, dtype=np.float32) * yr).astype(np.float32)
+    x0 = np.minimum(xs.astype(np.int64), width - 1)
+    y0 = np.minimum(ys.astype(np.int64), height - 1)
+    x1 = np.minimum(x0 + 1, width - 1)
+    y1 = np.minimum(y0 + 1, height - 1)
+    dx = (xs - x0.astype(np.float32)).astype(np.float32)[None, :]
+    dy = (ys - y0.astype(np.float32)).astype(np.float32)[:, None]
+    ex = (f(1) - dx).astype(np.float32)
+    ey = (f(1) - dy).astype(np.float32)
+
+    def lerp(p00, p01, p10, p11):
+        a = ((ex * ey).astype(np.float32) * p00).astype(np.float32)
+        a = (a + ((dx * ey).astype(np.float32) * p01).astype(np.float32)).astype(np.float32)
+        a = (a + ((ex * dy).astype(np.float32) * p10).astype(np.float32)).astype(np.float32)
+        return (a + ((dx * dy).astype(np.float32) * p11).astype(np.float32)).astype(np.float32)
+
+    g = lerp(grey[y0][:, x0], grey[y0][:, x1], grey[y1][:, x0], grey[y1][:, x1])
+    a = lerp(f(255), f(255), f(255), f(255))
+    out = np.empty((oh, ow, 4), np.uint8)
+    out[..., :3] = np.minimum(np.trunc(g), 255).astype(np.uint8)[..., None]
+    out[..., 3] = np.broadcast_to(np.minimum(np.trunc(a), 255).astype(np.uint8), (oh, ow))
+    return out

@@ -79,6 +79,24 @@ struct uvec2 {
     FBPH_QUAL uvec2(uint a, uint b) : x(a), y(b) {}
 };
 
+struct vec4 {
+    union { float x, r; };
+    union { float y, g; };
+    union { float z, b; };
+    union { float w, a; };
+    vec4() = default;
+    FBPH_QUAL vec4(float p, float q, float s, float t) : x(p), y(q), z(s), w(t) {}
+};
+
+struct uvec4 {
+    uint x, y, z, w;
+    uvec4() = default;
+    FBPH_QUAL uvec4(uint a, uint b, uint c, uint d) : x(a), y(b), z(c), w(d) {}
+};
+
+FBPH_QUAL bool operator==(const uvec2& a, const uvec2& b) { return a.x == b.x && a.y == b.y; }
+FBPH_QUAL bool operator!=(const uvec2& a, const uvec2& b) { return !(a == b); }
+
 FBPH_QUAL vec3::vec3(const uvec3& u) : x(static_cast<float>(u.x)), y(static_cast<float>(u.y)), z(static_cast<float>(u.z)) {}
 
 // Component-wise arithmetic.
@@ -106,6 +124,7 @@ FBPH_QUAL vec3 normalize(const vec3& v) { return v * (1.0f / length(v)); }
 
 template <typename T> FBPH_QUAL T max(T a, T b) { return a < b ? b : a; }
 template <typename T> FBPH_QUAL T min(T a, T b) { return b < a ? b : a; }
+template <typename T> FBPH_QUAL T clamp(T v, T lo, T hi) { return min(max(v, lo), hi); }
 FBPH_QUAL float abs(float a) { return a < 0.f ? -a : a; }
 FBPH_QUAL float sqrt(float a) { return sqrtf(a); }
 FBPH_QUAL uint sqrt(uint a) { return static_cast<uint>(sqrtf(static_cast<float>(a))); }

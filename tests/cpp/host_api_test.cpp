@@ -36,6 +36,12 @@ int main(int argc, char** argv) {
             std::printf("ok %zu\n", laser.lastVolume().size());
             return 0;
         }
+        if (mode == "images") {
+            NLosData d(argv[2]);
+            d.saveImages(std::string(argv[3]) + "/");
+            std::printf("ok %zu\n", d._dims[0]);
+            return 0;
+        }
         if (mode == "lct") {
             NLosData d(argv[2]);
             TransientParameters p;

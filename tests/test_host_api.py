@@ -116,6 +116,32 @@ def test_laser_depth_mode_writes_activations(driver, ctx, tmp_path):
     assert out.returncode == 0, out.stderr
     act = np.fromfile(tmp_path / "depths.raw", dtype=np.float32).reshape(64, 20)
     assert act.min() >= 0.0 and act.max() == pytest.approx(1.0)
+    # Laser.cu:409-424: one PNG per depth, an 8 x 8 scan enlarged to 256 x 256.
+    from oracle import numpy_ref
+    from tests.test_images_cpu import _decode_png
+
+    for d in (0, 7, 19):
+        img = _decode_png((tmp_path / f"transient_{d}.png").read_bytes())
+        np.testing.assert_array_equal(img, numpy_ref.transient_image(act.ravel(), 8, 8, (256, 256), stride=20,
+                                                                     offset=d))
+
+
+@pytest.mark.gpu
+def test_nlos_save_images_writes_normalised_slices(driver, ctx, tmp_path):
+    """NLosData::saveImages (NLosData.cpp:161-180): one normalised [cols][T] image per scan row."""
+    from fasterbackprojection_gb300 import nlos_io
+    from oracle import numpy_ref
+    from tests.test_images_cpu import _decode_png
+
+    cap, c = _capture(n=6, T=64)
+    nlos_io.write_nlos(tmp_path / "cap.nlos", c)
+    out = subprocess.run([str(driver), "images", str(tmp_path / "cap.nlos"), str(tmp_path / "img")],
+                         capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    data = cap.cube.reshape(6, 6 * 64)
+    for r in range(6):
+        img = _decode_png((tmp_path / "img" / f"transient_{r}.png").read_bytes())
+        np.testing.assert_array_equal(img, numpy_ref.transient_image(data[r], 6, 64, (6, 64), normalize=True))
 
 
 @pytest.mark.gpu
