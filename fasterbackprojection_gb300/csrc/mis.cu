@@ -64,7 +64,7 @@ __global__ void scan_totals_kernel(const S* __restrict__ cube, uint32_t L, uint3
     }
 }
 
-// backprojectConfocalVoxelMIS arithmetic, one thread per voxel, samples in order.
+// backprojectConfocalVoxelMIS arithmetic, one thread per voxel.
 struct MisRefParams {
     const void* rows;
     uint32_t pitch;
@@ -88,71 +88,107 @@ __device__ __forceinline__ float noise_next(const float* noise, uint32_t n, uint
     return noise[state % n];
 }
 
+// Sample s of voxel v starts its generator at state v + s
+// (transient_reconstruction.cuh:209), so everything a sample draws (proposal,
+// scan point, balance weight) depends on v + s alone: a block of kMisVoxels
+// consecutive voxels needs kMisVoxels + C - 1 states per chunk of C samples,
+// not kMisVoxels * C.  The block draws them once into shared memory; then
+// thread t takes its samples in the rotated order j = (k - t) mod C, so at
+// step k a warp's lanes share one or two states: one scan point, and
+// neighbouring voxels, so the cube reads coalesce.  Each sample's term is the
+// one-sample kernel's; the per-voxel sum runs in the rotated order.
+constexpr uint32_t kMisVoxels = 256, kMisChunk = 256;
+
+__device__ __forceinline__ void mis_draw(const MisRefParams& p, uint32_t state, float invL, uint32_t& l, float& a) {
+    float pdf, gpdf;
+    if (noise_next(p.noise, p.noise_size, state) < 0.5f) {
+        const float r1 = noise_next(p.noise, p.noise_size, state);
+        const float r2 = noise_next(p.noise, p.noise_size, state);
+        const uint32_t k = min((uint32_t)(r1 * (float)p.L), p.L - 1);
+        l = r2 < p.prob[k] ? k : p.alias[k];
+        pdf = l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l];
+        gpdf = pdf + 1.0f * invL;
+    } else {
+        l = min((uint32_t)(noise_next(p.noise, p.noise_size, state) * (float)p.L), p.L - 1);
+        pdf = 1.0f * invL;
+        gpdf = pdf + (l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l]);
+    }
+    a = pdf * ref_safe_rcp(gpdf);  // the balance weight
+}
+
 template <typename S>
-__global__ void mis_reference_kernel(MisRefParams p) {
-    const uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kMisVoxels) mis_reference_kernel(MisRefParams p) {
+    __shared__ float4 s_scan[kMisVoxels + kMisChunk - 1];
+    __shared__ float2 s_draw[kMisVoxels + kMisChunk - 1];  // (weight, scan point index bits)
+    const uint32_t t = threadIdx.x;
     const uint64_t slice = (uint64_t)p.Vx * p.Vy;
-    if (v >= slice * p.Vz) return;
-    const uint32_t vz = (uint32_t)(v / slice), vs = (uint32_t)(v % slice);
-    const uint32_t vy = vs / p.Vx, vx = vs % p.Vx;
-    const float px = p.xs[vx], py = p.ys[vz], pz = p.zs[vy];
+    const uint64_t v0 = (uint64_t)blockIdx.x * kMisVoxels, v = v0 + t;
+    const bool live = v < slice * p.Vz;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    if (live) {
+        const uint32_t vz = (uint32_t)(v / slice), vs = (uint32_t)(v % slice);
+        px = p.xs[vs % p.Vx];
+        py = p.ys[vz];
+        pz = p.zs[vs / p.Vx];
+    }
     const float rcp_dt = rcp_approx(p.dt);
     const float invL = ref_safe_rcp((float)p.L);
     const S* rows = static_cast<const S*>(p.rows);
     float ksum = 0.f, kcomp = 0.f, acc = 0.f;
-    // U samples at a time: their dependent load chains (noise, alias, scan
-    // point, cube) are independent of each other and run concurrently; the
-    // terms are still added in sample order.
-    constexpr int U = 4;
-    for (uint32_t s0 = 0; s0 < p.samples; s0 += U) {
-        float a[U], w[U], I[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            a[u] = 0.f;
-            w[u] = 0.f;
-            I[u] = 0.f;
-            const uint32_t s = s0 + u;
-            if (s >= p.samples) continue;
-            uint32_t state = (uint32_t)(slice * vz + vs + s);  // transient_reconstruction.cuh:209
+    for (uint32_t s0 = 0; s0 < p.samples; s0 += kMisChunk) {
+        const uint32_t ce = min(kMisChunk, p.samples - s0), ntab = kMisVoxels + ce - 1;
+        __syncthreads();  // the previous chunk's table is no longer read
+        for (uint32_t i = t; i < ntab; i += kMisVoxels) {
             uint32_t l;
-            float pdf, gpdf;
-            if (noise_next(p.noise, p.noise_size, state) < 0.5f) {
-                const float r1 = noise_next(p.noise, p.noise_size, state);
-                const float r2 = noise_next(p.noise, p.noise_size, state);
-                const uint32_t k = min((uint32_t)(r1 * (float)p.L), p.L - 1);
-                l = r2 < p.prob[k] ? k : p.alias[k];
-                pdf = l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l];
-                gpdf = pdf + 1.0f * invL;
-            } else {
-                l = min((uint32_t)(noise_next(p.noise, p.noise_size, state) * (float)p.L), p.L - 1);
-                pdf = 1.0f * invL;
-                gpdf = pdf + (l > 0 ? p.spatial[l] - p.spatial[l - 1] : p.spatial[l]);
-            }
-            const float4 g = p.scan[l];
-            float dist = fma_rn(sqrt_approx(ref_dot3(sub_rn(px, g.x), sub_rn(py, g.y), sub_rn(pz, g.z))), 2.f, -p.t0);
-            if (p.bounce) dist = add_rn(dist, g.w);
-            a[u] = pdf * ref_safe_rcp(gpdf);  // the balance weight
-            const int b = __float2int_rz(ref_bin_ratio(dist, rcp_dt));
-            if (b >= 0 && b < (int)p.T) {
-                I[u] = to_f32(rows[(uint64_t)l * p.pitch + b]);
-                w[u] = ref_safe_rcp(mul_rn(dist, dist));
-            }
+            float a;
+            mis_draw(p, (uint32_t)(v0 + s0 + i), invL, l, a);
+            s_scan[i] = p.scan[l];
+            s_draw[i] = make_float2(a, __uint_as_float(l));
         }
+        __syncthreads();
+        if (!live) continue;
+        const uint32_t r = t % ce;
+        // U steps at a time: their cube reads are in flight together; the
+        // terms are added in step order.
+        constexpr int U = 4;
+        for (uint32_t k0 = 0; k0 < ce; k0 += U) {
+            float A[U], W[U], I[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint32_t s = s0 + u;
-            if (s >= p.samples) break;
-            if (I[u] > FBP_EPS) acc = fmaf(a[u] * I[u], w[u], acc);
-            if ((s & 63) == 63 || s + 1 == p.samples) {
-                const float y = sub_rn(acc, kcomp);
-                const float t = add_rn(ksum, y);
-                kcomp = sub_rn(sub_rn(t, ksum), y);
-                ksum = t;
-                acc = 0.f;
+            for (int u = 0; u < U; ++u) {
+                A[u] = 0.f;
+                W[u] = 0.f;
+                I[u] = 0.f;
+                const uint32_t k = k0 + u;
+                if (k >= ce) continue;
+                const uint32_t e = t + (k >= r ? k - r : k + ce - r);
+                const float4 g = s_scan[e];
+                const float2 d = s_draw[e];
+                float dist = fma_rn(sqrt_approx(ref_dot3(sub_rn(px, g.x), sub_rn(py, g.y), sub_rn(pz, g.z))), 2.f,
+                                    -p.t0);
+                if (p.bounce) dist = add_rn(dist, g.w);
+                A[u] = d.x;
+                const int b = __float2int_rz(ref_bin_ratio(dist, rcp_dt));
+                if (b >= 0 && b < (int)p.T) {
+                    I[u] = to_f32(rows[(uint64_t)__float_as_uint(d.y) * p.pitch + b]);
+                    W[u] = ref_safe_rcp(mul_rn(dist, dist));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t n = s0 + k0 + u;  // samples taken so far, this one included: n + 1
+                if (k0 + u >= ce) break;
+                if (I[u] > FBP_EPS) acc = fmaf(A[u] * I[u], W[u], acc);
+                if ((n & 63) == 63 || n + 1 == p.samples) {
+                    const float y = sub_rn(acc, kcomp);
+                    const float tt = add_rn(ksum, y);
+                    kcomp = sub_rn(sub_rn(tt, ksum), y);
+                    ksum = tt;
+                    acc = 0.f;
+                }
             }
         }
     }
-    p.volume[v] = ksum;
+    if (live) p.volume[v] = ksum;
 }
 
 template <typename S>
@@ -451,7 +487,7 @@ static fbp_status mis_run(fbp_context* ctx, const fbp_recon_info& in, const void
         p.dt = in.time_step;
         p.bounce = in.discard_first_last_bounces == 0;
         p.volume = volume;
-        mis_reference_kernel<S><<<cdiv(V, 256), 256, 0, s>>>(p);
+        mis_reference_kernel<S><<<cdiv(V, kMisVoxels), kMisVoxels, 0, s>>>(p);
         FBP_CHECK_LAUNCH(ctx, "mis_reference_kernel");
         return FBP_OK;
     }

@@ -236,3 +236,67 @@ def transient_image(slice_, width, height, size, stride=1, offset=0, normalize=F
     out[..., :3] = np.minimum(np.trunc(g), 255).astype(np.uint8)[..., None]
     out[..., 3] = np.broadcast_to(np.minimum(np.trunc(a), 255).astype(np.uint8), (oh, ow))
     return out
+
+
+def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=None) -> np.ndarray:
+    """Sum over samples s < `samples` of backprojectConfocalVoxelMIS
+    (FasterBackprojection/transient_reconstruction.cuh:194-260, without the
+    race of its `+=`): voxel v, sample s starts its generator at state v + s
+    (uint32, :209), draws from the noise buffer with
+    getUniformRandom / getMISIndexAlias (transient_utils.cuh:18-53) and picks
+    the alias or the uniform proposal with the balance weight, all in float32
+    as the kernel does; the term weight * I / dist^2 is summed in FP64.
+    bins: [V][L] int32 time bins (the GPU's, from fbp_debug_confocal_bins),
+    else FP64 bins.  cube: [L][T].  Returns vol[Vz][Vy][Vx] float64."""
+    if int(info.discard_first_last_bounces) == 0:
+        raise NotImplementedError("mis_reference: bounce terms are not restated here")
+    f = np.float32
+    cube = np.asarray(cube, dtype=np.float32)
+    L, T = cube.shape
+    Vx, Vy, Vz = (int(v) for v in info.voxel_res)
+    V = Vx * Vy * Vz
+    noise = np.asarray(noise, dtype=np.float32)
+    n = np.uint64(noise.shape[0])
+    cdf = np.asarray(cdf, dtype=np.float32)
+    alias = np.asarray(alias, dtype=np.int64)
+    prob = np.asarray(prob, dtype=np.float32)
+    spatial_pdf = np.concatenate([cdf[:1], (cdf[1:] - cdf[:-1]).astype(np.float32)]).astype(np.float32)
+    inv_l = f(1.0) / f(L) if f(L) > f(1e-5) else np.finfo(np.float32).max
+    v = np.arange(V, dtype=np.int64)
+    vz, rem = v // (Vx * Vy), v % (Vx * Vy)
+    vy, vx = rem // Vx, rem % Vx
+    hm = np.asarray(info.hidden_min, dtype=np.float64)
+    vs = np.asarray(info.voxel_size, dtype=np.float64)
+    p = np.stack([hm[0] + (vx + 0.5) * vs[0], hm[1] + (vz + 0.5) * vs[1], hm[2] + (vy + 0.5) * vs[2]], axis=1)
+    lx = np.asarray(laser_xyz, dtype=np.float64)
+    out = np.zeros(V, dtype=np.float64)
+
+    def draw(state):
+        state = (state * np.uint64(747796405) + np.uint64(2891336453)) & np.uint64(0xFFFFFFFF)
+        return state, noise[(state % n).astype(np.int64)]
+
+    for s in range(samples):
+        state = ((v + s) & 0xFFFFFFFF).astype(np.uint64)
+        state, r0 = draw(state)
+        use_alias = r0 < f(0.5)
+        state_a, r1 = draw(state)
+        state_a, r2 = draw(state_a)
+        k = np.minimum((r1 * f(L)).astype(np.float32).astype(np.int64), L - 1)
+        l_alias = np.where(r2 < prob[k], k, alias[k])
+        _, ru = draw(state)
+        l_unif = np.minimum((ru * f(L)).astype(np.float32).astype(np.int64), L - 1)
+        l = np.where(use_alias, l_alias, l_unif)
+        pdf = np.where(use_alias, spatial_pdf[l], inv_l).astype(np.float32)
+        gpdf = np.where(use_alias, (spatial_pdf[l] + inv_l).astype(np.float32),
+                        (inv_l + spatial_pdf[l]).astype(np.float32)).astype(np.float32)
+        w = pdf.astype(np.float64) / gpdf.astype(np.float64)
+        dist = 2.0 * np.linalg.norm(p - lx[l], axis=1) - float(info.time_offset)
+        if bins is None:
+            b = np.floor(dist / float(info.time_step)).astype(np.int64)
+        else:
+            b = np.asarray(bins, dtype=np.int64).reshape(V, L)[v, l]
+        ok = (b >= 0) & (b < T)
+        I = np.where(ok, cube[l, np.clip(b, 0, T - 1)], 0.0)
+        ok &= I > 1e-5
+        out += np.where(ok, w * I / (dist * dist), 0.0)
+    return out.reshape(Vz, Vy, Vx)

@@ -53,6 +53,30 @@ def test_reference_mis_many_samples_is_deterministic(ctx, cuda):
     assert torch.equal(a, b) and float(a.abs().max()) > 0
 
 
+@pytest.mark.parametrize("samples", [1, 7, 64, 300])
+def test_reference_mis_many_samples_match_oracle(ctx, cuda, samples):
+    """The sum over samples of the reference's one-sample terms (its own
+    kernel races on `+=` beyond one sample), against the FP64 restatement with
+    the GPU's time bins: chunks of 256 samples, a ragged last chunk, and fewer
+    samples than a warp."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE
+    from oracle import numpy_ref
+
+    cap, info = _case()
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    cdf, alias, prob = ctx.mis_reference_tables(info, cube)
+    V = 24 * 20 * 28
+    noise = torch.rand(V + 17, generator=torch.Generator().manual_seed(6)).to(cuda)
+    got = ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE, samples, noise=noise).cpu().numpy()
+    bins = ctx.debug_confocal_bins(info, lx, torch.arange(V, device=cuda)).cpu().numpy()
+    want = numpy_ref.mis_reference(info, cap.cube, cap.laser_xyz, cdf, alias, prob, noise.cpu().numpy(), samples,
+                                   bins=bins)
+    assert float(np.abs(want).max()) > 0
+    assert rel_l2(got, want) < 1e-6
+
+
 @pytest.mark.parametrize("proposal", ["uniform", "spatial", "clusters", "clusters_cv"])
 def test_unbiased_estimators_converge_to_full_backprojection(ctx, cuda, proposal):
     import torch
