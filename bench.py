@@ -320,6 +320,7 @@ def run_ours(args):
             extras["learned_mis"] = learned_mis_leg(ctx, dev, info, cube, lx)
         if not args.no_configs:
             extras["reference_kernels"] = reference_kernels_leg(ctx, dev, info, cube, lx, vol)
+            extras["scatter_forms"] = scatter_forms_leg(ctx, dev, info, cube, lx)
             pk = measured_peaks()[0]
             extras["filters"] = filters_leg(ctx, dev, vol, cube, info.time_step, pk)
             extras["lct"] = lct_leg(ctx, dev, pk)
@@ -536,6 +537,69 @@ def reference_kernels_leg(ctx, dev, info, cube, lx, vol):
     elx, esx = torch.from_numpy(ecap.laser_xyz).to(dev), torch.from_numpy(ecap.sensor_xyz).to(dev)
     both("exhaustive_16^2x16^2x1024_8_slices", lambda: ctx.backproject_exhaustive(einfo, ec, elx, esx),
          lambda: harness.exhaustive_voxel(einfo, ec, elx, esx))
+    ctx.check_device_status()
+    return out
+
+
+def scatter_forms_leg(ctx, dev, info, cube, lx):
+    """The scatter-form rows next to the headline workload: the voxel-scattering
+    gather (the reference's ACCUMULATE_VOXEL_SCATTERING build) over the full
+    256^3 volume and against the reference's own kernel of that build on the
+    first 8 depth slices; the rasterised ellipsoid splat (700 bins, 256 x 256
+    pixel grid, the reference's GL defaults); the depth-plane images of a
+    64^2-scan, 200-plane reconstruction enlarged to 256 x 256."""
+    import ctypes
+
+    import torch
+
+    from fasterbackprojection_gb300 import make_info, scenes
+    from fasterbackprojection_gb300.api import linear_space
+
+    out = {}
+    V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
+    pairs = V * info.num_laser_targets
+    vol = torch.empty(V, dtype=torch.float32, device=dev)
+    _, ms = timed_ms(lambda: ctx.backproject_confocal_scatter(info, cube, lx, out=vol), reps=2)
+    e = {"workload": "256^2 x 1024 FP32 -> 256^3, voxel extent sqrt(3) * 7.8 mm / 2 = 6.8 mm, bins of 4.8 mm",
+         "ms": ms, "value": pairs / (ms / 1e3), "unit": UNIT}
+    try:
+        from oracle import harness
+
+        if harness.scatter_available():
+            harness.load()
+            sub = type(info)()
+            ctypes.memmove(ctypes.byref(sub), ctypes.byref(info), ctypes.sizeof(info))
+            sub.voxel_res[2] = 8
+            cube_tm = cube.t().contiguous()
+            o, o_ms = timed_ms(lambda: ctx.backproject_confocal_scatter(sub, cube, lx), reps=2)
+            r, r_ms = timed_ms(lambda: harness.confocal_voxel_scatter(sub, cube_tm, lx), reps=2)
+            del cube_tm
+            e["reference_8_slices"] = {"ours_ms": o_ms, "reference_ms": r_ms, "speedup": r_ms / o_ms,
+                                       "rel_l2": float(torch.linalg.vector_norm((o - r).double()) /
+                                                       max(float(torch.linalg.vector_norm(r.double())), 1e-30))}
+        else:
+            e["reference_8_slices"] = {"unavailable": "reference scatter build not present"}
+    except Exception as ex:  # pragma: no cover
+        e["reference_8_slices"] = {"unavailable": f"harness: {ex}"}
+    out["voxel_scattering"] = e
+    svol = torch.empty(V, dtype=torch.float32, device=dev)
+    _, ms = timed_ms(lambda: ctx.splat_backproject(info, cube, lx, max_bins=700, grid=(256, 256), out=svol), reps=2)
+    nz = int((cube[:, :700] > 1.1920929e-7).sum())
+    out["splat"] = {"workload": "256^2 x 1024 FP32, bins < 700, 256 x 256 pixel grid -> 256^3", "ms": ms,
+                    "instances": nz, "instances_per_s": nz / (ms / 1e3),
+                    "gl_timing": "unavailable on this box (no graphics stack)"}
+    del svol
+    cap = scenes.confocal_points(64, 512, 32e-12, n_points=200, seed=1)
+    dinfo = make_info(num_laser_targets=4096, num_time_bins=512, time_step=cap.time_step, voxel_res=(1, 1, 1),
+                      hidden_min=(0, 0, 0), voxel_size=(1, 1, 1))
+    depths = torch.from_numpy(linear_space(0.7, 0.9, 200)).to(dev)
+    act = ctx.backproject_depths(dinfo, torch.from_numpy(cap.cube).to(dev), torch.from_numpy(cap.laser_xyz).to(dev),
+                                 depths)
+    ctx.normalize_(act)
+    imgs = torch.empty((200, 256, 256, 4), dtype=torch.uint8, device=dev)
+    _, ms = timed_ms(lambda: ctx.depth_plane_images(act, 64, 64, size=(256, 256), out=imgs), reps=5)
+    out["depth_plane_images"] = {"workload": "200 planes of 64^2 -> 256^2 RGBA8 (bilinear)", "ms": ms,
+                                 "bytes_written": imgs.numel(), "achieved_gbs": imgs.numel() / (ms / 1e3) / 1e9}
     ctx.check_device_status()
     return out
 
