@@ -29,80 +29,96 @@ struct FilterTaps {
 // circularly by R on both sides: S[i] = P[(i - R) mod n], i < n + 2R, so
 //     out[t] = sum_{j=0}^{2R} taps[j] * S[t + pad + 2R - j]
 // is the circular correlation the padded FFTs compute.
-// Every thread produces Q = 8 consecutive outputs.  It keeps the 2Q values
-// S[b0 - j - Q .. b0 - j + Q) of the current block of Q taps in registers
-// (indices fixed at compile time), loads the next Q once per block, and adds
-// tap j + s to output q from register Q - s + q: one shared-memory load per
-// tap for Q FMAs.  Each output still sums its taps in order j = 0..2R.  The
-// series is stored Q-way interleaved (element e at (e % Q) * QS + e / Q), so
-// the loads of consecutive threads, Q elements apart, hit consecutive words.
+// Every thread produces Q = 8 consecutive outputs.  It keeps two windows of
+// Q values of S in registers (ping-pong: the window that served the high half
+// of one block of Q taps serves the low half of the next) and adds tap J + s
+// to output q from window slot Q + q - s: one 32-byte row of S per Q taps for
+// Q * Q FMAs.  Each output still sums its taps in order j = 0..2R; the taps
+// are zero-padded to a multiple of 2Q (zero terms), and S is preceded by F
+// zero slots (3Q <= F < 4Q, making S-index + F of every window start a
+// multiple of Q) so the last, unused window loads stay in bounds.
+// Rows of S are 8 floats; the two 16-byte halves of row k trade places when
+// bit 2 of k is set, so the 16-byte loads of 8 consecutive threads (8
+// consecutive rows) fall in 8 different bank groups.
 constexpr int kFilterQ = 8;
 
-__device__ __forceinline__ float sld(const float* sh, int qs, int e) {
-    return sh[(e & (kFilterQ - 1)) * qs + (e >> 3)];
+__device__ __forceinline__ int srow_addr(int k, int half) { return 8 * k + 4 * (half ^ ((k >> 2) & 1)); }
+
+__device__ __forceinline__ void srow_load(const float* sh, int k, float (&v)[kFilterQ]) {
+    const float4 a = *reinterpret_cast<const float4*>(sh + srow_addr(k, 0));
+    const float4 b = *reinterpret_cast<const float4*>(sh + srow_addr(k, 1));
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+// acc[q] += taps[J + st] * window slot (Q + q - st), slots [0, Q) in lo, [Q, 2Q) in hi.
+__device__ __forceinline__ void filter_block(const float* s_taps, int J, const float (&lo)[kFilterQ],
+                                             const float (&hi)[kFilterQ], float (&acc)[kFilterQ]) {
+    constexpr int Q = kFilterQ;
+    const float4 ta = *reinterpret_cast<const float4*>(s_taps + J);
+    const float4 tb = *reinterpret_cast<const float4*>(s_taps + J + 4);
+    const float t[Q] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+#pragma unroll
+    for (int st = 0; st < Q; ++st)
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int m = Q + q - st;
+            acc[q] = fmaf(m < Q ? lo[m] : hi[m - Q], t[st], acc[q]);
+        }
 }
 
 __global__ void __launch_bounds__(128) filter_h_kernel(float* __restrict__ data, uint64_t nseries, uint32_t T, int n,
-                                                       int R, int pad, int edge,
+                                                       int R, int pad, int edge, int F, int ntp, int rows,
                                                        const __grid_constant__ FilterTaps taps) {
     constexpr int Q = kFilterQ;
-    extern __shared__ float sh[];  // taps, then Q interleaved parts of QS floats
-    const int E = n + 2 * R, QS = (E + 2 * Q - 1) / Q + 1;
+    extern __shared__ __align__(16) float sh[];  // taps (ntp, zero-padded), then `rows` rows of S
+    const int E = n + 2 * R;
     const int ntaps = 2 * R + 1;
     float* s_taps = sh;
-    float* sser = sh + ((ntaps + 3) & ~3);
-    for (int j = threadIdx.x; j < ntaps; j += blockDim.x) s_taps[j] = taps.w[j];
+    float* sser = sh + ntp;
+    for (int j = threadIdx.x; j < ntp; j += blockDim.x) s_taps[j] = j < ntaps ? taps.w[j] : 0.f;
     for (uint64_t s = blockIdx.x; s < nseries; s += gridDim.x) {
         float* h = data + s * T;
         const float first = h[0], last = h[T - 1];
         // Fill in batches of 8 per thread, the batch's loads in flight together
-        // (the slots past E, read only for discarded outputs, are zero).
-        for (int i0 = threadIdx.x; i0 < Q * QS; i0 += 8 * blockDim.x) {
+        // (slots before S[0] and past S[E - 1] are zero).
+        for (int i0 = threadIdx.x; i0 < 8 * rows; i0 += 8 * blockDim.x) {
             float v[8];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-                const int i = i0 + b * blockDim.x;
+                const int ip = i0 + b * blockDim.x;  // slot index, S index ip - F
+                const int i = ip - F;
                 int k = i - R;  // circular index in [0, n); i - R >= -R > -n
                 if (k < 0) k += n;
                 while (k >= n) k -= n;
                 const int u = k - pad;  // signal index
-                if (i >= E) v[b] = 0.f;
+                if (i < 0 || i >= E) v[b] = 0.f;
                 else if (u >= 0 && u < (int)T) v[b] = h[u];
                 else if (edge) v[b] = u < 0 ? first : last;
                 else v[b] = 0.f;
             }
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
-                const int i = i0 + b * blockDim.x;
-                if (i < Q * QS) sser[(i & (Q - 1)) * QS + (i >> 3)] = v[b];
+                const int ip = i0 + b * blockDim.x;
+                if (ip < 8 * rows) sser[srow_addr(ip >> 3, (ip >> 2) & 1) + (ip & 3)] = v[b];
             }
         }
         __syncthreads();
         for (int t0 = threadIdx.x * Q; t0 < (int)T; t0 += blockDim.x * Q) {
-            // out[t0 + q] = sum_j taps[j] * S[b0 - j + q], b0 = t0 + pad + 2R (>= Q - 1 + ...)
-            const int b0 = t0 + pad + 2 * R;
-            float buf[2 * Q], acc[Q];
-#pragma unroll
-            for (int m = 0; m < 2 * Q; ++m) buf[m] = (b0 - Q + m >= 0) ? sld(sser, QS, b0 - Q + m) : 0.f;
+            // out[t0 + q] = sum_j taps[j] * S[b0 - j + q], b0 = t0 + pad + 2R; in slots
+            // b = b0 + F (a multiple of Q), window of block J: slots b - J - Q .. b - J + Q.
+            const int kb = (t0 + pad + 2 * R + F) >> 3;  // row of slot b
+            float A[Q], B[Q], acc[Q];
+            srow_load(sser, kb - 1, A);
+            srow_load(sser, kb, B);
 #pragma unroll
             for (int q = 0; q < Q; ++q) acc[q] = 0.f;
-            for (int j = 0; j < ntaps; j += Q) {
-#pragma unroll
-                for (int st = 0; st < Q; ++st) {
-                    if (j + st < ntaps) {
-                        const float t = s_taps[j + st];
-#pragma unroll
-                        for (int q = 0; q < Q; ++q) acc[q] = fmaf(buf[Q - st + q], t, acc[q]);
-                    }
-                }
-                // Next block: S[b0 - j - 2Q .. b0 - j).
-#pragma unroll
-                for (int m = 0; m < Q; ++m) buf[Q + m] = buf[m];
-#pragma unroll
-                for (int m = 0; m < Q; ++m) {
-                    const int e = b0 - j - 2 * Q + m;
-                    buf[m] = e >= 0 ? sld(sser, QS, e) : 0.f;
-                }
+            for (int J = 0; J < ntp; J += 2 * Q) {
+                const int k = kb - (J >> 3);
+                filter_block(s_taps, J, A, B, acc);
+                srow_load(sser, k - 2, B);  // low window of block J + Q
+                filter_block(s_taps, J + Q, B, A, acc);
+                srow_load(sser, k - 3, A);  // low window of block J + 2Q
             }
 #pragma unroll
             for (int q = 0; q < Q; ++q)
@@ -162,12 +178,19 @@ fbp_status filter_h_device(fbp_context* ctx, float* data, uint64_t nseries, uint
     FBP_TRY(filter_h_taps(T, delta_t, wl_mean, wl_sigma, taps, R, pad, n));
     FilterTaps tp{};
     for (size_t j = 0; j < taps.size(); ++j) tp.w[j] = taps[j];
-    const size_t smem = ((size_t)((2 * R + 1 + 3) & ~3) +
-                         (size_t)kFilterQ * ((n + 2 * R + 2 * kFilterQ - 1) / kFilterQ + 1)) * sizeof(float);
+    constexpr int Q = kFilterQ;
+    const int ntp = (2 * R + 1 + 2 * Q - 1) / (2 * Q) * (2 * Q);
+    if (ntp > kMaxTaps) return set_error(FBP_ERR_UNSUPPORTED, "filter_H: filter longer than the tap table");
+    // F zero slots before S: 3Q <= F < 4Q with (pad + 2R + F) % Q == 0.
+    const int F = 3 * Q + (Q - (pad + 2 * R + 3 * Q) % Q) % Q;
+    // Highest slot read: t0 + pad + 2R + F + Q - 1 with t0 <= T - 1 (< E + F + Q).
+    const int rows = (n + 2 * R + F + Q) / Q + 1;
+    const size_t smem = ((size_t)ntp + (size_t)Q * rows) * sizeof(float);
     if (smem > (size_t)ctx->smem_optin) return set_error(FBP_ERR_UNSUPPORTED, "filter_H: series too long for one CTA");
     FBP_TRY_CUDA(cudaFuncSetAttribute(filter_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned blocks = (unsigned)std::min<uint64_t>(nseries, (uint64_t)ctx->sm_count * 16);
-    filter_h_kernel<<<blocks, 128, smem, stream>>>(data, nseries, T, n, R, pad, border == FBP_BORDER_EDGE, tp);
+    filter_h_kernel<<<blocks, 128, smem, stream>>>(data, nseries, T, n, R, pad, border == FBP_BORDER_EDGE, F, ntp, rows,
+                                                   tp);
     FBP_CHECK_LAUNCH(ctx, "filter_h_kernel");
     return FBP_OK;
 }
