@@ -99,6 +99,8 @@ fbp_status fbp_destroy(fbp_context* ctx) {
         if (ctx->ws[i]) cudaFree(ctx->ws[i]);
     for (void* t : ctx->twiddles)
         if (t) cudaFree(t);
+    for (void* t : ctx->stage_twiddles)
+        if (t) cudaFree(t);
     if (ctx->status_dev) cudaFree(ctx->status_dev);
     delete ctx;
     return FBP_OK;

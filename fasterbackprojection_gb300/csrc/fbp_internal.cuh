@@ -76,8 +76,10 @@ struct fbp_context {
     size_t ws_bytes[fbp::WS_NUM_SLOTS] = {};
     int* status_dev = nullptr;  // device status word: 0 ok, else an fbp_status
     uint64_t launches = 0;
-    // FFT twiddle tables, one per power-of-two length (index log2 n).
+    // FFT twiddle tables, one per power-of-two length (index log2 n): the
+    // half table exp(-2 pi i k / n) and the per-pass tables of the LCT kernels.
     void* twiddles[16] = {};
+    void* stage_twiddles[16] = {};
     // Cached LCT plan: Wiener filter of the PSF and the resampling operator
     // for the last (N, M, slope, snr) seen; valid while lct_key_valid.
     bool lct_key_valid = false;

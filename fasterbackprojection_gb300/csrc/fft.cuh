@@ -58,4 +58,20 @@ fbp_status fft_launch(fbp_context* ctx, const FftLineParams& p, int mode, int lo
 // Lines per CTA for a transform of length 2^log2n (shared memory budget).
 int fft_lines_per_cta(int log2n);
 
+// The three-pass LCT of lct_fused.cu (scan grids N x N with 8 <= N <= 64,
+// 16 <= M <= 2048 bins; both powers of two).
+struct LctFusedInputs {
+    const float* data;            // capture: [M][N][N] (time_major) or [N][N][M]
+    int time_major;
+    int log2n, log2m;
+    const int *rp, *ci, *rpt, *cit;  // resampling operator and its transpose (CSR)
+    const float *v, *vt;
+    const float* gtab;            // [M] radiometric scale per grid index
+    int power, tiled;
+    const float2* wiener;         // [2M][2N][2N]
+    float* volume;                // [M][N][N]
+};
+bool lct_fused_supported(uint32_t N, uint32_t M);
+fbp_status lct_fused_run(fbp_context* ctx, const LctFusedInputs& in, cudaStream_t stream);
+
 }  // namespace fbp

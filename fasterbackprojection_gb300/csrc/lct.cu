@@ -160,7 +160,8 @@ static fbp_status lct_plan(fbp_context* ctx, uint32_t N, uint32_t M, double slop
     const size_t hdr = 256;
     const size_t bytes_ops = hdr + (2 * (M + 1) + 2 * nnz) * sizeof(int) + 2 * nnz * sizeof(float);
     const size_t bytes_aux = 256 + (X + Z) * sizeof(double) + 2 * (size_t)M * sizeof(float);
-    FBP_TRY(workspace(ctx, WS_LCT_OPERATOR, bytes_ops + bytes_aux, s, &o));
+    const size_t aux_at = (bytes_ops + 255) & ~size_t(255);  // the aux tables start 256-aligned
+    FBP_TRY(workspace(ctx, WS_LCT_OPERATOR, aux_at + bytes_aux, s, &o));
     char* base = static_cast<char*>(o);
     int* d_rp = reinterpret_cast<int*>(base + hdr);
     int* d_ci = d_rp + (M + 1);
@@ -168,7 +169,7 @@ static fbp_status lct_plan(fbp_context* ctx, uint32_t N, uint32_t M, double slop
     int* d_cit = d_rpt + (M + 1);
     float* d_v = reinterpret_cast<float*>(d_cit + nnz);
     float* d_vt = d_v + nnz;
-    char* aux = base + ((bytes_ops + 255) & ~size_t(255));
+    char* aux = base + aux_at;
     unsigned long long* d_count = reinterpret_cast<unsigned long long*>(aux);
     double* d_gx = reinterpret_cast<double*>(aux + 256);
     double* d_gz = d_gx + X;
@@ -247,6 +248,21 @@ fbp_status lct_run(fbp_context* ctx, const float* data, int layout, uint32_t N, 
     LctOperator op{};
     FBP_TRY(lct_plan(ctx, N, M, slope, (double)prm.snr, s, &invpsf, &op));
 
+    if (lct_fused_supported(N, M)) {
+        LctFusedInputs fi{};
+        fi.data = data;
+        fi.time_major = layout == FBP_LAYOUT_TIME_MAJOR;
+        fi.log2n = ln;
+        fi.log2m = lm;
+        fi.rp = op.rp; fi.ci = op.ci; fi.v = op.v;
+        fi.rpt = op.rpt; fi.cit = op.cit; fi.vt = op.vt;
+        fi.power = prm.diffuse ? 4 : 2;
+        fi.gtab = prm.diffuse ? op.g4 : op.g2;
+        fi.tiled = prm.grid_mode == FBP_LCT_GRID_REFERENCE;
+        fi.wiener = invpsf;
+        fi.volume = volume;
+        return lct_fused_run(ctx, fi, s);
+    }
     void* a = nullptr;
     const size_t nfull = (size_t)Z * X * X;
     FBP_TRY(workspace(ctx, WS_FFT_A, nfull * sizeof(float2), s, &a));

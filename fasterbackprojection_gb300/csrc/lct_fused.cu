@@ -1,0 +1,375 @@
+// Confocal LCT in three passes for scan grids up to 64 x 64 (padded planes
+// of at most 128 x 128 complex values fit one CTA's shared memory).
+//
+// The LCT of lct.cu (python/lct.py:97-211) pads the resampled capture to
+// (2M, 2N, 2N), takes a 3-D FFT, multiplies by the PSF's Wiener filter and
+// inverse-transforms.  The 3-D transform is separable, so here the axes run
+// in the order z, (y, x) forward, filter, (y, x), z inverse, and only what is
+// not padding is ever stored:
+//   1. lct_zfwd_kernel: per scan point (y, x), radiometric scale, resample
+//      the time axis with mtx, 2M-point FFT along z (the upper M inputs are
+//      zero padding); stores buf[kz][y][x] (an N x N plane per frequency kz).
+//   2. lct_plane_kernel: per kz, the 2N x 2N plane in shared memory (rows and
+//      columns >= N are zero padding, never materialised: the first pass of
+//      each forward transform skips them, the last pass of each inverse
+//      transform skips outputs that are cut), forward row and column FFTs, times the Wiener
+//      filter, inverse column and row FFTs; stores the N x N corner back.
+//   3. lct_zinv_kernel: per (y, x), inverse 2M-point FFT along z, then rows
+//      z < M of mtx^T (the inverse resample), the 1/(2M 2N 2N) normalisation
+//      and max(., 0); stores vol[z][y][x].
+// The FFTs are Stockham passes (radix 8, then 4 or 2) with compile-time
+// sizes; each pass reads its twiddles from a per-stage table
+// exp(-2 pi i r jm / (Ns R)) built in double precision on the host.
+#include "fft.cuh"
+#include "fft_codelets.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace fbp {
+namespace {
+
+// Entries of the stage tables of an n = 2^LOG2N transform: pass p starting at
+// 2^done covers Ns * R = 2^(done + bits) entries (jm < Ns, r < R).
+constexpr int stage_radix_bits(int log2n, int done) { return log2n - done >= 3 ? 3 : log2n - done; }
+constexpr int stage_offset(int log2n, int done) {
+    int off = 0;
+    for (int d = 0; d < done; d += stage_radix_bits(log2n, d)) off += 1 << (d + stage_radix_bits(log2n, d));
+    return off;
+}
+constexpr int stage_table_size(int log2n) { return stage_offset(log2n, log2n); }
+
+// Element e of line `line`: rows are contiguous lines, columns are strided.
+template <bool COLS>
+__device__ __forceinline__ int lean_addr(int line, int e, int rs) {
+    return COLS ? e * rs + pidx(line) : line * rs + pidx(e);
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void lean_dft(float2 (&v)[R]) {
+    if constexpr (R == 8) dft8<INV>(v);
+    else if constexpr (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+    else dft2<INV>(v[0], v[1]);
+}
+
+// One Stockham pass over NLINES lines of N = 2^LOG2N points (see fft.cu for
+// the formulation), NT threads, butterflies spread over the threads.
+// HALF_IN (first pass only): inputs N/2 .. N-1 are zero, i.e. the inputs
+// r >= R/2 of every butterfly, and are not read.  HALF_OUT (last pass only):
+// outputs N/2 .. N-1, the outputs k >= R/2 of every butterfly, are not
+// stored.  Stage tables hold R entries per jm (64-byte aligned for R = 8).
+template <int LOG2N, int DONE, int NLINES, int NT, bool INV, bool COLS, bool HALF_IN, bool HALF_OUT>
+__device__ __forceinline__ void lean_pass(float2* x, const float2* tw, int rs) {
+    constexpr int RB = stage_radix_bits(LOG2N, DONE), R = 1 << RB;
+    constexpr int N = 1 << LOG2N, NB = N / R, TOTAL = NLINES * NB, NS = 1 << DONE;
+    constexpr int PER = (TOTAL + NT - 1) / NT;
+    constexpr int RIN = HALF_IN ? R / 2 : R, ROUT = HALF_OUT ? R / 2 : R;
+    static_assert(!HALF_IN || DONE == 0, "zero inputs are a first-pass property");
+    static_assert(!HALF_OUT || DONE + RB == LOG2N, "dropped outputs are a last-pass property");
+    const float2* tws = tw + stage_offset(LOG2N, DONE);
+    float2 v[PER][R];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int b = threadIdx.x + u * NT;
+        if (TOTAL % NT == 0 || b < TOTAL) {
+            const int line = COLS ? b % NLINES : b / NB, j = COLS ? b / NLINES : b % NB;
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                v[u][r] = r < RIN ? x[lean_addr<COLS>(line, j + r * NB, rs)] : make_float2(0.f, 0.f);
+            if constexpr (DONE > 0) {
+                float2 w[R];
+                if constexpr (R >= 4) {
+                    const float4* t4 = reinterpret_cast<const float4*>(tws + (j & (NS - 1)) * R);
+#pragma unroll
+                    for (int q = 0; q < R / 2; ++q) {
+                        const float4 t = t4[q];
+                        w[2 * q] = make_float2(t.x, t.y);
+                        w[2 * q + 1] = make_float2(t.z, t.w);
+                    }
+                } else {
+                    w[1] = tws[(j & (NS - 1)) * R + 1];
+                }
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    if (INV) w[r].y = -w[r].y;
+                    v[u][r] = cmul(v[u][r], w[r]);
+                }
+            }
+            lean_dft<R, INV>(v[u]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int b = threadIdx.x + u * NT;
+        if (TOTAL % NT == 0 || b < TOTAL) {
+            const int line = COLS ? b % NLINES : b / NB, j = COLS ? b / NLINES : b % NB;
+            const int d = (j >> DONE) * NS * R + (j & (NS - 1));
+#pragma unroll
+            for (int k = 0; k < ROUT; ++k) x[lean_addr<COLS>(line, d + k * NS, rs)] = v[u][k];
+        }
+    }
+    __syncthreads();
+}
+
+// A full transform; HALF_IN / HALF_OUT as in lean_pass, for the first and
+// the last pass.
+template <int LOG2N, int DONE, int NLINES, int NT, bool INV, bool COLS, bool HALF_IN = false, bool HALF_OUT = false>
+__device__ __forceinline__ void lean_fft(float2* x, const float2* tw, int rs) {
+    if constexpr (DONE < LOG2N) {
+        constexpr int NEXT = DONE + stage_radix_bits(LOG2N, DONE);
+        lean_pass<LOG2N, DONE, NLINES, NT, INV, COLS, HALF_IN && DONE == 0, HALF_OUT && NEXT == LOG2N>(x, tw, rs);
+        lean_fft<LOG2N, NEXT, NLINES, NT, INV, COLS, HALF_IN, HALF_OUT>(x, tw, rs);
+    }
+}
+
+struct LctFusedParams {
+    const float* src;             // capture, strides (bin, row, column)
+    long long sz, sy, sx;
+    int N;                        // scan side
+    const int *rp, *ci;           // mtx rows (z' -> source bins)
+    const float* v;
+    const int *rpt, *cit;         // mtx^T rows (z -> z')
+    const float* vt;
+    const float* gtab;            // [M] radiometric scale per grid index
+    int power, tiled;
+    const float2* tw_z;           // stage tables, n = 2M and n = 2N
+    const float2* tw_x;
+    const float2* wiener;         // [2M][2N][2N]
+    float2* buf;                  // [2M][N][N]
+    float* vol;                   // [M][N][N]
+    float scale;                  // 1 / (2M * 2N * 2N)
+};
+
+constexpr int kZThreads = 512;
+
+// Lines per CTA of the z kernels: 64 KiB of line buffers at most, at most 8.
+constexpr int z_lines(int log2z) { return log2z <= 10 ? 8 : (log2z == 11 ? 4 : 2); }
+
+template <int LOG2Z>
+constexpr size_t zfwd_smem() {
+    constexpr int Z = 1 << LOG2Z, C = z_lines(LOG2Z);
+    return ((size_t)C * line_stride(Z) + stage_table_size(LOG2Z)) * sizeof(float2) + (size_t)C * (Z / 2) * sizeof(float);
+}
+template <int LOG2Z>
+constexpr size_t zinv_smem() {
+    constexpr int Z = 1 << LOG2Z, C = z_lines(LOG2Z);
+    return ((size_t)C * line_stride(Z) + stage_table_size(LOG2Z)) * sizeof(float2);
+}
+template <int LOG2X>
+constexpr size_t plane_smem() {
+    constexpr int X = 1 << LOG2X;
+    return ((size_t)X * line_stride(X) + stage_table_size(LOG2X)) * sizeof(float2);
+}
+template <int LOG2X>
+constexpr int plane_threads() { return LOG2X >= 7 ? 512 : 256; }
+
+template <int LOG2Z>
+__global__ void __launch_bounds__(kZThreads, 2) lct_zfwd_kernel(LctFusedParams p) {
+    constexpr int Z = 1 << LOG2Z, M = Z / 2, C = z_lines(LOG2Z), LS = line_stride(Z), TWN = stage_table_size(LOG2Z);
+    extern __shared__ __align__(16) float2 sm[];
+    float2* lines = sm;
+    float2* tw = lines + C * LS;
+    float* raw = reinterpret_cast<float*>(tw + TWN);  // [C][M], scaled capture
+    for (int i = threadIdx.x; i < TWN; i += kZThreads) tw[i] = p.tw_z[i];
+    const int N = p.N, y = blockIdx.y, x0 = blockIdx.x * C;
+    const bool time_inner = p.sz == 1;
+    for (int e = threadIdx.x; e < C * M; e += kZThreads) {
+        // Consecutive threads read consecutive addresses in either layout.
+        const int i = time_inner ? e / M : e % C, z = time_inner ? e % M : e / C;
+        float val = 0.f;
+        if (x0 + i < N) {
+            val = p.src[z * p.sz + y * p.sy + (long long)(x0 + i) * p.sx];
+            if (p.power > 0) val *= p.gtab[p.tiled ? (z * N + y) % M : z];
+        }
+        raw[i * M + z] = val;
+    }
+    __syncthreads();
+    // z' < M only: the first FFT pass treats z' >= M as zero without reading it.
+    for (int e = threadIdx.x; e < C * M; e += kZThreads) {
+        const int i = e / M, zp = e % M;
+        float acc = 0.f;
+        for (int k = p.rp[zp]; k < p.rp[zp + 1]; ++k) acc = fmaf(p.v[k], raw[i * M + p.ci[k]], acc);
+        lines[i * LS + pidx(zp)] = make_float2(acc, 0.f);
+    }
+    __syncthreads();
+    lean_fft<LOG2Z, 0, C, kZThreads, false, false, true, false>(lines, tw, LS);  // inputs z' >= M are zero
+    for (int e = threadIdx.x; e < C * Z; e += kZThreads) {
+        const int i = e % C, kz = e / C;
+        if (x0 + i < N) p.buf[((size_t)kz * N + y) * N + x0 + i] = lines[i * LS + pidx(kz)];
+    }
+}
+
+template <int LOG2X>
+__global__ void __launch_bounds__(plane_threads<LOG2X>()) lct_plane_kernel(LctFusedParams p) {
+    constexpr int X = 1 << LOG2X, N = X / 2, RS = line_stride(X), TWN = stage_table_size(LOG2X);
+    constexpr int NT = plane_threads<LOG2X>();
+    extern __shared__ __align__(16) float2 sm[];
+    float2* plane = sm;
+    float2* tw = plane + X * RS;
+    for (int i = threadIdx.x; i < TWN; i += NT) tw[i] = p.tw_x[i];
+    const size_t kz = blockIdx.x;
+    float2* g = p.buf + kz * N * N;
+    // The N x N corner only: the first passes of the forward row and column
+    // transforms treat x >= N and y >= N as zero without reading them.
+    for (int e = threadIdx.x; e < N * N; e += NT) {
+        const int y = e / N, x = e % N;
+        plane[y * RS + pidx(x)] = g[e];
+    }
+    __syncthreads();
+    lean_fft<LOG2X, 0, N, NT, false, false, true, false>(plane, tw, RS);  // rows y < N (the rest are zero), x >= N zero
+    lean_fft<LOG2X, 0, X, NT, false, true, true, false>(plane, tw, RS);   // every column, rows y >= N zero
+    const float2* w = p.wiener + kz * X * X;
+    for (int e = threadIdx.x; e < X * X; e += NT) {
+        const int y = e / X, x = e % X;
+        plane[y * RS + pidx(x)] = cmul(plane[y * RS + pidx(x)], w[e]);
+    }
+    __syncthreads();
+    lean_fft<LOG2X, 0, X, NT, true, true, false, true>(plane, tw, RS);    // every column, rows y < N kept
+    lean_fft<LOG2X, 0, N, NT, true, false, false, true>(plane, tw, RS);   // rows y < N, x < N kept
+    for (int e = threadIdx.x; e < N * N; e += NT) {
+        const int y = e / N, x = e % N;
+        g[e] = plane[y * RS + pidx(x)];
+    }
+}
+
+template <int LOG2Z>
+__global__ void __launch_bounds__(kZThreads, 2) lct_zinv_kernel(LctFusedParams p) {
+    constexpr int Z = 1 << LOG2Z, M = Z / 2, C = z_lines(LOG2Z), LS = line_stride(Z), TWN = stage_table_size(LOG2Z);
+    extern __shared__ __align__(16) float2 sm[];
+    float2* lines = sm;
+    float2* tw = lines + C * LS;
+    for (int i = threadIdx.x; i < TWN; i += kZThreads) tw[i] = p.tw_z[i];
+    const int N = p.N, y = blockIdx.y, x0 = blockIdx.x * C;
+    for (int e = threadIdx.x; e < C * Z; e += kZThreads) {
+        const int i = e % C, kz = e / C;
+        lines[i * LS + pidx(kz)] =
+            x0 + i < N ? p.buf[((size_t)kz * N + y) * N + x0 + i] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    lean_fft<LOG2Z, 0, C, kZThreads, true, false, false, true>(lines, tw, LS);  // z < M kept
+    for (int e = threadIdx.x; e < C * M; e += kZThreads) {
+        const int i = e % C, z = e / C;
+        if (x0 + i >= N) continue;
+        float acc = 0.f;
+        for (int k = p.rpt[z]; k < p.rpt[z + 1]; ++k) acc = fmaf(p.vt[k], lines[i * LS + pidx(p.cit[k])].x, acc);
+        p.vol[((size_t)z * N + y) * N + x0 + i] = fmaxf(acc * p.scale, 0.f);
+    }
+}
+
+// Stage tables for every LOG2N, in pass order (see stage_offset).
+fbp_status stage_twiddles(fbp_context* ctx, int log2n, cudaStream_t s, const float2** out) {
+    if (log2n < 1 || log2n > 15) return set_error(FBP_ERR_UNSUPPORTED, "FFT length must be 2..32768");
+    if (!ctx->stage_twiddles[log2n]) {
+        std::vector<float2> h;
+        for (int done = 0; done < log2n;) {
+            const int rb = log2n - done >= 3 ? 3 : log2n - done;
+            const int ns = 1 << done, r = 1 << rb;
+            for (int jm = 0; jm < ns; ++jm)
+                for (int k = 0; k < r; ++k) {
+                    const double a = -2.0 * M_PI * (double)k * (double)jm / (double)(ns * r);
+                    h.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+                }
+            done += rb;
+        }
+        void* d = nullptr;
+        FBP_TRY_CUDA(cudaMalloc(&d, h.size() * sizeof(float2)));
+        FBP_TRY_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice, s));
+        FBP_TRY_CUDA(cudaStreamSynchronize(s));  // h is a host temporary
+        ctx->stage_twiddles[log2n] = d;
+    }
+    *out = static_cast<const float2*>(ctx->stage_twiddles[log2n]);
+    return FBP_OK;
+}
+
+template <int LOG2Z>
+fbp_status launch_z(fbp_context* ctx, const LctFusedParams& p, bool forward, cudaStream_t s) {
+    constexpr int C = z_lines(LOG2Z);
+    const dim3 grid(cdiv(p.N, C), p.N);
+    if (forward) {
+        constexpr size_t smem = zfwd_smem<LOG2Z>();
+        static_assert(smem <= 200 * 1024, "z-forward tile too large");
+        auto k = lct_zfwd_kernel<LOG2Z>;
+        FBP_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<grid, kZThreads, smem, s>>>(p);
+        FBP_CHECK_LAUNCH(ctx, "lct_zfwd_kernel");
+    } else {
+        constexpr size_t smem = zinv_smem<LOG2Z>();
+        auto k = lct_zinv_kernel<LOG2Z>;
+        FBP_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<grid, kZThreads, smem, s>>>(p);
+        FBP_CHECK_LAUNCH(ctx, "lct_zinv_kernel");
+    }
+    return FBP_OK;
+}
+
+template <int LOG2X>
+fbp_status launch_plane(fbp_context* ctx, const LctFusedParams& p, unsigned planes, cudaStream_t s) {
+    constexpr size_t smem = plane_smem<LOG2X>();
+    static_assert(smem <= 200 * 1024, "plane tile too large");
+    auto k = lct_plane_kernel<LOG2X>;
+    FBP_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<planes, plane_threads<LOG2X>(), smem, s>>>(p);
+    FBP_CHECK_LAUNCH(ctx, "lct_plane_kernel");
+    return FBP_OK;
+}
+
+fbp_status dispatch_z(fbp_context* ctx, int log2z, const LctFusedParams& p, bool forward, cudaStream_t s) {
+    switch (log2z) {
+        case 5: return launch_z<5>(ctx, p, forward, s);
+        case 6: return launch_z<6>(ctx, p, forward, s);
+        case 7: return launch_z<7>(ctx, p, forward, s);
+        case 8: return launch_z<8>(ctx, p, forward, s);
+        case 9: return launch_z<9>(ctx, p, forward, s);
+        case 10: return launch_z<10>(ctx, p, forward, s);
+        case 11: return launch_z<11>(ctx, p, forward, s);
+        case 12: return launch_z<12>(ctx, p, forward, s);
+        default: return set_error(FBP_ERR_UNSUPPORTED, "fbp_lct: fused path needs 16 <= M <= 2048");
+    }
+}
+
+fbp_status dispatch_plane(fbp_context* ctx, int log2x, const LctFusedParams& p, unsigned planes, cudaStream_t s) {
+    switch (log2x) {
+        case 4: return launch_plane<4>(ctx, p, planes, s);
+        case 5: return launch_plane<5>(ctx, p, planes, s);
+        case 6: return launch_plane<6>(ctx, p, planes, s);
+        case 7: return launch_plane<7>(ctx, p, planes, s);
+        default: return set_error(FBP_ERR_UNSUPPORTED, "fbp_lct: fused path needs 8 <= N <= 64");
+    }
+}
+
+}  // namespace
+
+bool lct_fused_supported(uint32_t N, uint32_t M) { return N >= 8 && N <= 64 && M >= 16 && M <= 2048; }
+
+fbp_status lct_fused_run(fbp_context* ctx, const LctFusedInputs& in, cudaStream_t s) {
+    const int log2x = in.log2n + 1, log2z = in.log2m + 1;
+    const uint32_t N = 1u << in.log2n, M = 1u << in.log2m;
+    LctFusedParams p{};
+    p.src = in.data;
+    if (in.time_major) {
+        p.sz = (long long)N * N; p.sy = N; p.sx = 1;
+    } else {
+        p.sz = 1; p.sy = (long long)N * M; p.sx = M;
+    }
+    p.N = (int)N;
+    p.rp = in.rp; p.ci = in.ci; p.v = in.v;
+    p.rpt = in.rpt; p.cit = in.cit; p.vt = in.vt;
+    p.gtab = in.gtab;
+    p.power = in.power;
+    p.tiled = in.tiled;
+    p.wiener = in.wiener;
+    p.vol = in.volume;
+    p.scale = (float)(1.0 / ((double)(2 * M) * (double)(2 * N) * (double)(2 * N)));
+    FBP_TRY(stage_twiddles(ctx, log2z, s, &p.tw_z));
+    FBP_TRY(stage_twiddles(ctx, log2x, s, &p.tw_x));
+    void* b = nullptr;
+    FBP_TRY(workspace(ctx, WS_FFT_A, (size_t)2 * M * N * N * sizeof(float2), s, &b));
+    p.buf = static_cast<float2*>(b);
+    FBP_TRY(dispatch_z(ctx, log2z, p, true, s));
+    FBP_TRY(dispatch_plane(ctx, log2x, p, 2 * M, s));
+    FBP_TRY(dispatch_z(ctx, log2z, p, false, s));
+    return FBP_OK;
+}
+
+}  // namespace fbp

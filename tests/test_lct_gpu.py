@@ -51,6 +51,21 @@ def test_lct_config1_size_vs_fp64(ctx, cuda, grid):
     assert rel_l2(got, want) < 1e-4
 
 
+@pytest.mark.parametrize("n,m", [(4, 8), (128, 32), (8, 2048), (16, 1024), (64, 16)])
+def test_lct_sizes_vs_fp64(ctx, cuda, n, m):
+    """Scan grids and bin counts on both sides of the three-pass path's range
+    (8 <= N <= 64, 16 <= M <= 2048) against the FP64 restatement."""
+    import torch
+    from fasterbackprojection_gb300 import scenes
+
+    cap = scenes.confocal_points(n, m, 32e-12 * 512 / m, n_points=40, seed=n + m)
+    data = cap.cube.reshape(n, n, m).transpose(2, 0, 1).copy()
+    got = ctx.lct(torch.from_numpy(data).to(cuda), 1.0, cap.time_step, 0.8, True).cpu().numpy()
+    want = numpy_ref.lct(data.astype(np.float64), 1.0, cap.time_step, 0.8, True)
+    assert float(np.abs(want).max()) > 0
+    assert rel_l2(got, want) < 1e-4
+
+
 def test_lct_rejects_bad_sizes(ctx, cuda):
     import torch
     from fasterbackprojection_gb300 import FbpError
