@@ -174,15 +174,26 @@ __global__ void __launch_bounds__(kZThreads, 2) lct_zfwd_kernel(LctFusedParams p
     for (int i = threadIdx.x; i < TWN; i += kZThreads) tw[i] = p.tw_z[i];
     const int N = p.N, y = blockIdx.y, x0 = blockIdx.x * C;
     const bool time_inner = p.sz == 1;
-    for (int e = threadIdx.x; e < C * M; e += kZThreads) {
-        // Consecutive threads read consecutive addresses in either layout.
-        const int i = time_inner ? e / M : e % C, z = time_inner ? e % M : e / C;
-        float val = 0.f;
-        if (x0 + i < N) {
-            val = p.src[z * p.sz + y * p.sy + (long long)(x0 + i) * p.sx];
-            if (p.power > 0) val *= p.gtab[p.tiled ? (z * N + y) % M : z];
+    {
+        // All of a thread's loads in flight together; consecutive threads read
+        // consecutive addresses in either layout.
+        constexpr int PL = (C * M + kZThreads - 1) / kZThreads;
+        float val[PL];
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kZThreads;
+            const int i = time_inner ? e / M : e % C, z = time_inner ? e % M : e / C;
+            val[u] = (e < C * M && x0 + i < N) ? p.src[z * p.sz + y * p.sy + (long long)(x0 + i) * p.sx] : 0.f;
         }
-        raw[i * M + z] = val;
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kZThreads;
+            if (e >= C * M) break;
+            const int i = time_inner ? e / M : e % C, z = time_inner ? e % M : e / C;
+            float g = 1.f;
+            if (p.power > 0) g = p.gtab[p.tiled ? (z * N + y) % M : z];
+            raw[i * M + z] = val[u] * g;
+        }
     }
     __syncthreads();
     // z' < M only: the first FFT pass treats z' >= M as zero without reading it.
@@ -212,17 +223,45 @@ __global__ void __launch_bounds__(plane_threads<LOG2X>()) lct_plane_kernel(LctFu
     float2* g = p.buf + kz * N * N;
     // The N x N corner only: the first passes of the forward row and column
     // transforms treat x >= N and y >= N as zero without reading them.
-    for (int e = threadIdx.x; e < N * N; e += NT) {
-        const int y = e / N, x = e % N;
-        plane[y * RS + pidx(x)] = g[e];
+    {
+        constexpr int PL = (N * N + NT - 1) / NT;
+        float2 t[PL];
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * NT;
+            t[u] = e < N * N ? g[e] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * NT;
+            if (e < N * N) plane[(e / N) * RS + pidx(e % N)] = t[u];
+        }
     }
     __syncthreads();
     lean_fft<LOG2X, 0, N, NT, false, false, true, false>(plane, tw, RS);  // rows y < N (the rest are zero), x >= N zero
     lean_fft<LOG2X, 0, X, NT, false, true, true, false>(plane, tw, RS);   // every column, rows y >= N zero
-    const float2* w = p.wiener + kz * X * X;
-    for (int e = threadIdx.x; e < X * X; e += NT) {
-        const int y = e / X, x = e % X;
-        plane[y * RS + pidx(x)] = cmul(plane[y * RS + pidx(x)], w[e]);
+    {
+        // The plane's Wiener filter, all of a thread's loads in flight together.
+        // Rounds of 16 loads per thread keep the register count in bounds.
+        const float2* w = p.wiener + kz * X * X;
+        constexpr int PW = (X * X + NT - 1) / NT, RW = PW < 16 ? PW : 16;
+#pragma unroll
+        for (int c = 0; c < PW; c += RW) {
+            float2 t[RW];
+#pragma unroll
+            for (int u = 0; u < RW; ++u) {
+                const int e = threadIdx.x + (c + u) * NT;
+                t[u] = e < X * X ? w[e] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < RW; ++u) {
+                const int e = threadIdx.x + (c + u) * NT;
+                if (e < X * X) {
+                    const int a = (e / X) * RS + pidx(e % X);
+                    plane[a] = cmul(plane[a], t[u]);
+                }
+            }
+        }
     }
     __syncthreads();
     lean_fft<LOG2X, 0, X, NT, true, true, false, true>(plane, tw, RS);    // every column, rows y < N kept
@@ -241,10 +280,20 @@ __global__ void __launch_bounds__(kZThreads, 2) lct_zinv_kernel(LctFusedParams p
     float2* tw = lines + C * LS;
     for (int i = threadIdx.x; i < TWN; i += kZThreads) tw[i] = p.tw_z[i];
     const int N = p.N, y = blockIdx.y, x0 = blockIdx.x * C;
-    for (int e = threadIdx.x; e < C * Z; e += kZThreads) {
-        const int i = e % C, kz = e / C;
-        lines[i * LS + pidx(kz)] =
-            x0 + i < N ? p.buf[((size_t)kz * N + y) * N + x0 + i] : make_float2(0.f, 0.f);
+    {
+        constexpr int PL = (C * Z + kZThreads - 1) / kZThreads;
+        float2 t[PL];
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kZThreads;
+            const int i = e % C, kz = e / C;
+            t[u] = (e < C * Z && x0 + i < N) ? p.buf[((size_t)kz * N + y) * N + x0 + i] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kZThreads;
+            if (e < C * Z) lines[(e % C) * LS + pidx(e / C)] = t[u];
+        }
     }
     __syncthreads();
     lean_fft<LOG2Z, 0, C, kZThreads, true, false, false, true>(lines, tw, LS);  // z < M kept
