@@ -170,6 +170,50 @@ __device__ __forceinline__ float add_rz(float a, float b) {
     return r;
 }
 
+// Packed FP32 pairs (the f32x2 instructions of sm_100 and later): one
+// instruction applies the scalar operation above to both halves, with the
+// same rounding, so results are bitwise those of two scalar operations.
+typedef unsigned long long f32x2_t;
+__device__ __forceinline__ f32x2_t pack2(float lo, float hi) {
+    f32x2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(f32x2_t v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2_t sub_rn2(f32x2_t a, f32x2_t b) {
+    f32x2_t r;
+    asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2_t mul_rn2(f32x2_t a, f32x2_t b) {
+    f32x2_t r;
+    asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2_t fma_rn2(f32x2_t a, f32x2_t b, f32x2_t c) {
+    f32x2_t r;
+    asm("fma.rn.ftz.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ f32x2_t add_rz2(f32x2_t a, f32x2_t b) {
+    f32x2_t r;
+    asm("add.rz.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+// a * b and fmaf (no flush to zero) on both halves.
+__device__ __forceinline__ f32x2_t mulf2(f32x2_t a, f32x2_t b) {
+    f32x2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2_t fmaf2(f32x2_t a, f32x2_t b, f32x2_t c) {
+    f32x2_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // |d|^2 of the difference vector with the reference's rounding sequence:
 // the y product is rounded first, then x and z are fused in.
 __device__ __forceinline__ float ref_dot3(float dx, float dy, float dz) {
