@@ -187,6 +187,30 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
         const float cl = s_cl[buf_cur * CHMAX + i];
         const S* slot = s_slots + (size_t)(buf_cur * CH + i) * slot_stride;
         const float bnc = BOUNCE ? add_rn(lg.w, sg.w) : 0.f;
+        if constexpr (!EXACT_TRUNC && KV % 2 == 0) {
+            if (!safe) {
+                // Voxel pairs in packed FP32 pairs, the scalar loop's operations.
+                const f32x2_t t0p = pack2(p.t0, p.t0), rdp = pack2(rcp_dt, rcp_dt), clp = pack2(cl, cl);
+                const f32x2_t bncp = pack2(bnc, bnc);
+#pragma unroll
+                for (int j = 0; j < KV / 2; ++j) {
+                    f32x2_t dist = sub_rn2(add_rn2(pack2(dl[li][2 * j], dl[li][2 * j + 1]),
+                                                   pack2(ds[2 * j], ds[2 * j + 1])), t0p);
+                    if (BOUNCE) dist = add_rn2(dist, bncp);
+                    float b0, b1;
+                    unpack2(add_rz2(mul_rn2(dist, rdp), clp), b0, b1);
+                    const uint32_t i0 = min(__float_as_uint(b0) - 0x4B000000u, p.slot_w);
+                    const uint32_t i1 = min(__float_as_uint(b1) - 0x4B000000u, p.slot_w);
+                    const f32x2_t I = pack2(to_f32(slot[i0]), to_f32(slot[i1]));
+                    float s0, s1;
+                    unpack2(mul_rn2(dist, dist), s0, s1);
+                    const f32x2_t a = fmaf2(I, pack2(rcp_approx(s0), rcp_approx(s1)),
+                                            pack2(acc[2 * j], acc[2 * j + 1]));
+                    unpack2(a, acc[2 * j], acc[2 * j + 1]);
+                }
+                return;
+            }
+        }
 #pragma unroll
         for (int k = 0; k < KV; ++k) {
             float dist = sub_rn(add_rn(dl[li][k], ds[k]), p.t0);
@@ -207,10 +231,22 @@ exhaustive_gather_kernel(ExhaustiveGatherParams p) {
     auto point_dist = [&](const float4& g, float (&d)[KV]) {
         const float ddy = sub_rn(py, g.y), ddz = sub_rn(pz, g.z);
         const float ddy2 = mul_rn(ddy, ddy);
+        if constexpr (KV % 2 == 0) {
+            const f32x2_t gxp = pack2(g.x, g.x), ddzp = pack2(ddz, ddz), ddy2p = pack2(ddy2, ddy2);
 #pragma unroll
-        for (int k = 0; k < KV; ++k) {
-            const float dx = sub_rn(px[k], g.x);
-            d[k] = sqrt_approx(fma_rn(ddz, ddz, fma_rn(dx, dx, ddy2)));
+            for (int j = 0; j < KV / 2; ++j) {
+                const f32x2_t dx = sub_rn2(pack2(px[2 * j], px[2 * j + 1]), gxp);
+                float q0, q1;
+                unpack2(fma_rn2(ddzp, ddzp, fma_rn2(dx, dx, ddy2p)), q0, q1);
+                d[2 * j] = sqrt_approx(q0);
+                d[2 * j + 1] = sqrt_approx(q1);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < KV; ++k) {
+                const float dx = sub_rn(px[k], g.x);
+                d[k] = sqrt_approx(fma_rn(ddz, ddz, fma_rn(dx, dx, ddy2)));
+            }
         }
     };
 

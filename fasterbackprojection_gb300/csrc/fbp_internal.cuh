@@ -187,6 +187,11 @@ __device__ __forceinline__ f32x2_t sub_rn2(f32x2_t a, f32x2_t b) {
     asm("sub.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+__device__ __forceinline__ f32x2_t add_rn2(f32x2_t a, f32x2_t b) {
+    f32x2_t r;
+    asm("add.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ f32x2_t mul_rn2(f32x2_t a, f32x2_t b) {
     f32x2_t r;
     asm("mul.rn.ftz.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
