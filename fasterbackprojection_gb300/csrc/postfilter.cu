@@ -274,6 +274,64 @@ __global__ void __launch_bounds__(512) laplacian_filter_kernel(const float* __re
     out[((size_t)z * ny + y) * nx + x] = fma_rn(k3, c, -lap);
 }
 
+// The same filter for H <= 2, register-blocked along z: a thread owns one
+// (x, y) column of TZ outputs.  For each (dx, dy) in the reference's order it
+// loads the input column (TZ + 2H values) once and adds its 2H + 1 z terms
+// into every output, dz ascending, so each output still receives the terms
+// in the order x outermost, z innermost: bitwise equal to
+// laplacian_filter_kernel, with one shared-memory load per 2H + 1 adds
+// instead of one per add, and TZ independent sums.  Tile 32 x 4 x 32 outputs.
+template <int H>
+__global__ void __launch_bounds__(128) laplacian_zblock_kernel(const float* __restrict__ in, float* __restrict__ out,
+                                                               uint32_t nx, uint32_t ny, uint32_t nz, float k3) {
+    constexpr int K = 2 * H + 1, TX = 32, TY = 4, TZ = 32;
+    constexpr int EX = TX + 2 * H, EY = TY + 2 * H, EZ = TZ + 2 * H;
+    __shared__ float tile[EZ][EY][EX];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    constexpr int NT = TX * TY, NE = EX * EY * EZ, B = 8;
+    for (int i0 = tid; i0 < NE; i0 += B * NT) {
+        float v[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int i = i0 + u * NT;
+            v[u] = 0.f;  // zero outside the volume
+            if (i < NE) {
+                const int lx = i % EX, ly = (i / EX) % EY, lz = i / (EX * EY);
+                const int gx = x0 + lx - H, gy = y0 + ly - H, gz = z0 + lz - H;
+                if (gx >= 0 && gx < (int)nx && gy >= 0 && gy < (int)ny && gz >= 0 && gz < (int)nz)
+                    v[u] = in[((size_t)gz * ny + gy) * nx + gx];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (i0 + u * NT < NE) (&tile[0][0][0])[i0 + u * NT] = v[u];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = x0 + tx, y = y0 + ty;
+    if (x >= (int)nx || y >= (int)ny) return;
+    float lap[TZ];
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) lap[z] = 0.f;
+#pragma unroll 1
+    for (int dx = 0; dx < K; ++dx) {
+#pragma unroll 1
+        for (int dy = 0; dy < K; ++dy) {
+            float c[EZ];
+#pragma unroll
+            for (int z = 0; z < EZ; ++z) c[z] = tile[z][ty + dy][tx + dx];
+#pragma unroll
+            for (int z = 0; z < TZ; ++z)
+#pragma unroll
+                for (int dz = 0; dz < K; ++dz) lap[z] = add_rn(lap[z], c[z + dz]);
+        }
+    }
+#pragma unroll
+    for (int z = 0; z < TZ; ++z)
+        if (z0 + z < (int)nz) out[((size_t)(z0 + z) * ny + y) * nx + x] = fma_rn(k3, tile[z + H][ty + H][tx + H], -lap[z]);
+}
+
 fbp_status launch_log(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz, int ksize,
                       float sigma, cudaStream_t stream);
 fbp_status launch_laplacian(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz,
@@ -341,6 +399,12 @@ static fbp_status log_h(fbp_context* ctx, const float* in, float* out, uint32_t 
 template <int H>
 static fbp_status lap_h(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz, float k3,
                         cudaStream_t stream) {
+    if constexpr (H <= 2) {
+        const dim3 grid(cdiv(nx, 32), cdiv(ny, 4), cdiv(nz, 32));
+        laplacian_zblock_kernel<H><<<grid, dim3(32, 4), 0, stream>>>(in, out, nx, ny, nz, k3);
+        FBP_CHECK_LAUNCH(ctx, "laplacian_zblock_kernel");
+        return FBP_OK;
+    }
     constexpr int E = 8 + 2 * H;
     const size_t smem = sizeof(float) * E * E * E;
     FBP_TRY_CUDA(cudaFuncSetAttribute(laplacian_filter_kernel<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
