@@ -60,10 +60,33 @@ struct SplatGrid {
     uint32_t Vx, Vy, Vz;
 };
 
-// One CTA per instance: its threads walk the pixels of the disk's bounding box.
+// Pixel-centre coordinates and voxel indices of the grid's columns (x) and
+// rows (z), computed once per call with the per-pixel expressions: x = x0 +
+// ix * px, vx = (uint)((x - hx) / vsx), or -1 outside the volume.
+__global__ void splat_axes_kernel(SplatGrid gd, float* __restrict__ xs, int* __restrict__ vxs, float* __restrict__ zs,
+                                  int* __restrict__ vys) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < gd.w) {
+        const float x = __fadd_rn(gd.x0, __fmul_rn((float)i, gd.px));
+        const float fx = __fdiv_rn(__fsub_rn(x, gd.hx), gd.vsx);
+        xs[i] = x;
+        vxs[i] = (fx >= 0.f && (uint32_t)fx < gd.Vx) ? (int)(uint32_t)fx : -1;
+    }
+    if (i < gd.h) {
+        const float z = __fadd_rn(gd.z0, __fmul_rn((float)i, gd.pz));
+        const float fz = __fdiv_rn(__fsub_rn(z, gd.hz), gd.vsz);
+        zs[i] = z;
+        vys[i] = (fz >= 0.f && (uint32_t)fz < gd.Vy) ? (int)(uint32_t)fz : -1;  // volume vy <- world z
+    }
+}
+
+// One CTA per instance: 32 x 8 threads walk the rows and columns of the
+// disk's bounding box.
 __global__ void __launch_bounds__(256) splat_kernel(const SplatInstance* __restrict__ inst,
                                                     const unsigned int* __restrict__ count, uint32_t cap,
-                                                    SplatGrid gd, float* __restrict__ vol) {
+                                                    SplatGrid gd, const float* __restrict__ xs,
+                                                    const int* __restrict__ vxs, const float* __restrict__ zs,
+                                                    const int* __restrict__ vys, float* __restrict__ vol) {
     const uint32_t n = min(*count, cap);
     for (uint32_t k = blockIdx.x; k < n; k += gridDim.x) {
         const SplatInstance s = inst[k];
@@ -76,23 +99,25 @@ __global__ void __launch_bounds__(256) splat_kernel(const SplatInstance* __restr
         const int ix0 = (int)fmaxf(fx0, 0.f), ix1 = (int)fminf(fx1, (float)gd.w - 1.f);
         const int iz0 = (int)fmaxf(fz0, 0.f), iz1 = (int)fminf(fz1, (float)gd.h - 1.f);
         if (ix1 < ix0 || iz1 < iz0) continue;
-        const int nx = ix1 - ix0 + 1, npix = nx * (iz1 - iz0 + 1);
         const float r2 = __fmul_rn(s.r, s.r);
-        for (int p = threadIdx.x; p < npix; p += blockDim.x) {
-            const int ix = ix0 + p % nx, iz = iz0 + p / nx;
-            const float x = __fadd_rn(gd.x0, __fmul_rn((float)ix, gd.px));
-            const float z = __fadd_rn(gd.z0, __fmul_rn((float)iz, gd.pz));
-            const float dx = __fsub_rn(x, s.cx), dz = __fsub_rn(z, s.cz);
-            const float h2 = __fsub_rn(__fsub_rn(r2, __fmul_rn(dx, dx)), __fmul_rn(dz, dz));
-            if (h2 < 0.f) continue;
-            const float y = __fsub_rn(s.cy, __fsqrt_rn(h2));
-            const float fx = __fdiv_rn(__fsub_rn(x, gd.hx), gd.vsx);
-            const float fy = __fdiv_rn(__fsub_rn(y, gd.hy), gd.vsy);
-            const float fz = __fdiv_rn(__fsub_rn(z, gd.hz), gd.vsz);
-            if (fx < 0.f || fy < 0.f || fz < 0.f) continue;
-            const uint32_t vx = (uint32_t)fx, vz = (uint32_t)fy, vy = (uint32_t)fz;  // volume (vx, vy, vz) <- world (x, z, y)
-            if (vx >= gd.Vx || vy >= gd.Vy || vz >= gd.Vz) continue;
-            atomicAdd(vol + ((uint64_t)vz * gd.Vy + vy) * gd.Vx + vx, s.intensity);
+        for (int iz = iz0 + (int)threadIdx.y; iz <= iz1; iz += 8) {
+            const int vy = vys[iz];
+            if (vy < 0) continue;
+            const float dz = __fsub_rn(zs[iz], s.cz);
+            const float dz2 = __fmul_rn(dz, dz);
+            float* col = vol + (uint64_t)vy * gd.Vx;
+            for (int ix = ix0 + (int)threadIdx.x; ix <= ix1; ix += 32) {
+                const float dx = __fsub_rn(xs[ix], s.cx);
+                const float h2 = __fsub_rn(__fsub_rn(r2, __fmul_rn(dx, dx)), dz2);
+                const int vx = vxs[ix];
+                if (h2 < 0.f || vx < 0) continue;
+                const float y = __fsub_rn(s.cy, __fsqrt_rn(h2));
+                const float fy = __fdiv_rn(__fsub_rn(y, gd.hy), gd.vsy);
+                if (!(fy >= 0.f)) continue;
+                const uint32_t vz = (uint32_t)fy;  // volume vz <- world y
+                if (vz >= gd.Vz) continue;
+                atomicAdd(col + (uint64_t)vz * gd.Vy * gd.Vx + vx, s.intensity);
+            }
         }
     }
 }
@@ -108,10 +133,16 @@ fbp_status splat_typed(fbp_context* ctx, const fbp_recon_info& in, const void* c
     const uint64_t cap64 = (uint64_t)L * nbins;
     if (cap64 > 0x7FFFFFFFull) return set_error(FBP_ERR_UNSUPPORTED, "fbp_splat_backproject: too many (scan point, bin) pairs");
     const uint32_t cap = (uint32_t)cap64;
+    // Workspace: count, the axis tables (x, vx per column; z, vy per row), the instances.
+    const size_t axes = ((size_t)2 * (grid_w + grid_h) * 4 + 255) & ~size_t(255);
     void* ws = nullptr;
-    FBP_TRY(workspace(ctx, WS_MISC, 256 + (size_t)cap * sizeof(SplatInstance), s, &ws));
+    FBP_TRY(workspace(ctx, WS_MISC, 256 + axes + (size_t)cap * sizeof(SplatInstance), s, &ws));
     unsigned int* count = static_cast<unsigned int*>(ws);
-    SplatInstance* inst = reinterpret_cast<SplatInstance*>(static_cast<char*>(ws) + 256);
+    float* ax_x = reinterpret_cast<float*>(static_cast<char*>(ws) + 256);
+    int* ax_vx = reinterpret_cast<int*>(ax_x + grid_w);
+    float* ax_z = reinterpret_cast<float*>(ax_vx + grid_w);
+    int* ax_vy = reinterpret_cast<int*>(ax_z + grid_h);
+    SplatInstance* inst = reinterpret_cast<SplatInstance*>(static_cast<char*>(ws) + 256 + axes);
     const uint64_t V = (uint64_t)in.voxel_res[0] * in.voxel_res[1] * in.voxel_res[2];
     FBP_TRY_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned int), s));
     FBP_TRY_CUDA(cudaMemsetAsync(volume, 0, V * sizeof(float), s));
@@ -136,8 +167,10 @@ fbp_status splat_typed(fbp_context* ctx, const fbp_recon_info& in, const void* c
     gd.Vx = in.voxel_res[0];
     gd.Vy = in.voxel_res[1];
     gd.Vz = in.voxel_res[2];
+    splat_axes_kernel<<<cdiv(std::max(grid_w, grid_h), 256), 256, 0, s>>>(gd, ax_x, ax_vx, ax_z, ax_vy);
+    FBP_CHECK_LAUNCH(ctx, "splat_axes_kernel");
     const unsigned blocks = (unsigned)std::min<uint64_t>(cap, (uint64_t)ctx->sm_count * 64);
-    splat_kernel<<<std::max(1u, blocks), 256, 0, s>>>(inst, count, cap, gd, volume);
+    splat_kernel<<<std::max(1u, blocks), dim3(32, 8), 0, s>>>(inst, count, cap, gd, ax_x, ax_vx, ax_z, ax_vy, volume);
     FBP_CHECK_LAUNCH(ctx, "splat_kernel");
     return FBP_OK;
 }
