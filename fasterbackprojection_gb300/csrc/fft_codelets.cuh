@@ -71,6 +71,40 @@ __device__ __forceinline__ void dft8(float2* v) {
     v[7] = csub(e3, o3);
 }
 
+// 16-point DFT as 4 x 4: n = n1 + 4 n2, k = k2 + 4 k1; DFT4 over n2 for
+// every n1, twiddles w16^(n1 k2), DFT4 over n1 for every k2, then the
+// transposition back to natural order.
+template <bool INV>
+__device__ __forceinline__ float2 cmul_const(float2 a, float c, float s) {  // a * (c + i s)
+    return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+template <bool INV>
+__device__ __forceinline__ void dft16(float2* v) {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) dft4<INV>(v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]);
+    constexpr float c1 = 0.92387953251128674f, s1 = 0.38268343236508977f, h = 0.70710678118654752f;
+    constexpr float sg = INV ? 1.f : -1.f;  // sign of the imaginary parts of w16^k
+    v[5] = cmul_const<INV>(v[5], c1, sg * s1);     // n1 = 1, k2 = 1: w^1
+    v[9] = cmul_const<INV>(v[9], h, sg * h);       // n1 = 1, k2 = 2: w^2
+    v[13] = cmul_const<INV>(v[13], s1, sg * c1);   // n1 = 1, k2 = 3: w^3
+    v[6] = cmul_const<INV>(v[6], h, sg * h);       // n1 = 2, k2 = 1: w^2
+    v[10] = rot_mi<INV>(v[10]);                     // n1 = 2, k2 = 2: w^4
+    v[14] = cmul_const<INV>(v[14], -h, sg * h);    // n1 = 2, k2 = 3: w^6
+    v[7] = cmul_const<INV>(v[7], s1, sg * c1);     // n1 = 3, k2 = 1: w^3
+    v[11] = cmul_const<INV>(v[11], -h, sg * h);    // n1 = 3, k2 = 2: w^6
+    v[15] = cmul_const<INV>(v[15], -c1, -sg * s1); // n1 = 3, k2 = 3: w^9
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) dft4<INV>(v[4 * k2], v[4 * k2 + 1], v[4 * k2 + 2], v[4 * k2 + 3]);
+    // v[k1 + 4 k2] holds X[k2 + 4 k1].
+    float2 t[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) t[i] = v[i];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) v[k2 + 4 * k1] = t[k1 + 4 * k2];
+}
+
 // Shared-memory layout of a line: element j at pidx(j) = j + j/16 (one pad
 // slot per 128 bytes breaks the power-of-two strides of the Stockham writes
 // into different banks); lines are line_stride(n) = n + n/16 + 1 apart so the

@@ -17,7 +17,7 @@
 //   3. lct_zinv_kernel: per (y, x), inverse 2M-point FFT along z, then rows
 //      z < M of mtx^T (the inverse resample), the 1/(2M 2N 2N) normalisation
 //      and max(., 0); stores vol[z][y][x].
-// The FFTs are Stockham passes (radix 8, then 4 or 2) with compile-time
+// The FFTs are Stockham passes (radix 16 or 8, then 4 or 2) with compile-time
 // sizes; each pass reads its twiddles from a per-stage table
 // exp(-2 pi i r jm / (Ns R)) built in double precision on the host.
 #include "fft.cuh"
@@ -30,8 +30,12 @@ namespace fbp {
 namespace {
 
 // Entries of the stage tables of an n = 2^LOG2N transform: pass p starting at
-// 2^done covers Ns * R = 2^(done + bits) entries (jm < Ns, r < R).
-constexpr int stage_radix_bits(int log2n, int done) { return log2n - done >= 3 ? 3 : log2n - done; }
+// 2^done covers Ns * R = 2^(done + bits) entries (jm < Ns, r < R).  Radices:
+// the fewest passes, radix 16 where it saves one (4 bits), else 8, then 4 or 2.
+constexpr int stage_radix_bits(int log2n, int done) {
+    const int rem = log2n - done;
+    return (rem == 4 || rem == 7 || rem == 8 || rem >= 10) ? 4 : (rem >= 3 ? 3 : rem);
+}
 constexpr int stage_offset(int log2n, int done) {
     int off = 0;
     for (int d = 0; d < done; d += stage_radix_bits(log2n, d)) off += 1 << (d + stage_radix_bits(log2n, d));
@@ -47,7 +51,8 @@ __device__ __forceinline__ int lean_addr(int line, int e, int rs) {
 
 template <int R, bool INV>
 __device__ __forceinline__ void lean_dft(float2 (&v)[R]) {
-    if constexpr (R == 8) dft8<INV>(v);
+    if constexpr (R == 16) dft16<INV>(v);
+    else if constexpr (R == 8) dft8<INV>(v);
     else if constexpr (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
     else dft2<INV>(v[0], v[1]);
 }
@@ -57,7 +62,7 @@ __device__ __forceinline__ void lean_dft(float2 (&v)[R]) {
 // HALF_IN (first pass only): inputs N/2 .. N-1 are zero, i.e. the inputs
 // r >= R/2 of every butterfly, and are not read.  HALF_OUT (last pass only):
 // outputs N/2 .. N-1, the outputs k >= R/2 of every butterfly, are not
-// stored.  Stage tables hold R entries per jm (64-byte aligned for R = 8).
+// stored.  Stage tables hold R entries per jm (64-byte aligned for R >= 8).
 template <int LOG2N, int DONE, int NLINES, int NT, bool INV, bool COLS, bool HALF_IN, bool HALF_OUT>
 __device__ __forceinline__ void lean_pass(float2* x, const float2* tw, int rs) {
     constexpr int RB = stage_radix_bits(LOG2N, DONE), R = 1 << RB;
@@ -312,7 +317,7 @@ fbp_status stage_twiddles(fbp_context* ctx, int log2n, cudaStream_t s, const flo
     if (!ctx->stage_twiddles[log2n]) {
         std::vector<float2> h;
         for (int done = 0; done < log2n;) {
-            const int rb = log2n - done >= 3 ? 3 : log2n - done;
+            const int rb = stage_radix_bits(log2n, done);
             const int ns = 1 << done, r = 1 << rb;
             for (int jm = 0; jm < ns; ++jm)
                 for (int k = 0; k < r; ++k) {
