@@ -90,7 +90,7 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
         }
         return;
     }
-    if constexpr (PATH == PATH_2D && !SAFE && KV % 2 == 0) {
+    if constexpr (PATH != PATH_SCATTER && !SAFE && KV % 2 == 0) {
         // Voxel pairs (k, k + 1) in packed FP32 pairs: the same operations
         // as the scalar loop below, half the FP32 instructions.
         f32x2_t pxp[KV / 2], accp[KV / 2];
@@ -99,7 +99,8 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
             pxp[j] = pack2(px[2 * j], px[2 * j + 1]);
             accp[j] = pack2(acc[2 * j], acc[2 * j + 1]);
         }
-        const f32x2_t rcp2p = pack2(rcp2, rcp2);
+        const f32x2_t rcp2p = pack2(rcp2, rcp2), rdp = pack2(rcp_dt, rcp_dt), two = pack2(2.f, 2.f);
+        const f32x2_t nt0p = pack2(neg_t0, neg_t0);
 #pragma unroll 2
         for (int i = 0; i < nl; ++i) {
             const float4 g = geo[i];
@@ -109,26 +110,43 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
             const f32x2_t gxp = pack2(g.x, g.x), dy2p = pack2(dy2, dy2), dzp = pack2(dz, dz);
             const f32x2_t biasp = pack2(__int_as_float(m.x), __int_as_float(m.x));
             const f32x2_t wlp = WEIGHTED ? pack2(wts[i], wts[i]) : 0ull;
+            const f32x2_t gwp = pack2(g.w, g.w);
 #pragma unroll
             for (int j = 0; j < KV / 2; ++j) {
                 const f32x2_t dx = sub_rn2(pxp[j], gxp);
                 float q0, q1;
                 unpack2(fma_rn2(dzp, dzp, fma_rn2(dx, dx, dy2p)), q0, q1);
                 const f32x2_t d = pack2(sqrt_approx(q0), sqrt_approx(q1));
-                float b0, b1;
-                unpack2(add_rz2(mul_rn2(d, rcp2p), biasp), b0, b1);
-                uint32_t a0, a1;
-                if (CLAMP) {
-                    a0 = (uint32_t)m.y + (min(__float_as_uint(b0) - 0x4B000000u, slot_w) << SH);
-                    a1 = (uint32_t)m.y + (min(__float_as_uint(b1) - 0x4B000000u, slot_w) << SH);
+                f32x2_t x, dist = 0ull;
+                if (PATH == PATH_2D) {
+                    x = mul_rn2(d, rcp2p);
                 } else {
-                    a0 = (uint32_t)m.y + (__float_as_uint(b0) << SH);  // bias folded into m.y
-                    a1 = (uint32_t)m.y + (__float_as_uint(b1) << SH);
+                    dist = fma_rn2(d, two, nt0p);
+                    if (BOUNCE) dist = add_rn2(dist, gwp);
+                    x = mul_rn2(dist, rdp);
+                }
+                uint32_t a0, a1;
+                if (PATH == PATH_EXACT) {
+                    float x0, x1;
+                    unpack2(x, x0, x1);
+                    const int b0 = __float2int_rz(x0), b1 = __float2int_rz(x1);  // static_cast<int>
+                    a0 = (uint32_t)m.y + (min((uint32_t)(b0 - m.x), slot_w) << SH);
+                    a1 = (uint32_t)m.y + (min((uint32_t)(b1 - m.x), slot_w) << SH);
+                } else {
+                    float b0, b1;
+                    unpack2(add_rz2(x, biasp), b0, b1);
+                    if (CLAMP) {
+                        a0 = (uint32_t)m.y + (min(__float_as_uint(b0) - 0x4B000000u, slot_w) << SH);
+                        a1 = (uint32_t)m.y + (min(__float_as_uint(b1) - 0x4B000000u, slot_w) << SH);
+                    } else {
+                        a0 = (uint32_t)m.y + (__float_as_uint(b0) << SH);  // bias folded into m.y
+                        a1 = (uint32_t)m.y + (__float_as_uint(b1) << SH);
+                    }
                 }
                 f32x2_t I = pack2(lds_elem<S>(a0), lds_elem<S>(a1));
                 if (WEIGHTED) I = mulf2(I, wlp);
                 float s0, s1;
-                unpack2(mul_rn2(d, d), s0, s1);
+                unpack2(PATH == PATH_2D ? mul_rn2(d, d) : mul_rn2(dist, dist), s0, s1);
                 accp[j] = fmaf2(I, pack2(rcp_approx(s0), rcp_approx(s1)), accp[j]);
             }
         }
