@@ -334,10 +334,15 @@ extern "C" fbp_status fbp_transient_images(fbp_context* ctx, const float* data, 
                             normalize, rgba, (cudaStream_t)stream);
 }
 
+// The encoder indexes the filtered rows with 32-bit positions.
+constexpr uint64_t kPngMaxRaw = (uint64_t)1 << 30;
+
 extern "C" fbp_status fbp_write_png(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height) {
     clear_error();
     if (!path || !rgba || width == 0 || height == 0 || width > 65535 || height > 65535)
         return set_error(FBP_ERR_INVALID_ARG, "fbp_write_png: bad arguments");
+    if (((uint64_t)width * 4 + 1) * height > kPngMaxRaw)
+        return set_error(FBP_ERR_UNSUPPORTED, "fbp_write_png: image larger than 1 GiB of pixels");
     if (!write_file(path, encode_png(rgba, width, height)))
         return set_error(FBP_ERR_IO, std::string("fbp_write_png: cannot write ") + path);
     return FBP_OK;
@@ -352,6 +357,8 @@ extern "C" fbp_status fbp_save_transient_images(fbp_context* ctx, const float* d
     FBP_TRY(check_image_args("fbp_save_transient_images", data, width, height, num_planes, pixel_stride, plane_stride,
                              out_width, out_height));
     if (!prefix) return set_error(FBP_ERR_INVALID_ARG, "fbp_save_transient_images: null prefix");
+    if (((uint64_t)out_width * 4 + 1) * out_height > kPngMaxRaw)
+        return set_error(FBP_ERR_UNSUPPORTED, "fbp_save_transient_images: image larger than 1 GiB of pixels");
     const uint32_t num_depths = num_planes;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t plane = (size_t)out_width * out_height * 4, bytes = plane * num_depths;

@@ -122,3 +122,16 @@ def test_depth_image_size_rule():
     assert depth_image_size(256) == (256, 256)
     assert depth_image_size(300) == (300, 300)
     assert depth_image_size(16, exhaustive=True) == (64, 64)
+
+
+def test_png_writer_rejects_oversized_images(tmp_path, built):
+    """Above 1 GiB of filtered rows the writer refuses before reading pixels."""
+    import ctypes
+
+    from fasterbackprojection_gb300 import _lib
+
+    buf = np.zeros(16, np.uint8)
+    rc = _lib.load().fbp_write_png(str(tmp_path / "x.png").encode(), buf.ctypes.data_as(ctypes.c_void_p), 40000,
+                                   40000)
+    assert rc == _lib.FBP_ERR_UNSUPPORTED
+    assert not (tmp_path / "x.png").exists()
