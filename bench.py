@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import re
 import statistics
@@ -833,6 +834,32 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
     res["filter_h"] = {"ms": fh_ms, "bytes": 8 * nb, "achieved_gbs": 8 * nb / (fh_ms / 1e3) / 1e9,
                        "frac": 8 * nb / (fh_ms / 1e3) / 1e9 / peak,
                        "workload": "256^2 series x 1024 bins, wavelength 10 bins (taps over 1106 padded bins)"}
+    # LoG-FFT (LoGFFT::compute): ours against the reference's own arithmetic
+    # path, an R2C FFT, the half-grid response and a C2R FFT through cuFFT
+    # (the library the reference calls), on the same volume.
+    from fasterbackprojection_gb300 import FBP_FILTER_LOG_FFT
+
+    n = vol.shape[0]
+    _, lf_ms = timed_ms(lambda: ctx.postfilter(FBP_FILTER_LOG_FFT, vol, 5, 1.0, out=out))
+    f = torch.fft.fftfreq(n, device=vol.device).float()
+    fz, fy, fx = torch.meshgrid(f, f, f[: n // 2 + 1].abs(), indexing="ij")
+    k2 = fx * fx + fy * fy + fz * fz
+    resp = (-4 * math.pi ** 2 * k2 * torch.exp(-2 * math.pi ** 2 * k2)).contiguous()
+    ref_out = torch.empty_like(vol)
+
+    def cufft_path():
+        ref_out.copy_(torch.fft.irfftn(torch.fft.rfftn(vol) * resp, s=vol.shape, norm="forward"))
+
+    cf_ms = 0.0
+    try:
+        _, cf_ms = timed_ms(cufft_path)
+        rel = float(torch.linalg.vector_norm((out - ref_out).double()) / torch.linalg.vector_norm(ref_out.double()))
+    except RuntimeError as e:  # pragma: no cover
+        rel = None
+        cf_ms = None
+        res["log_fft_cufft_unavailable"] = str(e)
+    res["log_fft"] = {"ms": lf_ms, "cufft_r2c_c2r_ms": cf_ms, "rel_l2_vs_cufft": rel,
+                      "bytes": 8 * V, "frac": 8 * V / (lf_ms / 1e3) / 1e9 / peak}
     return res
 
 

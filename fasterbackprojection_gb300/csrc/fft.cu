@@ -103,17 +103,6 @@ __device__ __forceinline__ void fft_stages(float2* x, const float2* tw, int log2
     else if (log2n - done == 1) stockham_pass<2, INV>(x, tw, log2n, done, C);
 }
 
-// buildLoGKernel3D (transient_postprocessing.cuh:116-148) at full-grid index (x, y, z).
-__device__ __forceinline__ float log_response(int x, int y, int z, int nx, int ny, int nz, float sigma) {
-    const float fx = (x <= nx / 2) ? (float)x : (float)(x - nx);
-    const float fy = (y <= ny / 2) ? (float)y : (float)(y - ny);
-    const float fz = (z <= nz / 2) ? (float)z : (float)(z - nz);
-    const float fxn = fx / nx, fyn = fy / ny, fzn = fz / nz;
-    const float k2 = fxn * fxn + fyn * fyn + fzn * fzn;
-    const float pi = 3.14159265358979323846f;
-    return -4.0f * pi * pi * k2 * expf(-2.0f * pi * pi * sigma * sigma * k2);
-}
-
 // Element j of line i of this CTA's group.
 __device__ __forceinline__ long long fft_offset(const FftLineParams& p, long long base, int i, int j) {
     return base + (long long)i * p.line_step + (long long)j * p.elem_stride;
@@ -302,15 +291,17 @@ static int ilog2_exact(uint32_t v) {
 }
 
 // LoGFFT::compute (PostprocessingFilters.cu:36-77): out = unnormalised
-// inverse FFT of FFT(in) * LoG(k), done as full complex transforms of the real
-// volume (equal to the reference's R2C/C2R pair for this real, symmetric
-// response).  x-forward (real in), y-forward, z-forward * response * z-inverse,
+// inverse FFT of FFT(in) * LoG(k).  Sizes the half-spectrum path of
+// log_fft.cu covers go there; the rest run full complex transforms of the
+// real volume here (equal to the reference's R2C/C2R pair for this real,
+// symmetric response).  x-forward (real in), y-forward, z-forward * response * z-inverse,
 // y-inverse, x-inverse (real part out).
 fbp_status launch_log_fft(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz,
                           float sigma, cudaStream_t stream) {
     const int lx = ilog2_exact(nx), ly = ilog2_exact(ny), lz = ilog2_exact(nz);
     if (lx < 1 || ly < 1 || lz < 1 || lx > 12 || ly > 12 || lz > 12)
         return set_error(FBP_ERR_UNSUPPORTED, "LoG-FFT filter: sizes must be powers of two in [2, 4096]");
+    if (log_fft_half_supported(nx, ny, nz)) return launch_log_fft_half(ctx, in, out, nx, ny, nz, sigma, stream);
     void* buf = nullptr;
     FBP_TRY(workspace(ctx, WS_FFT_A, (size_t)nx * ny * nz * sizeof(float2), stream, &buf));
     FftLineParams p{};

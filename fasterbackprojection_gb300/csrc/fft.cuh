@@ -71,6 +71,11 @@ struct LctFusedInputs {
     const float2* wiener;         // [2M][2N][2N]
     float* volume;                // [M][N][N]
 };
+// The LoG-FFT filter on the half spectrum (log_fft.cu): every axis a power of
+// two in [32, 1024].
+bool log_fft_half_supported(uint32_t nx, uint32_t ny, uint32_t nz);
+fbp_status launch_log_fft_half(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz,
+                               float sigma, cudaStream_t stream);
 bool lct_fused_supported(uint32_t N, uint32_t M);
 fbp_status lct_fused_run(fbp_context* ctx, const LctFusedInputs& in, cudaStream_t stream);
 

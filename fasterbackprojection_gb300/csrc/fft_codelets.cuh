@@ -113,4 +113,15 @@ __device__ __forceinline__ int pidx(int j) { return j + (j >> 4); }
 __host__ __device__ constexpr int line_stride(int n) { return n + (n >> 4) + 1; }
 
 
+// buildLoGKernel3D (transient_postprocessing.cuh:116-148) at full-grid index (x, y, z).
+__device__ __forceinline__ float log_response(int x, int y, int z, int nx, int ny, int nz, float sigma) {
+    const float fx = (x <= nx / 2) ? (float)x : (float)(x - nx);
+    const float fy = (y <= ny / 2) ? (float)y : (float)(y - ny);
+    const float fz = (z <= nz / 2) ? (float)z : (float)(z - nz);
+    const float fxn = fx / nx, fyn = fy / ny, fzn = fz / nz;
+    const float k2 = fxn * fxn + fyn * fyn + fzn * fzn;
+    const float pi = 3.14159265358979323846f;
+    return -4.0f * pi * pi * k2 * expf(-2.0f * pi * pi * sigma * sigma * k2);
+}
+
 }  // namespace fbp

@@ -99,3 +99,29 @@ def test_log_fft_filter(ctx, cuda, n):
     K = torch.from_numpy(_log_response_np(n, 1.0)[:, :, : n // 2 + 1].astype(np.float32)).to(cuda)
     ref = torch.fft.irfftn(F * K, s=v.shape, norm="forward").cpu().numpy()
     assert rel_l2(got, ref) < 1e-5
+
+
+def _log_response_xyz(nx, ny, nz, sigma):
+    def freqs(n):
+        f = np.arange(n, dtype=np.float32)
+        return np.where(f <= n // 2, f, f - n).astype(np.float32) / np.float32(n)
+    fz, fy, fx = np.meshgrid(freqs(nz), freqs(ny), freqs(nx), indexing="ij")
+    k2 = fx * fx + fy * fy + fz * fz
+    pi = np.float32(np.pi)
+    return (-4 * pi * pi * k2 * np.exp(-2 * pi * pi * sigma * sigma * k2)).astype(np.float64)
+
+
+@pytest.mark.parametrize("shape", [(64, 32, 128), (16, 16, 16), (32, 256, 64)])
+def test_log_fft_filter_non_cubic(ctx, cuda, shape):
+    """Non-cubic volumes (z, y, x): the half-spectrum path for axes in
+    [32, 1024], the full complex passes below that."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_FILTER_LOG_FFT
+
+    nz, ny, nx = shape
+    vol = np.random.default_rng(nx * ny + nz).random(shape).astype(np.float32)
+    got = ctx.postfilter(FBP_FILTER_LOG_FFT, torch.from_numpy(vol).to(cuda), 5, 1.5).cpu().numpy()
+    want = np.real(np.fft.ifftn(np.fft.fftn(vol.astype(np.float64)) * _log_response_xyz(nx, ny, nz, 1.5)))
+    want *= nx * ny * nz
+    assert rel_l2(got, want) < 1e-5
+
