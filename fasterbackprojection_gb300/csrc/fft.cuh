@@ -58,7 +58,7 @@ fbp_status fft_launch(fbp_context* ctx, const FftLineParams& p, int mode, int lo
 // Lines per CTA for a transform of length 2^log2n (shared memory budget).
 int fft_lines_per_cta(int log2n);
 
-// The three-pass LCT of lct_fused.cu (scan grids N x N with 8 <= N <= 64,
+// The LCT of lct_fused.cu (scan grids N x N with 8 <= N <= 1024,
 // 16 <= M <= 2048 bins; both powers of two).
 struct LctFusedInputs {
     const float* data;            // capture: [M][N][N] (time_major) or [N][N][M]

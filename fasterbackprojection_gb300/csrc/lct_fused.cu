@@ -1,5 +1,6 @@
 // Confocal LCT in three passes for scan grids up to 64 x 64 (padded planes
-// of at most 128 x 128 complex values fit one CTA's shared memory).
+// of at most 128 x 128 complex values fit one CTA's shared memory), five for
+// larger grids (the plane pass split into row and column passes).
 //
 // The LCT of lct.cu (python/lct.py:97-211) pads the resampled capture to
 // (2M, 2N, 2N), takes a 3-D FFT, multiplies by the PSF's Wiener filter and
@@ -43,6 +44,7 @@ struct LctFusedParams {
     const float2* tw_x;
     const float2* wiener;         // [2M][2N][2N]
     float2* buf;                  // [2M][N][N]
+    float2* pad;                  // [2M][N][2N]: rows of the padded planes (N > 64 only)
     float* vol;                   // [M][N][N]
     float scale;                  // 1 / (2M * 2N * 2N)
 };
@@ -212,6 +214,132 @@ __global__ void __launch_bounds__(kZThreads, 2) lct_zinv_kernel(LctFusedParams p
     }
 }
 
+// Planes wider than one CTA's shared memory (N > 64): the (y, x) transform
+// as passes over rows y < N of the padded planes in global memory.
+//   lct_rows_kernel<.., false>: compact rows (x < N; the rest is zero padding,
+//     skipped by the first pass) -> forward 2N-point FFT -> pad[kz][y][.]
+//   lct_cols_kernel: columns of pad (rows y >= N are zero, skipped), forward
+//     FFT, times the Wiener filter, inverse FFT keeping rows y < N
+//   lct_rows_kernel<.., true>: inverse FFT of pad rows, x < N kept -> buf.
+constexpr int kRowThreads = 256;
+constexpr int row_lines(int log2x) { return (8192 >> log2x) < 32 ? (8192 >> log2x) : 32; }
+template <int LOG2X>
+constexpr size_t rows_smem() {
+    return ((size_t)row_lines(LOG2X) * line_stride(1 << LOG2X) + stage_table_size(LOG2X)) * sizeof(float2);
+}
+
+template <int LOG2X, bool INV>
+__global__ void __launch_bounds__(kRowThreads) lct_rows_kernel(LctFusedParams p) {
+    constexpr int X = 1 << LOG2X, N = X / 2, C = row_lines(LOG2X), LS = line_stride(X), TWN = stage_table_size(LOG2X);
+    constexpr int NIN = INV ? X : N, PL = (C * NIN + kRowThreads - 1) / kRowThreads;
+    extern __shared__ __align__(16) float2 sm[];
+    float2* lines = sm;
+    float2* tw = lines + C * LS;
+    for (int i = threadIdx.x; i < TWN; i += kRowThreads) tw[i] = p.tw_x[i];
+    const size_t kz = blockIdx.y;
+    const int y0 = blockIdx.x * C;
+    {
+        float2 v[PL];
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kRowThreads, i = e / NIN, x = e % NIN;
+            v[u] = make_float2(0.f, 0.f);
+            if (e < C * NIN && y0 + i < N)
+                v[u] = INV ? p.pad[(kz * N + y0 + i) * X + x] : p.buf[(kz * N + y0 + i) * N + x];
+        }
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kRowThreads;
+            if (e < C * NIN) lines[(e / NIN) * LS + pidx(e % NIN)] = v[u];
+        }
+    }
+    __syncthreads();
+    lean_fft<LOG2X, 0, C, kRowThreads, INV, false, !INV, INV>(lines, tw, LS);
+    constexpr int NOUT = INV ? N : X;
+    for (int e = threadIdx.x; e < C * NOUT; e += kRowThreads) {
+        const int i = e / NOUT, x = e % NOUT;
+        if (y0 + i >= N) continue;
+        const float2 c = lines[i * LS + pidx(x)];
+        if (INV) p.buf[(kz * N + y0 + i) * N + x] = c;
+        else p.pad[(kz * N + y0 + i) * X + x] = c;
+    }
+}
+
+template <int LOG2X>
+__global__ void __launch_bounds__(kRowThreads) lct_cols_kernel(LctFusedParams p) {
+    constexpr int X = 1 << LOG2X, N = X / 2, C = row_lines(LOG2X), LS = line_stride(X), TWN = stage_table_size(LOG2X);
+    constexpr int PL = (C * N + kRowThreads - 1) / kRowThreads;
+    extern __shared__ __align__(16) float2 sm[];
+    float2* lines = sm;
+    float2* tw = lines + C * LS;
+    for (int i = threadIdx.x; i < TWN; i += kRowThreads) tw[i] = p.tw_x[i];
+    const size_t kz = blockIdx.y;
+    const int x0 = blockIdx.x * C;
+    float2* plane = p.pad + kz * N * X;
+    {
+        float2 v[PL];
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kRowThreads, i = e % C, y = e / C;
+            v[u] = e < C * N ? plane[(size_t)y * X + x0 + i] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < PL; ++u) {
+            const int e = threadIdx.x + u * kRowThreads;
+            if (e < C * N) lines[(e % C) * LS + pidx(e / C)] = v[u];
+        }
+    }
+    __syncthreads();
+    lean_fft<LOG2X, 0, C, kRowThreads, false, false, true, false>(lines, tw, LS);  // rows y >= N are zero
+    {
+        const float2* w = p.wiener + kz * X * X;
+        constexpr int PW = (C * X + kRowThreads - 1) / kRowThreads, RW = PW < 16 ? PW : 16;
+#pragma unroll
+        for (int c = 0; c < PW; c += RW) {
+            float2 t[RW];
+#pragma unroll
+            for (int u = 0; u < RW; ++u) {
+                const int e = threadIdx.x + (c + u) * kRowThreads;
+                t[u] = e < C * X ? w[(size_t)(e / C) * X + x0 + e % C] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < RW; ++u) {
+                const int e = threadIdx.x + (c + u) * kRowThreads;
+                if (e < C * X) {
+                    const int a = (e % C) * LS + pidx(e / C);
+                    lines[a] = cmul(lines[a], t[u]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    lean_fft<LOG2X, 0, C, kRowThreads, true, false, false, true>(lines, tw, LS);  // rows y < N kept
+    for (int e = threadIdx.x; e < C * N; e += kRowThreads) {
+        const int i = e % C, y = e / C;
+        plane[(size_t)y * X + x0 + i] = lines[i * LS + pidx(y)];
+    }
+}
+
+template <int LOG2X>
+fbp_status launch_rows_cols(fbp_context* ctx, const LctFusedParams& p, unsigned planes, cudaStream_t s) {
+    constexpr int X = 1 << LOG2X, N = X / 2, C = row_lines(LOG2X);
+    constexpr size_t smem = rows_smem<LOG2X>();
+    static_assert(smem <= 200 * 1024, "row tile too large");
+    auto kf = lct_rows_kernel<LOG2X, false>;
+    auto kc = lct_cols_kernel<LOG2X>;
+    auto ki = lct_rows_kernel<LOG2X, true>;
+    FBP_TRY_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FBP_TRY_CUDA(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FBP_TRY_CUDA(cudaFuncSetAttribute(ki, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kf<<<dim3(cdiv(N, C), planes), kRowThreads, smem, s>>>(p);
+    FBP_CHECK_LAUNCH(ctx, "lct_rows_kernel");
+    kc<<<dim3(X / C, planes), kRowThreads, smem, s>>>(p);
+    FBP_CHECK_LAUNCH(ctx, "lct_cols_kernel");
+    ki<<<dim3(cdiv(N, C), planes), kRowThreads, smem, s>>>(p);
+    FBP_CHECK_LAUNCH(ctx, "lct_rows_kernel");
+    return FBP_OK;
+}
+
 template <int LOG2Z>
 fbp_status launch_z(fbp_context* ctx, const LctFusedParams& p, bool forward, cudaStream_t s) {
     constexpr int C = z_lines(LOG2Z);
@@ -264,7 +392,11 @@ fbp_status dispatch_plane(fbp_context* ctx, int log2x, const LctFusedParams& p, 
         case 5: return launch_plane<5>(ctx, p, planes, s);
         case 6: return launch_plane<6>(ctx, p, planes, s);
         case 7: return launch_plane<7>(ctx, p, planes, s);
-        default: return set_error(FBP_ERR_UNSUPPORTED, "fbp_lct: fused path needs 8 <= N <= 64");
+        case 8: return launch_rows_cols<8>(ctx, p, planes, s);
+        case 9: return launch_rows_cols<9>(ctx, p, planes, s);
+        case 10: return launch_rows_cols<10>(ctx, p, planes, s);
+        case 11: return launch_rows_cols<11>(ctx, p, planes, s);
+        default: return set_error(FBP_ERR_UNSUPPORTED, "fbp_lct: fused path needs 8 <= N <= 1024");
     }
 }
 
@@ -294,7 +426,7 @@ fbp_status stage_twiddles(fbp_context* ctx, int log2n, cudaStream_t s, const flo
     return FBP_OK;
 }
 
-bool lct_fused_supported(uint32_t N, uint32_t M) { return N >= 8 && N <= 64 && M >= 16 && M <= 2048; }
+bool lct_fused_supported(uint32_t N, uint32_t M) { return N >= 8 && N <= 1024 && M >= 16 && M <= 2048; }
 
 fbp_status lct_fused_run(fbp_context* ctx, const LctFusedInputs& in, cudaStream_t s) {
     const int log2x = in.log2n + 1, log2z = in.log2m + 1;
@@ -320,6 +452,11 @@ fbp_status lct_fused_run(fbp_context* ctx, const LctFusedInputs& in, cudaStream_
     void* b = nullptr;
     FBP_TRY(workspace(ctx, WS_FFT_A, (size_t)2 * M * N * N * sizeof(float2), s, &b));
     p.buf = static_cast<float2*>(b);
+    if (N > 64) {
+        void* pd = nullptr;
+        FBP_TRY(workspace(ctx, WS_FFT_C, (size_t)2 * M * N * (2 * N) * sizeof(float2), s, &pd));
+        p.pad = static_cast<float2*>(pd);
+    }
     FBP_TRY(dispatch_z(ctx, log2z, p, true, s));
     FBP_TRY(dispatch_plane(ctx, log2x, p, 2 * M, s));
     FBP_TRY(dispatch_z(ctx, log2z, p, false, s));

@@ -51,10 +51,11 @@ def test_lct_config1_size_vs_fp64(ctx, cuda, grid):
     assert rel_l2(got, want) < 1e-4
 
 
-@pytest.mark.parametrize("n,m", [(4, 8), (128, 32), (8, 2048), (16, 1024), (64, 16)])
+@pytest.mark.parametrize("n,m", [(4, 8), (128, 32), (256, 16), (8, 2048), (16, 1024), (64, 16)])
 def test_lct_sizes_vs_fp64(ctx, cuda, n, m):
-    """Scan grids and bin counts on both sides of the three-pass path's range
-    (8 <= N <= 64, 16 <= M <= 2048) against the FP64 restatement."""
+    """Scan grids and bin counts across the LCT paths (plane pass for
+    8 <= N <= 64, row and column passes above, the line pipeline outside
+    16 <= M <= 2048 or below N = 8) against the FP64 restatement."""
     import torch
     from fasterbackprojection_gb300 import scenes
 
