@@ -947,7 +947,9 @@ def learned_mis_leg(ctx, dev, info, cube, lx, n_train=2000, ks=(4, 8, 16, 32, 64
 
 
 def cpu_baseline(info, cube, lx):
-    rate, desc, dt = cpu_sample_rate(info, cube.cpu().numpy(), lx.cpu().numpy(), target_s=12.0)
+    # All host threads, whatever OMP_NUM_THREADS a launcher set (torchrun sets 1).
+    rate, desc, dt = cpu_sample_rate(info, cube.cpu().numpy(), lx.cpu().numpy(), target_s=12.0,
+                                     threads=os.cpu_count() or 1)
     return {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
             "sample": desc + f" ({dt:.1f} s)"}
 
@@ -978,7 +980,7 @@ def run_reference(args):
     rates = []
     desc = ""
     for k in range(args.warmup + args.steps):
-        r, desc, dt = cpu_sample_rate(info, cube, lx, target_s=4.0)
+        r, desc, dt = cpu_sample_rate(info, cube, lx, target_s=4.0, threads=os.cpu_count() or 1)
         if k >= args.warmup:
             rates.append(r)
     value = statistics.mean(rates)
