@@ -297,7 +297,9 @@ def run_ours(args):
                "matches_device_path": bool(torch.equal(host_vol.to(dev), vol2))}
 
     extras = {}
-    if not args.no_extras and rank == 0:
+    # The extra legs and the CPU baseline run with one GPU only: at N > 1 the
+    # line is the scaling measurement alone, so the other GPUs are not held.
+    if not args.no_extras and rank == 0 and ws == 1:
         # BF16 storage of the same capture.
         cube16 = cube.to(torch.bfloat16)
         for _ in range(2):
@@ -345,7 +347,7 @@ def run_ours(args):
         "bp_ms_per_launch": bp_ms,
         "gpu_launches": launches,
     }
-    if not args.no_extras and rank == 0:
+    if not args.no_extras and rank == 0 and ws == 1:
         line["cpu_baseline"] = cpu_baseline(info, cube, lx)
         line.update(extras)
     line["clocks"] = clk.summary()
