@@ -364,6 +364,51 @@ void Laser::reconstructAABBConfocalMIS(float* volume, const ReconstructionInfo& 
     throw std::runtime_error("Laser::reconstructAABBConfocalMIS: use fbp_mis_backproject");
 }
 
+// ---------------------------------------------------------- TransientImage
+
+TransientImage::TransientImage(uint16_t width, uint16_t height) : _width(width), _height(height) {}
+
+void TransientImage::save(const std::string& filename, const fbpref::uvec4* slice) {
+    if (!slice) throw std::runtime_error("TransientImage::save: null slice");
+    const size_t w = _width, h = _height;
+    std::vector<uint8_t> rgba(w * h * 4);
+    for (size_t y = 0; y < h; ++y)  // row y of the file is row h - 1 - y of the slice
+        for (size_t x = 0; x < w; ++x) {
+            const fbpref::uvec4& p = slice[(h - 1 - y) * w + x];
+            uint8_t* o = &rgba[(y * w + x) * 4];
+            o[0] = (uint8_t)std::min<uint32_t>(p.x, 255u);
+            o[1] = (uint8_t)std::min<uint32_t>(p.y, 255u);
+            o[2] = (uint8_t)std::min<uint32_t>(p.z, 255u);
+            o[3] = 255;
+        }
+    check(fbp_write_png(filename.c_str(), rgba.data(), _width, _height), "TransientImage::save");
+}
+
+void TransientImage::save(const std::string& filename, float* slice, const fbpref::uvec2& size, uint32_t stride,
+                          uint32_t offset, bool normalize) {
+    if (!slice) throw std::runtime_error("TransientImage::save: null slice");
+    const size_t n = (size_t)_width * _height;
+    std::vector<float> plane(n);
+    for (size_t i = 0; i < n; ++i) plane[i] = slice[offset + i * (size_t)stride];
+    float* d = device_upload(plane.data(), n);
+    uint8_t* img = nullptr;
+    const size_t bytes = (size_t)size.x * size.y * 4;
+    cudaError_t e = cudaMalloc(&img, std::max<size_t>(bytes, 1));
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        check_cuda(e, "cudaMalloc");
+    }
+    fbp_status st = fbp_transient_images(fbp_default_context(), d, _width, _height, 1, 1, n, size.x, size.y,
+                                         normalize ? 1 : 0, img, nullptr);
+    std::vector<uint8_t> host(bytes);
+    if (st == FBP_OK) e = cudaMemcpy(host.data(), img, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(img);
+    cudaFree(d);
+    check(st, "TransientImage::save");
+    check_cuda(e, "D2H");
+    check(fbp_write_png(filename.c_str(), host.data(), size.x, size.y), "TransientImage::save");
+}
+
 // --------------------------------------------------------------------- LCT
 
 LCT::LCT(ReconstructionInfo recInfo) : _info(recInfo) {}

@@ -7,10 +7,11 @@
 //   ReconstructionInfo / ReconstructionBuffers   GpuStructs.cuh:8-45
 //   Laser                 FasterBackprojection/Laser.cuh:14-48
 //   LCT                   FasterBackprojection/LCT.h:5-13 (constructor public here)
+//   TransientImage        FasterBackprojection/TransientImage.h:7-18
 //   PostprocessingFilters, None, Laplacian, LoG, LoGFFT   PostprocessingFilters.h:5-39
 // Errors surface as std::runtime_error, like the reference's
 // CudaHelper::checkError (CudaHelper.cpp:66-70).  glm is not a dependency:
-// the small vec2/vec3/uvec3 structs below have the same layout.
+// the small vec2/vec3/uvec2/uvec3/uvec4 structs below have the same layout.
 #pragma once
 
 #include <cstdint>
@@ -32,6 +33,15 @@ struct uvec3 {
     uvec3() = default;
     uvec3(uint32_t s) : x(s), y(s), z(s) {}
     uvec3(uint32_t a, uint32_t b, uint32_t c) : x(a), y(b), z(c) {}
+};
+struct uvec2 {
+    uint32_t x = 0, y = 0;
+    uvec2() = default;
+    explicit uvec2(uint32_t s) : x(s), y(s) {}
+    uvec2(uint32_t a, uint32_t b) : x(a), y(b) {}
+};
+struct uvec4 {
+    uint32_t x = 0, y = 0, z = 0, w = 0;
 };
 }  // namespace fbpref
 
@@ -110,6 +120,29 @@ public:
     // when missing.  Unlike the reference, _data itself is left unchanged
     // (its normalizeImage divides the host slice in place).
     void saveImages(const std::string& outPath);
+};
+
+// TransientImage.h:7-18: an RGBA8 image of width x height; save() writes it
+// as a PNG file.
+class TransientImage {
+public:
+    TransientImage(uint16_t width, uint16_t height);
+    virtual ~TransientImage() = default;
+    // TransientImage.cpp:31-44: channels x, y, z clamped to 255, alpha 255,
+    // rows flipped.  slice: width * height host values.
+    void save(const std::string& filename, const fbpref::uvec4* slice);
+    // TransientImage.cpp:46-64: grey pixels clamp(uint(v * 255), 0, 255) of
+    // slice[offset + idx * stride] (host memory), rows flipped, bilinearly
+    // resized to `size` when it differs (made on the GPU by
+    // fbp_transient_images).  normalize divides by the plane's maximum first;
+    // unlike the reference, `slice` itself is not modified.
+    void save(const std::string& filename, float* slice, const fbpref::uvec2& size, uint32_t stride, uint32_t offset,
+              bool normalize = false);
+    uint16_t getWidth() const { return _width; }
+    uint16_t getHeight() const { return _height; }
+
+private:
+    uint16_t _width, _height;
 };
 
 // PostprocessingFilters.h:5-39.  compute() replaces `input` with a new device

@@ -36,6 +36,20 @@ int main(int argc, char** argv) {
             std::printf("ok %zu\n", laser.lastVolume().size());
             return 0;
         }
+        if (mode == "timage") {
+            // A 7 x 5 float slice (stride 3, offset 1) enlarged to 13 x 9, and a
+            // 4 x 3 uvec4 slice.
+            std::vector<float> f(1 + 3 * 35);
+            for (size_t i = 0; i < f.size(); ++i) f[i] = (float)((i * 37) % 101) / 97.0f;
+            TransientImage a(7, 5);
+            a.save(std::string(argv[2]) + "/float.png", f.data(), fbpref::uvec2(13, 9), 3, 1, false);
+            std::vector<fbpref::uvec4> u(12);
+            for (size_t i = 0; i < u.size(); ++i) u[i] = {(uint32_t)(i * 40), (uint32_t)(300 - i), (uint32_t)i, 7};
+            TransientImage b(4, 3);
+            b.save(std::string(argv[2]) + "/uvec4.png", u.data());
+            std::printf("ok\n");
+            return 0;
+        }
         if (mode == "images") {
             NLosData d(argv[2]);
             d.saveImages(std::string(argv[3]) + "/");

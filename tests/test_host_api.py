@@ -158,3 +158,21 @@ def test_lct_class_matches_c_abi(driver, ctx, cuda, tmp_path):
     want = ctx.lct(torch.from_numpy(cap.cube.reshape(16, 16, 128)).to(cuda), 1.0, cap.time_step,
                    layout=FBP_LAYOUT_TIME_INNER).cpu().numpy()
     assert rel_l2(vol, want) < 1e-6
+
+
+@pytest.mark.gpu
+def test_transient_image_class_matches_the_reference_conversion(driver, ctx, tmp_path):
+    """TransientImage::save, both overloads (TransientImage.cpp:31-64)."""
+    from oracle import numpy_ref
+    from tests.test_images_cpu import _decode_png
+
+    out = subprocess.run([str(driver), "timage", str(tmp_path)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    f = np.array([((i * 37) % 101) / np.float32(97.0) for i in range(1 + 3 * 35)], np.float32)
+    np.testing.assert_array_equal(_decode_png((tmp_path / "float.png").read_bytes()),
+                                  numpy_ref.transient_image(f, 7, 5, (13, 9), stride=3, offset=1))
+    u = np.array([(i * 40, 300 - i, i, 7) for i in range(12)], np.uint32).reshape(3, 4, 4)
+    want = np.minimum(u, 255).astype(np.uint8)[::-1].copy()
+    want[..., 3] = 255
+    np.testing.assert_array_equal(_decode_png((tmp_path / "uvec4.png").read_bytes()), want)
+
