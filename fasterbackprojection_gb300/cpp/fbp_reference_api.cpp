@@ -359,9 +359,23 @@ void Laser::reconstructShape(const TransientParameters& tp) {
 }
 
 void Laser::reconstructAABBConfocalMIS(float* volume, const ReconstructionInfo& recInfo) const {
-    (void)volume;
-    (void)recInfo;
-    throw std::runtime_error("Laser::reconstructAABBConfocalMIS: use fbp_mis_backproject");
+    // Laser.cu:526-611: the reference's one-sample MIS over L/4 samples per
+    // voxel with its default noise buffer, on this capture's data (the
+    // reference reads the buffers its last toGpu left in __constant__ memory).
+    if (!volume) throw std::runtime_error("Laser::reconstructAABBConfocalMIS: null volume");
+    if (!_nlosData->_isConfocal) throw std::runtime_error("Laser::reconstructAABBConfocalMIS: confocal captures only");
+    float* cube = device_upload(_nlosData->_data.data(), _nlosData->_data.size());
+    fbpref::vec3* lx = device_upload(_nlosData->_laserGridPositions.data(), _nlosData->_laserGridPositions.size());
+    fbp_mis_params prm{};
+    prm.proposal = FBP_MIS_REFERENCE;
+    prm.samples = 0;  // L / 4 (Laser.cu:590)
+    const fbp_status st = fbp_mis_backproject(fbp_default_context(), &recInfo, cube, FBP_F32, FBP_LAYOUT_TIME_INNER,
+                                              reinterpret_cast<const float*>(lx), &prm, volume, nullptr);
+    const cudaError_t e = cudaDeviceSynchronize();
+    cudaFree(lx);
+    cudaFree(cube);
+    check(st, "Laser::reconstructAABBConfocalMIS");
+    check_cuda(e, "Laser::reconstructAABBConfocalMIS");
 }
 
 // ---------------------------------------------------------- TransientImage

@@ -182,8 +182,10 @@ public:
     // "<outputFolder>depths.raw" (depth mode: float32 [L][D]) plus the depth
     // planes as "<outputFolder>transient_<d>.png" (Laser.cu:409-424, 461-476).
     void reconstructShape(const TransientParameters& transientParams);
-    // Laser.cu:526-611 with the unbiased estimator (see fbp.h); `volume` is a
-    // device buffer of Vx*Vy*Vz floats.
+    // Laser.cu:526-611: the reference's one-sample MIS (L/4 samples per voxel,
+    // default noise buffer; samples summed in order, FBP_MIS_REFERENCE of
+    // fbp_mis_backproject) on this capture; `volume` is a device buffer of
+    // Vx*Vy*Vz floats.
     void reconstructAABBConfocalMIS(float* volume, const ReconstructionInfo& recInfo) const;
 
     // The last reconstruction (host copy).

@@ -8,6 +8,8 @@
 #include <fstream>
 #include <string>
 
+#include <cuda_runtime.h>
+
 #include "fbp_reference_api.hpp"
 
 int main(int argc, char** argv) {
@@ -34,6 +36,28 @@ int main(int argc, char** argv) {
             Laser laser(&d);
             laser.reconstructShape(p);
             std::printf("ok %zu\n", laser.lastVolume().size());
+            return 0;
+        }
+        if (mode == "mis") {
+            NLosData d(argv[2]);
+            TransientParameters p;
+            p._voxelResolution = fbpref::uvec3(8);
+            ReconstructionInfo info;
+            ReconstructionBuffers buf;
+            d.toGpu(info, buf, p);
+            cudaFree(buf._intensity);
+            cudaFree(buf._laserTargets);
+            cudaFree(buf._sensorTargets);
+            float* vol = nullptr;
+            if (cudaMalloc(&vol, 512 * sizeof(float)) != cudaSuccess) return 5;
+            Laser laser(&d);
+            laser.reconstructAABBConfocalMIS(vol, info);
+            std::vector<float> h(512);
+            cudaMemcpy(h.data(), vol, h.size() * sizeof(float), cudaMemcpyDeviceToHost);
+            cudaFree(vol);
+            std::ofstream f(argv[3], std::ios::binary);
+            f.write(reinterpret_cast<const char*>(h.data()), h.size() * sizeof(float));
+            std::printf("ok\n");
             return 0;
         }
         if (mode == "timage") {

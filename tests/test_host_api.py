@@ -176,3 +176,25 @@ def test_transient_image_class_matches_the_reference_conversion(driver, ctx, tmp
     want[..., 3] = 255
     np.testing.assert_array_equal(_decode_png((tmp_path / "uvec4.png").read_bytes()), want)
 
+
+@pytest.mark.gpu
+def test_laser_mis_entry_point_runs_the_reference_mode(driver, ctx, cuda, tmp_path):
+    """Laser::reconstructAABBConfocalMIS (Laser.cu:526-611) = FBP_MIS_REFERENCE
+    with L/4 samples and the default noise buffer, on the capture's data."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE, make_info, nlos_io
+
+    cap, c = _capture()
+    nlos_io.write_nlos(tmp_path / "cap.nlos", c)
+    out = subprocess.run([str(driver), "mis", str(tmp_path / "cap.nlos"), str(tmp_path / "mis.raw")],
+                         capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    got = np.fromfile(tmp_path / "mis.raw", dtype=np.float32).reshape(8, 8, 8)
+    info = make_info(num_laser_targets=64, num_time_bins=256, time_step=cap.time_step, voxel_res=(8, 8, 8),
+                     hidden_min=(-1.0, -2.0, -1.0), voxel_size=(0.25, 0.25, 0.25), discard_first_last_bounces=0,
+                     laser_position=(0.1, -0.2, 0.0), sensor_position=(0.0, -0.2, 0.1))
+    want = ctx.mis_backproject(info, torch.from_numpy(cap.cube).to(cuda), torch.from_numpy(cap.laser_xyz).to(cuda),
+                               FBP_MIS_REFERENCE, 0).cpu().numpy()
+    assert float(np.abs(want).max()) > 0
+    np.testing.assert_array_equal(got, want)
+
