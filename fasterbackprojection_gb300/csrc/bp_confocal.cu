@@ -224,8 +224,21 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(z_end - z_begin, 4 * kWZ));
     const bool bounce = in.discard_first_last_bounces == 0;
     if (scatter) {
-        if (bounce) return go_confocal<S, PATH_SCATTER, true, false, true>(ctx, p, grid, wp.smem, stream);
-        return go_confocal<S, PATH_SCATTER, false, false, true>(ctx, p, grid, wp.smem, stream);
+        // Steps per (voxel, scan point): at most ceil(diagonal / (dt + EPS)),
+        // one more where rounding lands on the end; the kernel unrolls 2..4
+        // of them and loops over the rest.
+        const double steps = std::ceil(vdiag / ((double)in.time_step + (double)FBP_EPS));
+        const int sp = (int)std::min(std::max(steps, 2.0), (double)kScatterMaxPrefix);
+        if (sp == 2) {
+            if (bounce) return go_confocal<S, PATH_SCATTER, true, false, true>(ctx, p, grid, wp.smem, stream);
+            return go_confocal<S, PATH_SCATTER, false, false, true>(ctx, p, grid, wp.smem, stream);
+        }
+        if (sp == 3) {
+            if (bounce) return go_confocal<S, PATH_SCATTER + 1, true, false, true>(ctx, p, grid, wp.smem, stream);
+            return go_confocal<S, PATH_SCATTER + 1, false, false, true>(ctx, p, grid, wp.smem, stream);
+        }
+        if (bounce) return go_confocal<S, PATH_SCATTER + 2, true, false, true>(ctx, p, grid, wp.smem, stream);
+        return go_confocal<S, PATH_SCATTER + 2, false, false, true>(ctx, p, grid, wp.smem, stream);
     }
     if (smp) return dispatch_confocal<S, true>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
     return dispatch_confocal<S, false>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);

@@ -15,11 +15,17 @@ namespace fbp {
 // In PATH_2D / PATH_FAST the bin is floor(x) - a via a round-toward-zero add of
 // 2^23 - a; without CLAMP the window planner guarantees every bin of the tile
 // lies inside its window, so the -2^23 bias folds into the shared-memory base.
-//   PATH_SCATTER the reference's ACCUMULATE_VOXEL_SCATTERING variant
+//   PATH_SCATTER + j  the reference's ACCUMULATE_VOXEL_SCATTERING variant
 //               (transient_reconstruction.cuh:112-126): every bin of the
 //               path range dist -/+ the voxel's half diagonal, stepped by
-//               (dt + EPS) in float like the reference, bins by conversion.
+//               (dt + EPS) in float like the reference.  The first 2 + j
+//               steps run unrolled and predicated (the voxels' walks
+//               interleave), any further ones in a loop; bins by the same
+//               round-toward-zero add (the path is never negative).
 enum { PATH_2D = 0, PATH_FAST = 1, PATH_EXACT = 2, PATH_SCATTER = 3 };
+constexpr int kScatterMaxPrefix = 4;
+__host__ __device__ constexpr bool is_scatter(int path) { return path >= PATH_SCATTER; }
+__host__ __device__ constexpr int scatter_prefix(int path) { return path - PATH_SCATTER + 2; }
 
 template <typename S>
 __device__ __forceinline__ float lds_elem(uint32_t addr);
@@ -56,41 +62,104 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
                                                float (&acc)[KV], float ext = 0.f, float step = 0.f) {
     constexpr int SH = ElemShift<S>::value;
     const float rcp2 = 2.f * rcp_dt;  // exact
-    if constexpr (PATH == PATH_SCATTER) {
-        const int max_it = (int)(2.f * ext / step) + 4;
+    if constexpr (is_scatter(PATH)) {
+        constexpr int SP = scatter_prefix(PATH);
+        static_assert(SP >= 1 && SP <= kScatterMaxPrefix, "prefix within the step bound");
+        const int max_it = (int)(2.f * ext / step) + 4;  // >= 4 >= SP
+        // The reference adds I * w per bin with an atomic: one rounding for
+        // the product, one for the sum, in bin order.  The count bound only
+        // matters where dist is so large that adding the step no longer
+        // changes it (no such path reaches a bin).  Once dd >= dmax it stays
+        // there, so a predicated step past the end only reads (the clamped
+        // index keeps it inside the slot).
         for (int i = 0; i < nl; ++i) {
             const float4 g = geo[i];
-            const int2 m = meta[i];  // (window start bin a, slot shared address)
+            const int2 m = meta[i];  // (float 2^23 - a for window start bin a, slot shared address)
+            const float bias = __int_as_float(m.x);
             const float wl = WEIGHTED ? wts[i] : 1.f;
             const float dy = sub_rn(py, g.y), dz = sub_rn(pz, g.z);
             const float dy2 = mul_rn(dy, dy);
-#pragma unroll
-            for (int k = 0; k < KV; ++k) {
-                const float dx = sub_rn(px[k], g.x);
-                const float d = sqrt_approx(fma_rn(dz, dz, fma_rn(dx, dx, dy2)));
-                float dist = fma_rn(d, 2.f, neg_t0);
-                if (BOUNCE) dist = add_rn(dist, g.w);
-                const float w = SAFE ? ref_safe_rcp(mul_rn(dist, dist)) : rcp_approx(mul_rn(dist, dist));
-                float dd = fmaxf(0.f, sub_rn(dist, ext));
-                const float dmax = add_rn(dist, ext);
-                float a = acc[k];
-                // The reference adds I * w per bin with an atomic: one rounding
-                // for the product, one for the sum, in bin order.  The count
-                // bound only matters where dist is so large that adding the
-                // step no longer changes it (no such path reaches a bin).
-                for (int it = 0; dd < dmax && it < max_it; ++it) {
-                    const int b = __float2int_rz(ref_bin_ratio(dd, rcp_dt));
-                    float I = lds_elem<S>((uint32_t)m.y + (min((uint32_t)(b - m.x), slot_w) << SH));
+            auto bin_at = [&](float dd) -> uint32_t {
+                const uint32_t bits = __float_as_uint(add_rz(ref_bin_ratio(dd, rcp_dt), bias));
+                return (uint32_t)m.y + (min(bits - 0x4B000000u, slot_w) << SH);
+            };
+            // Steps SP.. of one walk (rare: a diagonal longer than the planned steps).
+            auto walk_rest = [&](float a, float dd, float dmax, float w) -> float {
+                for (int it = SP; dd < dmax && it < max_it; ++it) {
+                    float I = lds_elem<S>(bin_at(dd));
                     if (WEIGHTED) I *= wl;
                     a = add_rn(a, mul_rn(I, w));
                     dd = add_rn(dd, step);
                 }
-                acc[k] = a;
+                return a;
+            };
+            if constexpr (!SAFE && KV % 2 == 0) {
+                // Voxel pairs (k, k + 1) in packed FP32 pairs, step by step.
+                const f32x2_t gxp = pack2(g.x, g.x), dy2p = pack2(dy2, dy2), dzp = pack2(dz, dz);
+                const f32x2_t gwp = pack2(g.w, g.w), extp = pack2(ext, ext), stepp = pack2(step, step);
+                const f32x2_t rdp = pack2(rcp_dt, rcp_dt), biasp = pack2(bias, bias), wlp = pack2(wl, wl);
+#pragma unroll
+                for (int j = 0; j < KV / 2; ++j) {
+                    const f32x2_t dx = sub_rn2(pack2(px[2 * j], px[2 * j + 1]), gxp);
+                    float q0, q1, s0, s1, e0, e1, h0, h1;
+                    unpack2(fma_rn2(dzp, dzp, fma_rn2(dx, dx, dy2p)), q0, q1);
+                    f32x2_t dist = fma_rn2(pack2(sqrt_approx(q0), sqrt_approx(q1)), pack2(2.f, 2.f),
+                                           pack2(neg_t0, neg_t0));
+                    if (BOUNCE) dist = add_rn2(dist, gwp);
+                    unpack2(mul_rn2(dist, dist), s0, s1);
+                    const f32x2_t w = pack2(rcp_approx(s0), rcp_approx(s1));
+                    unpack2(sub_rn2(dist, extp), e0, e1);
+                    unpack2(add_rn2(dist, extp), h0, h1);  // dmax
+                    f32x2_t dd = pack2(fmaxf(0.f, e0), fmaxf(0.f, e1));
+                    float a0 = acc[2 * j], a1 = acc[2 * j + 1];
+#pragma unroll
+                    for (int it = 0; it < SP; ++it) {
+                        float d0, d1, b0, b1, t0, t1;
+                        unpack2(dd, d0, d1);
+                        unpack2(add_rz2(mul_rn2(dd, rdp), biasp), b0, b1);
+                        const uint32_t i0 = min(__float_as_uint(b0) - 0x4B000000u, slot_w);
+                        const uint32_t i1 = min(__float_as_uint(b1) - 0x4B000000u, slot_w);
+                        f32x2_t I = pack2(lds_elem<S>((uint32_t)m.y + (i0 << SH)),
+                                          lds_elem<S>((uint32_t)m.y + (i1 << SH)));
+                        if (WEIGHTED) I = mul_rn2(I, wlp);
+                        unpack2(add_rn2(pack2(a0, a1), mul_rn2(I, w)), t0, t1);
+                        a0 = d0 < h0 ? t0 : a0;
+                        a1 = d1 < h1 ? t1 : a1;
+                        dd = add_rn2(dd, stepp);
+                    }
+                    float d0, d1, w0, w1;
+                    unpack2(dd, d0, d1);
+                    unpack2(w, w0, w1);
+                    acc[2 * j] = walk_rest(a0, d0, h0, w0);
+                    acc[2 * j + 1] = walk_rest(a1, d1, h1, w1);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < KV; ++k) {
+                    const float dx = sub_rn(px[k], g.x);
+                    const float d = sqrt_approx(fma_rn(dz, dz, fma_rn(dx, dx, dy2)));
+                    float dist = fma_rn(d, 2.f, neg_t0);
+                    if (BOUNCE) dist = add_rn(dist, g.w);
+                    const float w = SAFE ? ref_safe_rcp(mul_rn(dist, dist)) : rcp_approx(mul_rn(dist, dist));
+                    float dd = fmaxf(0.f, sub_rn(dist, ext));
+                    const float dmax = add_rn(dist, ext);
+                    float a = acc[k];
+#pragma unroll
+                    for (int it = 0; it < SP; ++it) {
+                        const bool on = dd < dmax;
+                        float I = lds_elem<S>(bin_at(dd));
+                        if (WEIGHTED) I *= wl;
+                        const float t = add_rn(a, mul_rn(I, w));
+                        a = on ? t : a;
+                        dd = add_rn(dd, step);
+                    }
+                    acc[k] = walk_rest(a, dd, dmax, w);
+                }
             }
         }
         return;
     }
-    if constexpr (PATH != PATH_SCATTER && !SAFE && KV % 2 == 0) {
+    if constexpr (!is_scatter(PATH) && !SAFE && KV % 2 == 0) {
         // Voxel pairs (k, k + 1) in packed FP32 pairs: the same operations
         // as the scalar loop below, half the FP32 instructions.
         f32x2_t pxp[KV / 2], accp[KV / 2];
@@ -249,8 +318,8 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
     const float neg_t0 = -p.t0;
     // PATH_SCATTER: length(voxelSize) / 2 and the step timeStep + EPS, in the
     // reference's FP32 arithmetic (transient_reconstruction.cuh:113-125).
-    const float scat_ext = PATH == PATH_SCATTER ? mul_rn(0.5f, sqrt_approx(ref_dot3(p.vs[0], p.vs[1], p.vs[2]))) : 0.f;
-    const float scat_step = PATH == PATH_SCATTER ? add_rn(p.dt, FBP_EPS) : 0.f;
+    const float scat_ext = is_scatter(PATH) ? mul_rn(0.5f, sqrt_approx(ref_dot3(p.vs[0], p.vs[1], p.vs[2]))) : 0.f;
+    const float scat_step = is_scatter(PATH) ? add_rn(p.dt, FBP_EPS) : 0.f;
 
     // Sentinels of every slot and the whole zero slot.
     for (int i = tid; i < 2 * CH * ALIGN; i += NT) {
@@ -362,7 +431,7 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                 const float dmax = sqrtf(fx * fx + fy * fy + fz * fz);
                 const float bnc = BOUNCE ? g.w : 0.f;
                 float pmin = 2.f * dmin + neg_t0 + bnc, pmax = 2.f * dmax + neg_t0 + bnc;
-                if (PATH == PATH_SCATTER) {  // the bins of dist -/+ ext, stepped past dist + ext
+                if (is_scatter(PATH)) {  // the bins of dist -/+ ext, stepped past dist + ext
                     pmin = fmaxf(0.f, pmin - 1.01f * scat_ext);
                     pmax = pmax + 1.01f * scat_ext + scat_step;
                 }
@@ -397,7 +466,7 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
             const uint32_t slot_elem = skip ? zero_slot : (uint32_t)(buf * CH + tid) * slot_stride;
             uint32_t saddr = sbase + (uint32_t)slots_off + (slot_elem << SH);
             int bias;
-            if (PATH == PATH_EXACT || PATH == PATH_SCATTER) {
+            if (PATH == PATH_EXACT) {
                 bias = a;
             } else {
                 bias = __float_as_int((float)(8388608 - a));
@@ -406,7 +475,7 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
             if (item >= nitems || l >= p.L) {
                 // Beyond the last scan point: x + 0 < 2^23 lands on the sentinel
                 // (CLAMP) or, unclamped, reads the zero slot at index 0.
-                bias = (PATH == PATH_EXACT || PATH == PATH_SCATTER) ? 0x40000000 : 0;
+                bias = PATH == PATH_EXACT ? 0x40000000 : 0;
                 saddr = sbase + (uint32_t)slots_off + (zero_slot << SH);
                 if (!CLAMP && PATH != PATH_EXACT) saddr -= (__float_as_uint(0.f) << SH);
                 g = make_float4(3.0e18f, 3.0e18f, 3.0e18f, 0.f);  // far away: x is huge

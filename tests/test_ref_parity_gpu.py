@@ -193,22 +193,29 @@ def test_normalize_bitwise(ctx, harness, cuda):
     assert torch.equal(ref, got)
 
 
-@pytest.mark.parametrize("mode", ["plain", "bounces", "t0"])
+@pytest.mark.parametrize("mode", ["plain", "bounces", "t0", "fine", "mid"])
 def test_voxel_scattering_single_scan_bitwise(ctx, harness, cuda, mode):
     """The ACCUMULATE_VOXEL_SCATTERING build: with one scan point each voxel's
     bins are added by one reference thread in bin order, so the volume must
-    match bit for bit (ext, step and every visited bin included)."""
+    match bit for bit (ext, step and every visited bin included).  "fine" and
+    "mid" set the voxel diagonal to 0.35-1.0 and 2.1-2.9 time steps (two and
+    three steps per pair); the random geometries of the other modes take
+    3 to 30 steps."""
     import torch
 
     if not harness.scatter_available():
         pytest.skip("voxel-scattering build of the reference kernels not present")
-    rng = np.random.default_rng({"plain": 11, "bounces": 12, "t0": 13}[mode])
+    rng = np.random.default_rng({"plain": 11, "bounces": 12, "t0": 13, "fine": 14, "mid": 15}[mode])
     T = 2048
     cube = torch.from_numpy((2.0 ** (np.arange(T) % 3)).astype(np.float32)).to(cuda)
     mismatch = total = 0
     for trial in range(8):
         info = _rand_geometry(rng, 32, T, 0 if mode == "bounces" else 1, 0.6 if mode == "t0" else 0.0,
                               res=(32, 24, 40))
+        if mode in ("fine", "mid"):
+            lo, hi = (0.2, 0.6) if mode == "fine" else (1.2, 1.7)
+            for k in range(3):
+                info.voxel_size[k] = info.time_step * float(rng.uniform(lo, hi))
         lxyz = torch.tensor([[rng.uniform(-1, 1), 0.0, rng.uniform(-1, 1)]], dtype=torch.float32, device=cuda)
         ref = harness.confocal_voxel_scatter(info, cube, lxyz)
         got = ctx.backproject_confocal_scatter(info, cube.view(1, T), lxyz)
