@@ -114,7 +114,7 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
                     float a0 = acc[2 * j], a1 = acc[2 * j + 1];
 #pragma unroll
                     for (int it = 0; it < SP; ++it) {
-                        float d0, d1, b0, b1, t0, t1;
+                        float d0, d1, b0, b1, p0, p1;
                         unpack2(dd, d0, d1);
                         unpack2(add_rz2(mul_rn2(dd, rdp), biasp), b0, b1);
                         const uint32_t i0 = min(__float_as_uint(b0) - 0x4B000000u, slot_w);
@@ -122,9 +122,9 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
                         f32x2_t I = pack2(lds_elem<S>((uint32_t)m.y + (i0 << SH)),
                                           lds_elem<S>((uint32_t)m.y + (i1 << SH)));
                         if (WEIGHTED) I = mul_rn2(I, wlp);
-                        unpack2(add_rn2(pack2(a0, a1), mul_rn2(I, w)), t0, t1);
-                        a0 = d0 < h0 ? t0 : a0;
-                        a1 = d1 < h1 ? t1 : a1;
+                        unpack2(mul_rn2(I, w), p0, p1);
+                        a0 = add_rn_if_lt(a0, p0, d0, h0);
+                        a1 = add_rn_if_lt(a1, p1, d1, h1);
                         dd = add_rn2(dd, stepp);
                     }
                     float d0, d1, w0, w1;
@@ -146,11 +146,9 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
                     float a = acc[k];
 #pragma unroll
                     for (int it = 0; it < SP; ++it) {
-                        const bool on = dd < dmax;
                         float I = lds_elem<S>(bin_at(dd));
                         if (WEIGHTED) I *= wl;
-                        const float t = add_rn(a, mul_rn(I, w));
-                        a = on ? t : a;
+                        a = add_rn_if_lt(a, mul_rn(I, w), dd, dmax);
                         dd = add_rn(dd, step);
                     }
                     acc[k] = walk_rest(a, dd, dmax, w);

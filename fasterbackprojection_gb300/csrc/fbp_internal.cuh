@@ -163,6 +163,14 @@ __device__ __forceinline__ float sub_rn(float a, float b) {
     asm("sub.rn.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
     return r;
 }
+// a + p (round to nearest) where x < y, else a unchanged: one compare and a
+// predicated add.
+__device__ __forceinline__ float add_rn_if_lt(float a, float p, float x, float y) {
+    asm("{\n\t.reg .pred q;\n\tsetp.lt.f32 q, %2, %3;\n\t@q add.rn.ftz.f32 %0, %0, %1;\n\t}"
+        : "+f"(a)
+        : "f"(p), "f"(x), "f"(y));
+    return a;
+}
 // add with round-toward-zero: used for the float->bin truncation trick.
 __device__ __forceinline__ float add_rz(float a, float b) {
     float r;

@@ -42,7 +42,8 @@ struct FilterTaps {
 // consecutive rows) fall in 8 different bank groups.
 constexpr int kFilterQ = 8;
 
-__device__ __forceinline__ int srow_addr(int k, int half) { return 8 * k + 4 * (half ^ ((k >> 2) & 1)); }
+// 8k + 4 (half ^ bit 2 of k): bit 2 of 8k is clear, so OR and XOR compose.
+__device__ __forceinline__ int srow_addr(int k, int half) { return ((k << 3) | (k & 4)) ^ (half << 2); }
 
 __device__ __forceinline__ void srow_load(const float* sh, int k, float (&v)[kFilterQ]) {
     const float4 a = *reinterpret_cast<const float4*>(sh + srow_addr(k, 0));
@@ -79,29 +80,24 @@ __global__ void __launch_bounds__(128) filter_h_kernel(float* __restrict__ data,
     for (int j = threadIdx.x; j < ntp; j += blockDim.x) s_taps[j] = j < ntaps ? taps.w[j] : 0.f;
     for (uint64_t s = blockIdx.x; s < nseries; s += gridDim.x) {
         float* h = data + s * T;
-        const float first = h[0], last = h[T - 1];
-        // Fill in batches of 8 per thread, the batch's loads in flight together
-        // (slots before S[0] and past S[E - 1] are zero).
-        for (int i0 = threadIdx.x; i0 < 8 * rows; i0 += 8 * blockDim.x) {
-            float v[8];
+        // Fill one 16-byte half row (four consecutive slots) per thread and
+        // step.  Slots before S[0] and past S[E - 1] are zero; a slot whose
+        // signal index falls outside [0, T) takes the clamped border sample
+        // (edge) or zero, so every load is in bounds and unconditional.
+        for (int g = threadIdx.x; g < 2 * rows; g += blockDim.x) {
+            float v[4];
 #pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                const int ip = i0 + b * blockDim.x;  // slot index, S index ip - F
-                const int i = ip - F;
-                int k = i - R;  // circular index in [0, n); i - R >= -R > -n
-                if (k < 0) k += n;
-                while (k >= n) k -= n;
+            for (int b = 0; b < 4; ++b) {
+                const int i = 4 * g + b - F;  // S index
+                int k = i - R;                // circular index: -R <= k < n + R for i in [0, E), R < n
+                k += k < 0 ? n : 0;
+                k -= k >= n ? n : 0;
                 const int u = k - pad;  // signal index
-                if (i < 0 || i >= E) v[b] = 0.f;
-                else if (u >= 0 && u < (int)T) v[b] = h[u];
-                else if (edge) v[b] = u < 0 ? first : last;
-                else v[b] = 0.f;
+                const float x = h[min(max(u, 0), (int)T - 1)];
+                const bool keep = i >= 0 && i < E && (edge || (u >= 0 && u < (int)T));
+                v[b] = keep ? x : 0.f;
             }
-#pragma unroll
-            for (int b = 0; b < 8; ++b) {
-                const int ip = i0 + b * blockDim.x;
-                if (ip < 8 * rows) sser[srow_addr(ip >> 3, (ip >> 2) & 1) + (ip & 3)] = v[b];
-            }
+            *reinterpret_cast<float4*>(sser + srow_addr(g >> 1, g & 1)) = make_float4(v[0], v[1], v[2], v[3]);
         }
         __syncthreads();
         for (int t0 = threadIdx.x * Q; t0 < (int)T; t0 += blockDim.x * Q) {
