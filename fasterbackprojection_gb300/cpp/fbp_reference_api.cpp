@@ -7,7 +7,6 @@
 #include <cmath>
 #include <cstring>
 #include <fstream>
-#include <memory>
 #include <mutex>
 #include <sys/stat.h>
 
@@ -21,13 +20,28 @@ void check_cuda(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// An owned device array of n elements (at least one), optionally filled from
+// host memory; freed on scope exit unless released.
 template <typename T>
-T* device_upload(const T* host, size_t n) {
-    T* d = nullptr;
-    check_cuda(cudaMalloc(&d, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc");
-    if (n) check_cuda(cudaMemcpy(d, host, n * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
-    return d;
-}
+class DeviceArray {
+public:
+    explicit DeviceArray(size_t n) { check_cuda(cudaMalloc(&_p, std::max<size_t>(n, 1) * sizeof(T)), "cudaMalloc"); }
+    DeviceArray(const T* host, size_t n) : DeviceArray(n) {
+        if (n) check_cuda(cudaMemcpy(_p, host, n * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    }
+    DeviceArray(const DeviceArray&) = delete;
+    DeviceArray& operator=(const DeviceArray&) = delete;
+    ~DeviceArray() { cudaFree(_p); }
+    T* get() const { return _p; }
+    T* release() {
+        T* p = _p;
+        _p = nullptr;
+        return p;
+    }
+
+private:
+    T* _p = nullptr;
+};
 
 void make_dirs(const std::string& path) {
     std::string cur;
@@ -169,19 +183,21 @@ void NLosData::saveImages(const std::string& outPath) {
     make_dirs(outPath);
     const size_t slice = _data.size() / _dims[0];
     if (slice != _dims[1] * _dims[2]) throw std::runtime_error("NLosData: dims do not match the data size");
-    float* d = device_upload(_data.data(), _data.size());
-    const fbp_status st = fbp_save_transient_images(fbp_default_context(), d, (uint32_t)_dims[1], (uint32_t)_dims[2],
-                                                    (uint32_t)_dims[0], 1, slice, (uint32_t)_dims[1],
-                                                    (uint32_t)_dims[2], 1, outPath.c_str(), nullptr);
-    cudaFree(d);
-    check(st, "NLosData::saveImages");
+    DeviceArray<float> d(_data.data(), _data.size());
+    check(fbp_save_transient_images(fbp_default_context(), d.get(), (uint32_t)_dims[1], (uint32_t)_dims[2],
+                                    (uint32_t)_dims[0], 1, slice, (uint32_t)_dims[1], (uint32_t)_dims[2], 1,
+                                    outPath.c_str(), nullptr),
+          "NLosData::saveImages");
 }
 
 void NLosData::toGpu(ReconstructionInfo& in, ReconstructionBuffers& buf, const TransientParameters& tp) {
     std::memset(&in, 0, sizeof(in));
-    buf._intensity = device_upload(_data.data(), _data.size());
-    buf._sensorTargets = device_upload(_cameraGridPositions.data(), _cameraGridPositions.size());
-    buf._laserTargets = device_upload(_laserGridPositions.data(), _laserGridPositions.size());
+    DeviceArray<float> intensity(_data.data(), _data.size());
+    DeviceArray<fbpref::vec3> sensors(_cameraGridPositions.data(), _cameraGridPositions.size());
+    DeviceArray<fbpref::vec3> lasers(_laserGridPositions.data(), _laserGridPositions.size());
+    buf._intensity = intensity.release();
+    buf._sensorTargets = sensors.release();
+    buf._laserTargets = lasers.release();
     auto set3 = [](float* d, const fbpref::vec3& v) {
         d[0] = v.x;
         d[1] = v.y;
@@ -215,17 +231,12 @@ void NLosData::toGpu(ReconstructionInfo& in, ReconstructionBuffers& buf, const T
 
 static void run_filter(fbp_filter kind, float*& input, const fbpref::uvec3& size, const TransientParameters& p) {
     fbp_context* ctx = fbp_default_context();
-    float* out = nullptr;
-    const size_t n = (size_t)size.x * size.y * size.z;
-    check_cuda(cudaMalloc(&out, n * sizeof(float)), "cudaMalloc");
-    const fbp_status st = fbp_postfilter(ctx, kind, p._kernelSize, p._sigma, input, out, size.x, size.y, size.z, nullptr);
-    if (st != FBP_OK) {
-        cudaFree(out);
-        check(st, "PostprocessingFilters::compute");
-    }
+    DeviceArray<float> out((size_t)size.x * size.y * size.z);
+    check(fbp_postfilter(ctx, kind, p._kernelSize, p._sigma, input, out.get(), size.x, size.y, size.z, nullptr),
+          "PostprocessingFilters::compute");
     check_cuda(cudaDeviceSynchronize(), "PostprocessingFilters::compute");
     cudaFree(input);
-    input = out;
+    input = out.release();
 }
 
 void Laplacian::compute(float*& input, const fbpref::uvec3& size, const TransientParameters& p) const {
@@ -292,19 +303,15 @@ void Laser::reconstructShape(const TransientParameters& tp) {
     make_dirs(tp._outputFolder);
     if (tp._reconstructAABB) {
         const size_t V = (size_t)in.voxel_res[0] * in.voxel_res[1] * in.voxel_res[2];
-        float* vol = nullptr;
-        check_cuda(cudaMalloc(&vol, V * sizeof(float)), "cudaMalloc");
-        std::unique_ptr<float, void (*)(float*)> hold(nullptr, [](float*) {});
-        fbp_status st = exhaustive ? fbp_backproject_exhaustive(ctx, &in, buf._intensity, FBP_F32,
-                                                                reinterpret_cast<float*>(buf._laserTargets),
-                                                                reinterpret_cast<float*>(buf._sensorTargets), vol, nullptr)
-                                   : fbp_backproject_confocal(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
-                                                              reinterpret_cast<float*>(buf._laserTargets), vol, nullptr);
-        if (st != FBP_OK) {
-            cudaFree(vol);
-            check(st, "backprojection");
-        }
+        // The filters replace the buffer they are given (PostprocessingFilters::compute(float*&, ...)).
+        float* vol = DeviceArray<float>(V).release();
         try {
+            check(exhaustive ? fbp_backproject_exhaustive(ctx, &in, buf._intensity, FBP_F32,
+                                                          reinterpret_cast<float*>(buf._laserTargets),
+                                                          reinterpret_cast<float*>(buf._sensorTargets), vol, nullptr)
+                             : fbp_backproject_confocal(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
+                                                        reinterpret_cast<float*>(buf._laserTargets), vol, nullptr),
+                  "backprojection");
             postprocessingFilter(tp._postprocessingFilterType)
                 ->compute(vol, fbpref::uvec3(in.voxel_res[0], in.voxel_res[1], in.voxel_res[2]), tp);
             check(fbp_normalize_minmax(ctx, vol, V, nullptr), "normalizeMatrix");
@@ -324,36 +331,33 @@ void Laser::reconstructShape(const TransientParameters& tp) {
     // Laser.cu:365-377: D depths around the focus depth |(min.y + max.y) / 2|.
     const double focus = std::fabs((in.hidden_min[1] + in.hidden_max[1]) * 0.5f);
     std::vector<double> depths = linearSpace(focus - 0.1f, focus + 0.1f, (int)tp._numReconstructionDepths);
-    double* ddep = device_upload(depths.data(), depths.size());
+    DeviceArray<double> ddep(depths.data(), depths.size());
     // The activation has num_sensor_targets rows (Laser.cu:389, 441); rows
     // past the laser targets stay zero.
     const uint32_t D = (uint32_t)depths.size();
     const size_t rows = std::max(in.num_laser_targets, in.num_sensor_targets);
     const size_t npix = rows * D;
-    float* act = nullptr;
-    check_cuda(cudaMalloc(&act, npix * sizeof(float)), "cudaMalloc");
-    fbp_status st = FBP_OK;
+    DeviceArray<float> act(npix);
     if (rows > in.num_laser_targets)
-        check_cuda(cudaMemset(act, 0, npix * sizeof(float)), "cudaMemset");
-    st = fbp_backproject_depths(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
-                                reinterpret_cast<float*>(buf._laserTargets),
-                                reinterpret_cast<float*>(buf._sensorTargets), ddep, D, act, nullptr);
-    if (st == FBP_OK) st = fbp_normalize_minmax(ctx, act, npix, nullptr);
+        check_cuda(cudaMemset(act.get(), 0, npix * sizeof(float)), "cudaMemset");
+    check(fbp_backproject_depths(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
+                                 reinterpret_cast<float*>(buf._laserTargets),
+                                 reinterpret_cast<float*>(buf._sensorTargets), ddep.get(), D, act.get(), nullptr),
+          "depth reconstruction");
+    check(fbp_normalize_minmax(ctx, act.get(), npix, nullptr), "depth reconstruction");
     _lastVolume.resize(npix);
-    if (st == FBP_OK)
-        check_cuda(cudaMemcpy(_lastVolume.data(), act, npix * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
+    check_cuda(cudaMemcpy(_lastVolume.data(), act.get(), npix * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
     // Laser.cu:410-424, 462-476: one image per depth of side sqrt(num_sensor_targets),
     // enlarged to 256 (confocal, when smaller) or 4x (exhaustive).
     const uint32_t side = (uint16_t)std::sqrt((float)in.num_sensor_targets);
     const bool confocal = in.capture_system == FBP_CONFOCAL;
     const uint32_t out = confocal ? side * (side < 256u ? 256u / side : 1u) : side * 4u;
-    if (st == FBP_OK && side > 0) {
+    if (side > 0) {
         make_dirs(tp._outputFolder);
-        st = fbp_save_transient_images(ctx, act, side, side, D, D, 1, out, out, 0, tp._outputFolder.c_str(), nullptr);
+        check(fbp_save_transient_images(ctx, act.get(), side, side, D, D, 1, out, out, 0, tp._outputFolder.c_str(),
+                                        nullptr),
+              "depth reconstruction");
     }
-    cudaFree(act);
-    cudaFree(ddep);
-    check(st, "depth reconstruction");
     if (!write_raw(tp._outputFolder + "depths.raw", _lastVolume))
         throw std::runtime_error("Laser: cannot write " + tp._outputFolder + "depths.raw");
 }
@@ -364,18 +368,15 @@ void Laser::reconstructAABBConfocalMIS(float* volume, const ReconstructionInfo& 
     // reference reads the buffers its last toGpu left in __constant__ memory).
     if (!volume) throw std::runtime_error("Laser::reconstructAABBConfocalMIS: null volume");
     if (!_nlosData->_isConfocal) throw std::runtime_error("Laser::reconstructAABBConfocalMIS: confocal captures only");
-    float* cube = device_upload(_nlosData->_data.data(), _nlosData->_data.size());
-    fbpref::vec3* lx = device_upload(_nlosData->_laserGridPositions.data(), _nlosData->_laserGridPositions.size());
+    DeviceArray<float> cube(_nlosData->_data.data(), _nlosData->_data.size());
+    DeviceArray<fbpref::vec3> lx(_nlosData->_laserGridPositions.data(), _nlosData->_laserGridPositions.size());
     fbp_mis_params prm{};
     prm.proposal = FBP_MIS_REFERENCE;
     prm.samples = 0;  // L / 4 (Laser.cu:590)
-    const fbp_status st = fbp_mis_backproject(fbp_default_context(), &recInfo, cube, FBP_F32, FBP_LAYOUT_TIME_INNER,
-                                              reinterpret_cast<const float*>(lx), &prm, volume, nullptr);
-    const cudaError_t e = cudaDeviceSynchronize();
-    cudaFree(lx);
-    cudaFree(cube);
-    check(st, "Laser::reconstructAABBConfocalMIS");
-    check_cuda(e, "Laser::reconstructAABBConfocalMIS");
+    check(fbp_mis_backproject(fbp_default_context(), &recInfo, cube.get(), FBP_F32, FBP_LAYOUT_TIME_INNER,
+                              reinterpret_cast<const float*>(lx.get()), &prm, volume, nullptr),
+          "Laser::reconstructAABBConfocalMIS");
+    check_cuda(cudaDeviceSynchronize(), "Laser::reconstructAABBConfocalMIS");
 }
 
 // ---------------------------------------------------------- TransientImage
@@ -404,22 +405,14 @@ void TransientImage::save(const std::string& filename, float* slice, const fbpre
     const size_t n = (size_t)_width * _height;
     std::vector<float> plane(n);
     for (size_t i = 0; i < n; ++i) plane[i] = slice[offset + i * (size_t)stride];
-    float* d = device_upload(plane.data(), n);
-    uint8_t* img = nullptr;
+    DeviceArray<float> d(plane.data(), n);
     const size_t bytes = (size_t)size.x * size.y * 4;
-    cudaError_t e = cudaMalloc(&img, std::max<size_t>(bytes, 1));
-    if (e != cudaSuccess) {
-        cudaFree(d);
-        check_cuda(e, "cudaMalloc");
-    }
-    fbp_status st = fbp_transient_images(fbp_default_context(), d, _width, _height, 1, 1, n, size.x, size.y,
-                                         normalize ? 1 : 0, img, nullptr);
+    DeviceArray<uint8_t> img(bytes);
+    check(fbp_transient_images(fbp_default_context(), d.get(), _width, _height, 1, 1, n, size.x, size.y,
+                               normalize ? 1 : 0, img.get(), nullptr),
+          "TransientImage::save");
     std::vector<uint8_t> host(bytes);
-    if (st == FBP_OK) e = cudaMemcpy(host.data(), img, bytes, cudaMemcpyDeviceToHost);
-    cudaFree(img);
-    cudaFree(d);
-    check(st, "TransientImage::save");
-    check_cuda(e, "D2H");
+    check_cuda(cudaMemcpy(host.data(), img.get(), bytes, cudaMemcpyDeviceToHost), "D2H");
     check(fbp_write_png(filename.c_str(), host.data(), size.x, size.y), "TransientImage::save");
 }
 
@@ -437,13 +430,9 @@ void LCT::reconstructAABB(const ReconstructionInfo& in, const ReconstructionBuff
     p.snr = _snr;
     p.diffuse = _diffuse ? 1 : 0;
     p.grid_mode = FBP_LCT_GRID_REFERENCE;
-    float* vol = nullptr;
-    check_cuda(cudaMalloc(&vol, (size_t)T * L * sizeof(float)), "cudaMalloc");
-    const fbp_status st = fbp_lct(fbp_default_context(), buf._intensity, FBP_LAYOUT_TIME_INNER, N, T, &p, vol, nullptr);
-    if (st == FBP_OK) {
-        _volume.resize((size_t)T * L);
-        check_cuda(cudaMemcpy(_volume.data(), vol, _volume.size() * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
-    }
-    cudaFree(vol);
-    check(st, "LCT::reconstructAABB");
+    DeviceArray<float> vol((size_t)T * L);
+    check(fbp_lct(fbp_default_context(), buf._intensity, FBP_LAYOUT_TIME_INNER, N, T, &p, vol.get(), nullptr),
+          "LCT::reconstructAABB");
+    _volume.resize((size_t)T * L);
+    check_cuda(cudaMemcpy(_volume.data(), vol.get(), _volume.size() * sizeof(float), cudaMemcpyDeviceToHost), "D2H");
 }
