@@ -52,13 +52,10 @@ __device__ __forceinline__ void srow_load(const float* sh, int k, float (&v)[kFi
     v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
 }
 
-// acc[q] += taps[J + st] * window slot (Q + q - st), slots [0, Q) in lo, [Q, 2Q) in hi.
-__device__ __forceinline__ void filter_block(const float* s_taps, int J, const float (&lo)[kFilterQ],
-                                             const float (&hi)[kFilterQ], float (&acc)[kFilterQ]) {
+// acc[q] += t[st] * window slot (Q + q - st), slots [0, Q) in lo, [Q, 2Q) in hi.
+__device__ __forceinline__ void filter_block(const float* t, const float (&lo)[kFilterQ], const float (&hi)[kFilterQ],
+                                             float (&acc)[kFilterQ]) {
     constexpr int Q = kFilterQ;
-    const float4 ta = *reinterpret_cast<const float4*>(s_taps + J);
-    const float4 tb = *reinterpret_cast<const float4*>(s_taps + J + 4);
-    const float t[Q] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
 #pragma unroll
     for (int st = 0; st < Q; ++st)
 #pragma unroll
@@ -68,6 +65,19 @@ __device__ __forceinline__ void filter_block(const float* s_taps, int J, const f
         }
 }
 
+// Taps J .. J + Q - 1 from the shared copy (two 16-byte loads).
+__device__ __forceinline__ void filter_block_shared(const float* s_taps, int J, const float (&lo)[kFilterQ],
+                                                    const float (&hi)[kFilterQ], float (&acc)[kFilterQ]) {
+    const float4 ta = *reinterpret_cast<const float4*>(s_taps + J);
+    const float4 tb = *reinterpret_cast<const float4*>(s_taps + J + 4);
+    const float t[kFilterQ] = {ta.x, ta.y, ta.z, ta.w, tb.x, tb.y, tb.z, tb.w};
+    filter_block(t, lo, hi, acc);
+}
+
+// NJ > 0: exactly NJ blocks of 2Q taps, unrolled, each FMA reading its tap
+// from the kernel parameters (constant bank; zero past the last tap).
+// NJ == 0: any tap count, taps from the shared copy.
+template <int NJ>
 __global__ void __launch_bounds__(128) filter_h_kernel(float* __restrict__ data, uint64_t nseries, uint32_t T, int n,
                                                        int R, int pad, int edge, int F, int ntp, int rows,
                                                        const __grid_constant__ FilterTaps taps) {
@@ -109,12 +119,23 @@ __global__ void __launch_bounds__(128) filter_h_kernel(float* __restrict__ data,
             srow_load(sser, kb, B);
 #pragma unroll
             for (int q = 0; q < Q; ++q) acc[q] = 0.f;
-            for (int J = 0; J < ntp; J += 2 * Q) {
-                const int k = kb - (J >> 3);
-                filter_block(s_taps, J, A, B, acc);
-                srow_load(sser, k - 2, B);  // low window of block J + Q
-                filter_block(s_taps, J + Q, B, A, acc);
-                srow_load(sser, k - 3, A);  // low window of block J + 2Q
+            if constexpr (NJ > 0) {
+#pragma unroll
+                for (int jj = 0; jj < NJ; ++jj) {
+                    const int k = kb - 2 * jj;  // kb - J / Q with J = 2Q jj
+                    filter_block(taps.w + 2 * Q * jj, A, B, acc);
+                    srow_load(sser, k - 2, B);  // low window of block J + Q
+                    filter_block(taps.w + 2 * Q * jj + Q, B, A, acc);
+                    srow_load(sser, k - 3, A);  // low window of block J + 2Q
+                }
+            } else {
+                for (int J = 0; J < ntp; J += 2 * Q) {
+                    const int k = kb - (J >> 3);
+                    filter_block_shared(s_taps, J, A, B, acc);
+                    srow_load(sser, k - 2, B);  // low window of block J + Q
+                    filter_block_shared(s_taps, J + Q, B, A, acc);
+                    srow_load(sser, k - 3, A);  // low window of block J + 2Q
+                }
             }
 #pragma unroll
             for (int q = 0; q < Q; ++q)
@@ -183,12 +204,29 @@ fbp_status filter_h_device(fbp_context* ctx, float* data, uint64_t nseries, uint
     const int rows = (n + 2 * R + F + Q) / Q + 1;
     const size_t smem = ((size_t)ntp + (size_t)Q * rows) * sizeof(float);
     if (smem > (size_t)ctx->smem_optin) return set_error(FBP_ERR_UNSUPPORTED, "filter_H: series too long for one CTA");
-    FBP_TRY_CUDA(cudaFuncSetAttribute(filter_h_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const unsigned blocks = (unsigned)std::min<uint64_t>(nseries, (uint64_t)ctx->sm_count * 16);
-    filter_h_kernel<<<blocks, 128, smem, stream>>>(data, nseries, T, n, R, pad, border == FBP_BORDER_EDGE, F, ntp, rows,
-                                                   tp);
-    FBP_CHECK_LAUNCH(ctx, "filter_h_kernel");
-    return FBP_OK;
+    auto go = [&](auto kernel) -> fbp_status {
+        FBP_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kernel<<<blocks, 128, smem, stream>>>(data, nseries, T, n, R, pad, border == FBP_BORDER_EDGE, F, ntp, rows, tp);
+        FBP_CHECK_LAUNCH(ctx, "filter_h_kernel");
+        return FBP_OK;
+    };
+    // Unrolled forms for 2 .. 12 blocks of 16 taps (wavelengths of about 2
+    // to 20 bins; 10 bins, the reference's default, gives 107 taps = 7 blocks).
+    switch (ntp / (2 * Q)) {
+        case 2: return go(filter_h_kernel<2>);
+        case 3: return go(filter_h_kernel<3>);
+        case 4: return go(filter_h_kernel<4>);
+        case 5: return go(filter_h_kernel<5>);
+        case 6: return go(filter_h_kernel<6>);
+        case 7: return go(filter_h_kernel<7>);
+        case 8: return go(filter_h_kernel<8>);
+        case 9: return go(filter_h_kernel<9>);
+        case 10: return go(filter_h_kernel<10>);
+        case 11: return go(filter_h_kernel<11>);
+        case 12: return go(filter_h_kernel<12>);
+        default: return go(filter_h_kernel<0>);
+    }
 }
 
 }  // namespace fbp

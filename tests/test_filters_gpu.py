@@ -67,6 +67,22 @@ def test_filter_h_vs_fp64_fft(ctx, cuda, T, border):
     assert rel_l2(d.cpu().numpy(), want) < 2e-6
 
 
+@pytest.mark.parametrize("wl_bins", [1.5, 3.0, 6.0, 30.0])
+def test_filter_h_wavelengths_vs_fp64_fft(ctx, cuda, wl_bins):
+    """Tap counts of 2 to 20 blocks of 16 (the unrolled forms and the general
+    loop), against the FP64 padded-FFT pipeline."""
+    import torch
+
+    rng = np.random.default_rng(int(wl_bins * 10))
+    T = 1024
+    data = rng.poisson(2.0, (200, T)).astype(np.float32)
+    step = 0.0048
+    d = torch.from_numpy(data).to(cuda)
+    ctx.filter_h_(d, step, wl_mean=wl_bins * step)
+    want = numpy_ref.filter_h(data, step, wl_mean=wl_bins * step)
+    assert rel_l2(d.cpu().numpy(), want) < 2e-6
+
+
 def test_filter_h_vs_reference_fft_pipeline(ctx, cuda):
     """Against the reference's own arithmetic path on the GPU: padded series,
     batched C2C FFT (cuFFT through torch), the spectrum product, unnormalised
