@@ -70,12 +70,46 @@ def _np_dtype_code(a: np.ndarray) -> int:
     raise TypeError(f"unsupported host cube dtype {a.dtype} (float32, float16, or uint16 bfloat16 bits)")
 
 
-def _ptr(t) -> c_void_p:
+def _ptr(t, min_numel: int = 0, dtype=None, name: str = "tensor") -> c_void_p:
+    """Device address of a contiguous CUDA tensor (NULL for None).  The kernels
+    take plain pointers, so the sizes they will touch are checked here: a host
+    tensor, a tensor smaller than `min_numel` elements or one of another
+    element type than `dtype` raises before any launch."""
     if t is None:
         return c_void_p(0)
+    if not getattr(t, "is_cuda", False):
+        raise TypeError(f"{name} must be a CUDA tensor (got {type(t).__name__}"
+                        f"{' on ' + str(t.device) if hasattr(t, 'device') else ''})")
     if not t.is_contiguous():
-        raise ValueError("tensor must be contiguous")
+        raise ValueError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype} (got {t.dtype})")
+    if t.numel() < min_numel:
+        raise ValueError(f"{name} has {t.numel()} elements, needs at least {min_numel}")
     return c_void_p(t.data_ptr())
+
+
+def _f32():
+    import torch
+
+    return torch.float32
+
+
+def _voxels(info: ReconInfo) -> int:
+    vx, vy, vz = info.voxel_res
+    return int(vx) * int(vy) * int(vz)
+
+
+def _cube_elems(info: ReconInfo, exhaustive: bool = False) -> int:
+    L, T = int(info.num_laser_targets), int(info.num_time_bins)
+    return L * (int(info.num_sensor_targets) if exhaustive else 1) * T
+
+
+def _plane_span(width: int, height: int, num_planes: int, pixel_stride: int, plane_stride: int) -> int:
+    """Elements up to the last pixel read: plane p pixel i at p*plane_stride + i*pixel_stride."""
+    if width <= 0 or height <= 0 or num_planes <= 0:
+        return 0
+    return (num_planes - 1) * plane_stride + (width * height - 1) * pixel_stride + 1
 
 
 class Context:
@@ -125,8 +159,10 @@ class Context:
         vx, vy, vz = info.voxel_res
         if out is None:
             out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
-        check(self._lib.fbp_backproject_confocal(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
-                                                 _ptr(laser_xyz), _ptr(out), self._stream(stream)))
+        check(self._lib.fbp_backproject_confocal(self._h, byref(info), _ptr(cube, _cube_elems(info), name="cube"),
+                                                 _dtype_code(cube), layout,
+                                                 _ptr(laser_xyz, 3 * info.num_laser_targets, _f32(), "laser_xyz"),
+                                                 _ptr(out, _voxels(info), _f32(), "out"), self._stream(stream)))
         return out
 
     def backproject_confocal_scatter(self, info: ReconInfo, cube, laser_xyz, out=None,
@@ -137,8 +173,10 @@ class Context:
         vx, vy, vz = info.voxel_res
         if out is None:
             out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
-        check(self._lib.fbp_backproject_confocal_scatter(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
-                                                         _ptr(laser_xyz), _ptr(out), self._stream(stream)))
+        check(self._lib.fbp_backproject_confocal_scatter(self._h, byref(info), _ptr(cube, _cube_elems(info), name="cube"),
+                                                         _dtype_code(cube), layout,
+                                                         _ptr(laser_xyz, 3 * info.num_laser_targets, _f32(), "laser_xyz"),
+                                                         _ptr(out, _voxels(info), _f32(), "out"), self._stream(stream)))
         return out
 
     def splat_backproject(self, info: ReconInfo, cube, laser_xyz, max_bins: int = 700, grid=(256, 256), out=None,
@@ -149,8 +187,10 @@ class Context:
         vx, vy, vz = info.voxel_res
         if out is None:
             out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
-        check(self._lib.fbp_splat_backproject(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
-                                              _ptr(laser_xyz), max_bins, grid[0], grid[1], _ptr(out),
+        check(self._lib.fbp_splat_backproject(self._h, byref(info), _ptr(cube, _cube_elems(info), name="cube"),
+                                              _dtype_code(cube), layout,
+                                              _ptr(laser_xyz, 3 * info.num_laser_targets, _f32(), "laser_xyz"),
+                                              max_bins, grid[0], grid[1], _ptr(out, _voxels(info), _f32(), "out"),
                                               self._stream(stream)))
         return out
 
@@ -162,8 +202,11 @@ class Context:
         vx, vy, _ = info.voxel_res
         if out is None:
             out = torch.empty((z_end - z_begin, vy, vx), dtype=torch.float32, device=cube.device)
-        check(self._lib.fbp_backproject_confocal_slab(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
-                                                      _ptr(laser_xyz), z_begin, z_end, _ptr(out),
+        nz = max(0, min(int(z_end), int(info.voxel_res[2])) - int(z_begin))
+        check(self._lib.fbp_backproject_confocal_slab(self._h, byref(info), _ptr(cube, _cube_elems(info), name="cube"),
+                                                      _dtype_code(cube), layout,
+                                                      _ptr(laser_xyz, 3 * info.num_laser_targets, _f32(), "laser_xyz"),
+                                                      z_begin, z_end, _ptr(out, nz * vx * vy, _f32(), "out"),
                                                       self._stream(stream)))
         return out
 
@@ -173,9 +216,11 @@ class Context:
         vx, vy, vz = info.voxel_res
         if out is None:
             out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
-        check(self._lib.fbp_backproject_exhaustive(self._h, byref(info), _ptr(cube), _dtype_code(cube),
-                                                   _ptr(laser_xyz), _ptr(sensor_xyz), _ptr(out),
-                                                   self._stream(stream)))
+        check(self._lib.fbp_backproject_exhaustive(self._h, byref(info), _ptr(cube, _cube_elems(info, True), name="cube"),
+                                                   _dtype_code(cube),
+                                                   _ptr(laser_xyz, 3 * info.num_laser_targets, _f32(), "laser_xyz"),
+                                                   _ptr(sensor_xyz, 3 * info.num_sensor_targets, _f32(), "sensor_xyz"),
+                                                   _ptr(out, _voxels(info), _f32(), "out"), self._stream(stream)))
         return out
 
     def backproject_depths(self, info: ReconInfo, cube, laser_xyz, depths, sensor_xyz=None, out=None,
@@ -186,9 +231,17 @@ class Context:
         D = int(depths.numel())
         if out is None:
             out = torch.empty((L, D), dtype=torch.float32, device=cube.device)
-        check(self._lib.fbp_backproject_depths(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
-                                               _ptr(laser_xyz), _ptr(sensor_xyz), _ptr(depths), D, _ptr(out),
-                                               self._stream(stream)))
+        import torch
+
+        exhaustive = info.capture_system == _lib.FBP_EXHAUSTIVE
+        check(self._lib.fbp_backproject_depths(self._h, byref(info),
+                                               _ptr(cube, _cube_elems(info, exhaustive), name="cube"),
+                                               _dtype_code(cube), layout,
+                                               _ptr(laser_xyz, 3 * L, _f32(), "laser_xyz"),
+                                               _ptr(sensor_xyz, 3 * info.num_sensor_targets if exhaustive else 0,
+                                                    _f32(), "sensor_xyz"),
+                                               _ptr(depths, D, torch.float64, "depths"), D,
+                                               _ptr(out, L * D, _f32(), "out"), self._stream(stream)))
         return out
 
     def transient_images(self, data, width: int, height: int, num_planes: int, pixel_stride: int,
@@ -201,8 +254,11 @@ class Context:
         ow, oh = size if size is not None else (width, height)
         if out is None:
             out = torch.empty((num_planes, oh, ow, 4), dtype=torch.uint8, device=data.device)
-        check(self._lib.fbp_transient_images(self._h, _ptr(data), width, height, num_planes, pixel_stride,
-                                             plane_stride, ow, oh, int(normalize), _ptr(out), self._stream(stream)))
+        check(self._lib.fbp_transient_images(self._h, _ptr(data, _plane_span(width, height, num_planes, pixel_stride,
+                                                                              plane_stride), _f32(), "data"),
+                                             width, height, num_planes, pixel_stride, plane_stride, ow, oh,
+                                             int(normalize), _ptr(out, num_planes * oh * ow * 4, torch.uint8, "out"),
+                                             self._stream(stream)))
         return out
 
     def depth_plane_images(self, activation, width: int, height: int, size=None, normalize: bool = False,
@@ -215,7 +271,9 @@ class Context:
                               plane_stride: int, prefix: str, size=None, normalize: bool = False, stream=None):
         """Writes "<prefix>transient_<p>.png" for every plane."""
         ow, oh = size if size is not None else (width, height)
-        check(self._lib.fbp_save_transient_images(self._h, _ptr(data), width, height, num_planes, pixel_stride,
+        span = _plane_span(width, height, num_planes, pixel_stride, plane_stride)
+        check(self._lib.fbp_save_transient_images(self._h, _ptr(data, span, _f32(), "data"), width, height,
+                                                  num_planes, pixel_stride,
                                                   plane_stride, ow, oh, int(normalize), prefix.encode(),
                                                   self._stream(stream)))
 
@@ -249,12 +307,13 @@ class Context:
         vz, vy, vx = vol.shape
         if out is None:
             out = torch.empty_like(vol)
-        check(self._lib.fbp_postfilter(self._h, kind, kernel_size, sigma, _ptr(vol), _ptr(out), vx, vy, vz,
+        check(self._lib.fbp_postfilter(self._h, kind, kernel_size, sigma, _ptr(vol, 0, _f32(), "vol"),
+                                       _ptr(out, vol.numel(), _f32(), "out"), vx, vy, vz,
                                        self._stream(stream)))
         return out
 
     def normalize_(self, v, stream=None):
-        check(self._lib.fbp_normalize_minmax(self._h, _ptr(v), v.numel(), self._stream(stream)))
+        check(self._lib.fbp_normalize_minmax(self._h, _ptr(v, 0, _f32(), "v"), v.numel(), self._stream(stream)))
         return v
 
     def filter_h_(self, data, delta_t: float, wl_mean: float | None = None, wl_sigma: float = 0.0,
@@ -263,7 +322,8 @@ class Context:
         n, T = data.shape[0] if data.dim() > 1 else 1, data.shape[-1]
         n = data.numel() // T
         wl = delta_t * 10.0 if wl_mean is None else wl_mean
-        check(self._lib.fbp_filter_h(self._h, _ptr(data), n, T, delta_t, wl, wl_sigma, border, self._stream(stream)))
+        check(self._lib.fbp_filter_h(self._h, _ptr(data, 0, _f32(), "data"), n, T, delta_t, wl, wl_sigma, border,
+                                     self._stream(stream)))
         return data
 
     # -------------------------------------------------------------------- MIS
@@ -275,10 +335,13 @@ class Context:
         vx, vy, vz = info.voxel_res
         if out is None:
             out = torch.empty((vz, vy, vx), dtype=torch.float32, device=cube.device)
-        prm = MisParams(proposal, samples, seed, _ptr(noise), 0 if noise is None else noise.numel(),
-                        _ptr(tile_cluster_cdf), cluster_side, scan_side, cv_side)
-        check(self._lib.fbp_mis_backproject(self._h, byref(info), _ptr(cube), _dtype_code(cube), layout,
-                                            _ptr(laser_xyz), byref(prm), _ptr(out), self._stream(stream)))
+        prm = MisParams(proposal, samples, seed, _ptr(noise, 0, _f32(), "noise"),
+                        0 if noise is None else noise.numel(), _ptr(tile_cluster_cdf, 0, _f32(), "tile_cluster_cdf"),
+                        cluster_side, scan_side, cv_side)
+        check(self._lib.fbp_mis_backproject(self._h, byref(info), _ptr(cube, _cube_elems(info), name="cube"),
+                                            _dtype_code(cube), layout,
+                                            _ptr(laser_xyz, 3 * info.num_laser_targets, _f32(), "laser_xyz"),
+                                            byref(prm), _ptr(out, _voxels(info), _f32(), "out"), self._stream(stream)))
         return out
 
     def mis_reference_tables(self, info: ReconInfo, cube, layout=_lib.FBP_LAYOUT_TIME_INNER, stream=None):
@@ -305,7 +368,8 @@ class Context:
         if out is None:
             out = torch.empty((M, N, N), dtype=torch.float32, device=data.device)
         prm = LctParams(width, bin_length, snr, int(diffuse), grid_mode)
-        check(self._lib.fbp_lct(self._h, _ptr(data), layout, N, M, byref(prm), _ptr(out), self._stream(stream)))
+        check(self._lib.fbp_lct(self._h, _ptr(data, M * N * N, _f32(), "data"), layout, N, M, byref(prm),
+                                _ptr(out, M * N * N, _f32(), "out"), self._stream(stream)))
         return out
 
     # -------------------------------------------------------- learned proposal

@@ -148,3 +148,46 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
+def test_device_pointer_checks_reject_host_and_short_tensors():
+    """The Python layer hands kernels plain pointers: host memory, a wrong
+    element type and (through the sizes each entry point needs) short
+    buffers are refused before any launch."""
+    import torch
+
+    from fasterbackprojection_gb300.api import _plane_span, _ptr
+
+    assert _ptr(None).value is None
+    with pytest.raises(TypeError, match="CUDA tensor"):
+        _ptr(torch.zeros(4), name="cube")
+    with pytest.raises(TypeError, match="CUDA tensor"):
+        _ptr(np.zeros(4, np.float32))
+
+    class FakeCuda:  # stands in for a device tensor on a machine without one
+        is_cuda = True
+        dtype = torch.float32
+
+        def __init__(self, n, contiguous=True):
+            self.n, self.c = n, contiguous
+
+        def is_contiguous(self):
+            return self.c
+
+        def numel(self):
+            return self.n
+
+        def data_ptr(self):
+            return 4096
+
+    assert _ptr(FakeCuda(12), 12, torch.float32).value == 4096
+    with pytest.raises(ValueError, match="at least 13"):
+        _ptr(FakeCuda(12), 13, name="out")
+    with pytest.raises(ValueError, match="contiguous"):
+        _ptr(FakeCuda(12, contiguous=False))
+    with pytest.raises(TypeError, match="float64"):
+        _ptr(FakeCuda(12), 0, torch.float64, "depths")
+    # Plane p, pixel i at p * plane_stride + i * pixel_stride.
+    assert _plane_span(16, 16, 200, 200, 1) == 256 * 200
+    assert _plane_span(12, 40, 5, 1, 480) == 5 * 480
+    assert _plane_span(0, 4, 4, 4, 1) == 0
