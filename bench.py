@@ -934,7 +934,7 @@ def learned_mis_leg(ctx, dev, info, cube, lx, n_train=2000, ks=(4, 8, 16, 32, 64
     data_s = data.seconds
     del data
     return {
-        "workload": "config-2 capture in BF16 (256^2 x 1024 -> 256^3); K clusters of 16x16 scan points per "
+        "workload": "256^2 x 1024 confocal patch capture in BF16 (-> 256^3); K clusters of 16x16 scan points per "
                     "8x16x16-voxel tile, systematic sampling, whole clusters gathered",
         "training": {"scenes": n_train, "tiles": int(n_train * 64), "epochs": 4, "losses": losses,
                      "data_s": data_s, "train_s": train_s},

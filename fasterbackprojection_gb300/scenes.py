@@ -62,7 +62,8 @@ def random_points(n_points: int, depth_range, seed: int, xz_range=(-1.0, 1.0)):
 
 def confocal_points(n: int, T: int, dt_s: float, n_points: int = 200, depth_range=(0.4, 1.2), seed: int = 1,
                     photons: float = 1e4, noise: bool = True) -> Capture:
-    """Config-1 style capture: seeded points, albedo / r^4 at round(2r / (c dt))."""
+    """Confocal point-scene capture (the 64^2 x 512 LCT shape and small test cases):
+    seeded points, albedo / r^4 at round(2r / (c dt))."""
     step = LIGHT_SPEED * dt_s
     lx = wall_grid(n)
     pts, alb, rng = random_points(n_points, depth_range, seed)
@@ -109,7 +110,8 @@ def confocal_points_torch(n: int, T: int, dt_s: float, n_points: int = 200, dept
 
 def exhaustive_points(nl: int, ns: int, T: int, dt_s: float, n_points: int = 500, depth_range=(0.4, 1.4),
                       seed: int = 3, photons: float = 1e4, noise: bool = True) -> Capture:
-    """Config-3 style capture: [L][S][T], albedo / (r_l^2 r_s^2) at round((r_l + r_s) / (c dt))."""
+    """Exhaustive (laser x SPAD) point-scene capture: [L][S][T], albedo / (r_l^2 r_s^2)
+    at round((r_l + r_s) / (c dt))."""
     step = LIGHT_SPEED * dt_s
     lx = wall_grid(nl)
     sx = wall_grid(ns)
@@ -164,7 +166,7 @@ def exhaustive_points_torch(nl: int, ns: int, T: int, dt_s: float, n_points: int
 
 
 def patch_points(n_patches: int, depth_range, seed: int, sample: float = 0.004):
-    """Config-2 scene: planar patches (edge U[0.1, 0.4] m, normal uniform on
+    """Patch scene of the 256^2 x 1024 confocal workload: planar patches (edge U[0.1, 0.4] m, normal uniform on
     the hemisphere facing the wall) sampled every `sample` metres."""
     rng = np.random.default_rng(seed)
     pts, alb = [], []
@@ -190,7 +192,7 @@ def patch_points(n_patches: int, depth_range, seed: int, sample: float = 0.004):
 
 def confocal_patches_torch(n: int, T: int, dt_s: float, n_patches: int = 8, depth_range=(0.3, 1.5), seed: int = 2,
                            photons: float = 1e4, device="cuda", sample: float = 0.004, noise: bool = True) -> Capture:
-    """Config-2 capture generated on the device (65536 scan points x ~10^5
+    """The 256^2 x 1024 confocal patch capture generated on the device (65536 scan points x ~10^5
     scene samples is too slow in NumPy).  Returns torch tensors on `device`."""
     import torch
 

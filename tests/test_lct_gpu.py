@@ -38,7 +38,7 @@ def test_lct_layouts_and_plan_cache(ctx, cuda):
 
 
 @pytest.mark.parametrize("grid", ["reference", "depth"])
-def test_lct_config1_size_vs_fp64(ctx, cuda, grid):
+def test_lct_64x64x512_vs_fp64(ctx, cuda, grid):
     """64 x 64 scan, 512 bins of 32 ps (the LCT benchmark shape)."""
     import torch
     from fasterbackprojection_gb300 import FBP_LCT_GRID_DEPTH, FBP_LCT_GRID_REFERENCE, scenes
