@@ -119,32 +119,53 @@ struct BitOut {
     std::vector<uint8_t>& out;
     uint64_t acc = 0;
     int n = 0;
-    void put(uint32_t bits, int count) {  // LSB first
+    void put(uint32_t bits, int count) {  // LSB first, count <= 16
         acc |= (uint64_t)bits << n;
         n += count;
-        while (n >= 8) {
-            out.push_back((uint8_t)acc);
-            acc >>= 8;
-            n -= 8;
+        if (n >= 32) {  // four whole bytes at a time
+            const uint8_t four[4] = {(uint8_t)acc, (uint8_t)(acc >> 8), (uint8_t)(acc >> 16), (uint8_t)(acc >> 24)};
+            out.insert(out.end(), four, four + 4);
+            acc >>= 32;
+            n -= 32;
         }
     }
-    void put_code(uint32_t code, int len) {  // Huffman codes go MSB first
-        uint32_t r = 0;
-        for (int i = 0; i < len; ++i) r |= ((code >> i) & 1u) << (len - 1 - i);
-        put(r, len);
-    }
     void flush() {
-        if (n > 0) out.push_back((uint8_t)acc);
+        for (; n > 0; n -= 8) {
+            out.push_back((uint8_t)acc);
+            acc >>= 8;
+        }
         acc = 0;
         n = 0;
     }
 };
 
+// The fixed literal/length code of RFC 1951 3.2.6, bit-reversed once for the
+// LSB-first writer: code[sym] | length << 16.
+struct FixedCodes {
+    uint32_t lit[288];
+    uint32_t dist[30];
+    static uint32_t reversed(uint32_t code, int len) {
+        uint32_t r = 0;
+        for (int i = 0; i < len; ++i) r |= ((code >> i) & 1u) << (len - 1 - i);
+        return r;
+    }
+    FixedCodes() {
+        for (uint32_t sym = 0; sym < 288; ++sym) {
+            uint32_t code, len;
+            if (sym < 144) code = 0x30 + sym, len = 8;
+            else if (sym < 256) code = 0x190 + (sym - 144), len = 9;
+            else if (sym < 280) code = sym - 256, len = 7;
+            else code = 0xC0 + (sym - 280), len = 8;
+            lit[sym] = reversed(code, (int)len) | len << 16;
+        }
+        for (uint32_t d = 0; d < 30; ++d) dist[d] = reversed(d, 5) | 5u << 16;
+    }
+};
+const FixedCodes kFixed;
+
 void put_literal(BitOut& b, uint32_t sym) {
-    if (sym < 144) b.put_code(0x30 + sym, 8);
-    else if (sym < 256) b.put_code(0x190 + (sym - 144), 9);
-    else if (sym < 280) b.put_code(sym - 256, 7);
-    else b.put_code(0xC0 + (sym - 280), 8);
+    const uint32_t c = kFixed.lit[sym];
+    b.put(c & 0xFFFF, (int)(c >> 16));
 }
 
 const uint16_t kLenBase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27,
@@ -161,11 +182,12 @@ void put_match(BitOut& b, uint32_t len, uint32_t dist) {
     b.put(len - kLenBase[lc], kLenExtra[lc]);
     int dc = 29;
     while (kDistBase[dc] > dist) --dc;
-    b.put_code(dc, 5);
+    b.put(kFixed.dist[dc] & 0xFFFF, 5);
     b.put(dist - kDistBase[dc], kDistExtra[dc]);
 }
 
 void zlib_compress(const std::vector<uint8_t>& in, std::vector<uint8_t>& out) {
+    out.reserve(out.size() + in.size() + in.size() / 8 + 64);  // fixed codes: at most 9 bits per byte
     out.push_back(0x78);
     out.push_back(0x01);
     BitOut b{out};
@@ -174,7 +196,12 @@ void zlib_compress(const std::vector<uint8_t>& in, std::vector<uint8_t>& out) {
     constexpr uint32_t kWin = 32768, kHash = 1u << 15, kChain = 24;
     std::vector<int32_t> head(kHash, -1), prev(kWin, -1);
     const size_t n = in.size();
-    auto hash3 = [&](size_t i) { return ((in[i] << 10) ^ (in[i + 1] << 5) ^ in[i + 2]) & (kHash - 1); };
+    // Multiplicative (Fibonacci) hash of the three bytes: filtered RGBA rows
+    // are full of zero bytes, which a shift-and-xor hash folds into few buckets.
+    auto hash3 = [&](size_t i) {
+        const uint32_t v = (uint32_t)in[i] | (uint32_t)in[i + 1] << 8 | (uint32_t)in[i + 2] << 16;
+        return (v * 2654435761u) >> 17;  // 15 bits
+    };
     auto insert = [&](size_t i) {
         if (i + 2 >= n) return;
         const uint32_t h = hash3(i);
@@ -188,6 +215,13 @@ void zlib_compress(const std::vector<uint8_t>& in, std::vector<uint8_t>& out) {
             int32_t c = head[hash3(i)];
             const uint32_t maxlen = (uint32_t)std::min<size_t>(258, n - i);
             for (uint32_t k = 0; k < kChain && c >= 0 && i - (size_t)c <= kWin; ++k) {
+                // A candidate that differs at the current best length cannot be longer.
+                if (best < maxlen && in[c + best] != in[i + best]) {
+                    const int32_t nx = prev[c & (kWin - 1)];
+                    if (nx >= c) break;
+                    c = nx;
+                    continue;
+                }
                 uint32_t l = 0;
                 while (l < maxlen && in[c + l] == in[i + l]) ++l;
                 if (l > best) {
@@ -212,10 +246,17 @@ void zlib_compress(const std::vector<uint8_t>& in, std::vector<uint8_t>& out) {
     }
     put_literal(b, 256);
     b.flush();
+    // Adler-32 (RFC 1950 8.2), reduced modulo 65521 once per 5552 bytes: the
+    // longest run whose sums cannot overflow 32 bits.
     uint32_t s1 = 1, s2 = 0;
-    for (uint8_t v : in) {
-        s1 = (s1 + v) % 65521u;
-        s2 = (s2 + s1) % 65521u;
+    for (size_t at = 0; at < n;) {
+        const size_t end = std::min(n, at + 5552);
+        for (; at < end; ++at) {
+            s1 += in[at];
+            s2 += s1;
+        }
+        s1 %= 65521u;
+        s2 %= 65521u;
     }
     const uint32_t adler = (s2 << 16) | s1;
     for (int k = 3; k >= 0; --k) out.push_back((uint8_t)(adler >> (8 * k)));
