@@ -74,6 +74,18 @@ def confocal_voxel(info, cube, laser_xyz, layout=LAYOUT_TIME_INNER, bins=None) -
     return vol
 
 
+def confocal_scatter_voxel(info, cube, laser_xyz, layout=LAYOUT_TIME_INNER) -> np.ndarray:
+    """FP64 volume [Vz][Vy][Vx] of the ACCUMULATE_VOXEL_SCATTERING build."""
+    lib = load()
+    o = to_oracle_info(info)
+    vx, vy, vz = o.voxel_res
+    vol = np.empty((vz, vy, vx), dtype=np.float64)
+    rc = lib.oracle_confocal_scatter_voxel(ctypes.byref(o), _p(_f32(cube)), c_int(layout), _p(_f32(laser_xyz)),
+                                           _p(vol))
+    assert rc == 0, rc
+    return vol
+
+
 def confocal_voxel_subset(info, cube, laser_xyz, idx, layout=LAYOUT_TIME_INNER, bins=None) -> np.ndarray:
     """FP64 values of the voxels idx; bins (len(idx) x L int32), when given,
     replace the FP64 bin computation."""

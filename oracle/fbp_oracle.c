@@ -136,6 +136,50 @@ int oracle_confocal_voxel_subset_bins(const oracle_info* in, const float* cube, 
     return 0;
 }
 
+/* transient_reconstruction.cuh:112-126 (ACCUMULATE_VOXEL_SCATTERING): the walk
+ * over [max(0, dist - ext), dist + ext) in steps of timeStep + EPS; the
+ * reference's thread returns at the first bin outside [0, T). */
+static double scatter_voxel_value(const oracle_info* in, const float* cube, int layout, const float* laser_xyz,
+                                  const double* bounce, int64_t v) {
+    const uint32_t Vx = in->voxel_res[0], Vy = in->voxel_res[1];
+    const uint32_t L = in->num_laser_targets, T = in->num_time_bins;
+    const uint32_t slice = Vx * Vy;
+    const uint32_t vz = (uint32_t)(v / slice), rem = (uint32_t)(v % slice);
+    const uint32_t vy = rem / Vx, vx = rem % Vx;
+    const double vs0 = in->voxel_size[0], vs1 = in->voxel_size[1], vs2 = in->voxel_size[2];
+    const double ext = 0.5 * sqrt(vs0 * vs0 + vs1 * vs1 + vs2 * vs2);
+    const double dt = in->time_step, step = dt + (double)ORACLE_EPS;
+    double p[3];
+    voxel_center(in, vx, vy, vz, p);
+    double acc = 0.0;
+    for (uint32_t l = 0; l < L; ++l) {
+        double lp[3];
+        load3(laser_xyz + 3 * (size_t)l, lp);
+        const double dist = dist3(lp, p) * 2.0 - (double)in->time_offset + bounce[l];
+        const double w = safe_rcp_d(dist * dist);
+        const double dmax = dist + ext;
+        for (double d = dist - ext > 0.0 ? dist - ext : 0.0; d < dmax; d += step) {
+            const int32_t b = bin_of(d, dt, T);
+            if (b < 0) break;
+            const float I = cube[confocal_index(layout, l, (uint32_t)b, L, T)];
+            if (I > ORACLE_EPS) acc += (double)I * w;
+        }
+    }
+    return acc;
+}
+
+int oracle_confocal_scatter_voxel(const oracle_info* in, const float* cube, int layout, const float* laser_xyz,
+                                  double* vol) {
+    if (!(in->time_step > 0.f)) return 2; /* the walk needs a positive step */
+    const int64_t V = (int64_t)in->voxel_res[0] * in->voxel_res[1] * in->voxel_res[2];
+    double* bounce = confocal_bounces(in, laser_xyz);
+    if (!bounce) return 1;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t v = 0; v < V; ++v) vol[v] = scatter_voxel_value(in, cube, layout, laser_xyz, bounce, v);
+    free(bounce);
+    return 0;
+}
+
 /* FP32 restatement of backprojectConfocalVoxel: the reference arithmetic in
  * float (IEEE sqrt and divide), one task per voxel summing over all scan
  * points.  Used as the timed CPU baseline. */

@@ -64,6 +64,14 @@ int oracle_confocal_voxel_subset(const oracle_info* info, const float* cube, int
 int oracle_confocal_voxel_subset_bins(const oracle_info* info, const float* cube, int layout, const float* laser_xyz,
                                       const int64_t* idx, int64_t n, const int32_t* bins, double* out);
 
+/* The ACCUMULATE_VOXEL_SCATTERING build of backprojectConfocalVoxel
+ * (transient_reconstruction.cuh:112-126), FP64: per (voxel, scan point) every
+ * bin of the path d = max(0, dist - ext) .. dist + ext (exclusive) stepped by
+ * timeStep + EPS, ext = |voxelSize| / 2, ending at the first bin outside
+ * [0, T); each I > 1e-5 adds I / dist^2. */
+int oracle_confocal_scatter_voxel(const oracle_info* info, const float* cube, int layout, const float* laser_xyz,
+                                  double* vol);
+
 /* FP32 restatement of the same kernel (reference arithmetic in float, IEEE
  * sqrt/div, one thread per voxel instead of per pair): the timed CPU baseline. */
 int oracle_confocal_voxel_f32_subset(const oracle_info* info, const float* cube, int layout, const float* laser_xyz,

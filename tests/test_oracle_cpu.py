@@ -181,6 +181,72 @@ def test_confocal_oracle_known_answer_single_pair():
     assert cpu.confocal_voxel(o, cube, np.zeros((1, 3), np.float32))[0, 0, 0] == 0.0
 
 
+def _loop_scatter(o, cube_tmajor, lxyz):
+    """Pure-Python restatement of the ACCUMULATE_VOXEL_SCATTERING build
+    (transient_reconstruction.cuh:112-126), FP64, cube[t*L + l]."""
+    Vx, Vy, Vz = o.voxel_res
+    L, T = o.num_laser_targets, o.num_time_bins
+    vol = np.zeros((Vz, Vy, Vx))
+    lp = np.array(o.laser_position[:], dtype=np.float64)
+    sp = np.array(o.sensor_position[:], dtype=np.float64)
+    vs = np.array(o.voxel_size[:], dtype=np.float64)
+    ext = 0.5 * float(np.sqrt(vs @ vs))
+    step = o.time_step + float(np.float32(1e-5))
+    for vz in range(Vz):
+        for vy in range(Vy):
+            for vx in range(Vx):
+                p = np.array([o.hidden_min[0] + vx * vs[0] + 0.5 * vs[0], o.hidden_min[1] + vz * vs[1] + 0.5 * vs[1],
+                              o.hidden_min[2] + vy * vs[2] + 0.5 * vs[2]])
+                for l in range(L):
+                    q = lxyz[l].astype(np.float64)
+                    dist = np.linalg.norm(p - q) * 2.0 - o.time_offset
+                    if o.discard_first_last_bounces == 0:
+                        dist += np.linalg.norm(q - lp) + np.linalg.norm(q - sp)
+                    d2 = dist * dist
+                    w = 1.0 / d2 if abs(d2) > 1e-5 else np.finfo(np.float32).max
+                    d = max(0.0, dist - ext)
+                    while d < dist + ext:
+                        x = d / o.time_step
+                        if not (x > -1 and x < T):
+                            break  # the reference's thread returns
+                        I = cube_tmajor[int(x) * L + l]
+                        if I > np.float32(1e-5):
+                            vol[vz, vy, vx] += I * w
+                        d += step
+    return vol
+
+
+@pytest.mark.parametrize("discard,t0", [(1, 0.0), (0, 0.0), (1, 0.05)])
+def test_scatter_oracle_matches_python_loop(discard, t0):
+    rng = np.random.default_rng(9)
+    L, T = 9, 64
+    lxyz = np.stack([rng.uniform(-1, 1, L), np.zeros(L), rng.uniform(-1, 1, L)], 1).astype(np.float32)
+    o = _info(L, T, 0.05, (3, 4, 5), (-0.5, -1.2, -0.4), (0.3, 0.2, 0.25), discard, t0)
+    cube = rng.uniform(0, 2, (T, L)).astype(np.float32)  # time-major
+    cube[cube < 0.3] = 0
+    want = _loop_scatter(o, cube.ravel(), lxyz)
+    got_tm = cpu.confocal_scatter_voxel(o, cube, lxyz, layout=cpu.LAYOUT_TIME_MAJOR)
+    got_ti = cpu.confocal_scatter_voxel(o, np.ascontiguousarray(cube.T), lxyz, layout=cpu.LAYOUT_TIME_INNER)
+    np.testing.assert_allclose(got_tm, want, rtol=1e-12)
+    np.testing.assert_array_equal(got_tm, got_ti)
+    # Several bins per pair: the walk adds more than the single-bin form.
+    assert got_tm.sum() > cpu.confocal_voxel(o, cube, lxyz, layout=cpu.LAYOUT_TIME_MAJOR).sum()
+
+
+def test_scatter_oracle_known_answer_and_walk_end():
+    # dist = 1.0 m, voxel diagonal sqrt(0.03) -> ext 0.0866; steps of 0.1 + 1e-5
+    # from 0.9134 visit bins 9 and 10 (the next start, 1.1134, is past 1.0866).
+    o = _info(1, 32, 0.1, (1, 1, 1), (-0.05, -0.55, -0.05), (0.1, 0.1, 0.1))
+    cube = np.zeros((1, 32), np.float32)
+    cube[0, 9], cube[0, 10], cube[0, 11] = 2.0, 3.0, 7.0
+    lx = np.zeros((1, 3), np.float32)
+    assert cpu.confocal_scatter_voxel(o, cube, lx)[0, 0, 0] == pytest.approx(5.0, rel=1e-6)
+    # T = 10: bin 10 is outside the capture, the walk stops there.
+    o.num_time_bins = 10
+    assert cpu.confocal_scatter_voxel(o, np.ascontiguousarray(cube[:, :10]), lx)[0, 0, 0] == pytest.approx(2.0,
+                                                                                                          rel=1e-6)
+
+
 def test_confocal_subset_matches_full():
     rng = np.random.default_rng(3)
     L, T = 16, 128
