@@ -138,3 +138,97 @@ def write_cube(path, vol: np.ndarray) -> None:
 
 def read_cube(path, shape) -> np.ndarray:
     return np.fromfile(path, dtype="<f4").reshape(shape)
+
+
+# ------------------------------------------------------------ HDF5 captures
+
+_HDF5_FIELDS = ("cameraGridPositions", "cameraGridNormals", "cameraPosition", "laserGridNormals",
+                "laserGridPositions", "laserPosition", "t", "t0", "deltaT", "isConfocal", "data")
+
+
+def _grid(raw) -> np.ndarray:
+    """NLosData::setUp(vector<vec3>&, raw[3][W][H]) (NLosData.cpp:205-222):
+    entry x * W + y holds (raw[0][x][y], raw[1][x][y], raw[2][x][y]).  The
+    reference indexes with W for both axes, so only square grids are
+    well-defined there; other shapes are refused."""
+    a = np.asarray(raw, dtype=np.float64)
+    if a.ndim != 3 or a.shape[0] != 3:
+        raise ValueError(f"grid dataset must be 3 x W x H, got {a.shape}")
+    if a.shape[1] != a.shape[2]:
+        raise ValueError(f"non-square grid {a.shape[1]} x {a.shape[2]}: the reference's indexing is undefined")
+    return np.ascontiguousarray(a.astype(np.float32).reshape(3, -1).T)
+
+
+def _vec(raw, n: int, name: str) -> tuple:
+    a = np.asarray(raw, dtype=np.float64).ravel()
+    if a.size != n:
+        raise ValueError(f"{name}: expected {n} values, got {a.size}")  # NLosData.cpp:191-203
+    return tuple(float(np.float32(v)) for v in a)
+
+
+def _sum_bounces(raw: np.ndarray, bounce_axis: int) -> np.ndarray:
+    """data += float(raw) over the bounces in order, in float32
+    (NLosData.cpp:233-242, 256-265, 289-305)."""
+    acc = np.zeros(np.delete(raw.shape, bounce_axis), dtype=np.float32)
+    for b in range(raw.shape[bounce_axis]):
+        acc = (acc + np.take(raw, b, axis=bounce_axis).astype(np.float32)).astype(np.float32)
+    return acc
+
+
+def from_datasets(ds) -> NLosCapture:
+    """The capture NLosData builds from an HDF5 file (NLosData.cpp:28-123,
+    186-308), given its datasets as arrays (a dict, an h5py File, ...):
+    grids flattened x * W + y, positions and sizes to float32, t0 read as an
+    integer, the hidden box from hiddenVolumePosition +- hiddenVolumeSize / 2
+    in float32 (a scalar size means (s, 0.1, s)), and the transient data with
+    its bounces summed, time innermost: confocal [1][T][B][R][C] or
+    [T][B][R][C] -> [R][C][T], exhaustive [1][T][B][lR][lC][cR][cC] ->
+    [lR][lC][cR][cC][T]."""
+    missing = [k for k in _HDF5_FIELDS if k not in ds]
+    if missing:
+        raise ValueError("NLosData: Missing required datasets in the file: " + ", ".join(missing))
+    f32 = np.float32
+    pos = np.asarray(ds["hiddenVolumePosition"], dtype=np.float64).ravel()
+    size = np.asarray(ds["hiddenVolumeSize"], dtype=np.float64)
+    size = np.array([size.item(), 0.1, size.item()]) if size.ndim == 0 or size.size == 1 else size.ravel()
+    hmin = tuple(float(f32(pos[k]) - f32(size[k]) / f32(2.0)) for k in range(3))
+    hmax = tuple(float(f32(pos[k]) + f32(size[k]) / f32(2.0)) for k in range(3))
+    confocal = bool(int(np.asarray(ds["isConfocal"]).item()))
+    raw = np.asarray(ds["data"])
+    if confocal:
+        if raw.ndim == 5:
+            if raw.shape[0] != 1:
+                raise ValueError("NLosData: one channel expected")
+            raw = raw[0]
+        if raw.ndim != 4:
+            raise ValueError("NLosData: Invalid dimensions for confocal data.")
+        T, _, R, C = raw.shape
+        data = np.transpose(_sum_bounces(raw, 1), (1, 2, 0))  # [T][R][C] -> [R][C][T]
+        dims = [R, C, T]
+    else:
+        if raw.ndim != 7 or raw.shape[0] != 1:
+            raise ValueError("NLosData: exhaustive data must be [1][T][B][lR][lC][cR][cC]")
+        _, T, _, lR, lC, cR, cC = raw.shape
+        data = np.transpose(_sum_bounces(raw[0], 1), (1, 2, 3, 4, 0))
+        dims = [lR, lC, cR, cC, T]
+    return NLosCapture(
+        data=np.ascontiguousarray(data, dtype=np.float32).ravel(), dims=dims,
+        camera_grid_positions=_grid(ds["cameraGridPositions"]), camera_grid_normals=_grid(ds["cameraGridNormals"]),
+        camera_position=_vec(ds["cameraPosition"], 3, "cameraPosition"),
+        camera_grid_size=_vec(ds["cameraGridSize"], 2, "cameraGridSize"),
+        laser_grid_positions=_grid(ds["laserGridPositions"]), laser_grid_normals=_grid(ds["laserGridNormals"]),
+        laser_position=_vec(ds["laserPosition"], 3, "laserPosition"),
+        laser_grid_size=_vec(ds["laserGridSize"], 2, "laserGridSize"),
+        hidden_min=hmin, hidden_max=hmax, temporal_resolution=int(np.asarray(ds["t"]).item()),
+        delta_t=float(f32(np.asarray(ds["deltaT"], dtype=np.float64).item())),
+        t0=float(int(np.asarray(ds["t0"]).item())), is_confocal=confocal)
+
+
+def read_hdf5(path) -> NLosCapture:
+    """An HDF5 capture through h5py (when installed) and from_datasets."""
+    try:
+        import h5py
+    except ImportError as e:  # pragma: no cover - depends on the environment
+        raise ImportError("reading HDF5 captures needs h5py; convert once to .nlos elsewhere") from e
+    with h5py.File(path, "r") as f:
+        return from_datasets({k: f[k][()] for k in f.keys()})
