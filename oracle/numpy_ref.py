@@ -238,7 +238,30 @@ def transient_image(slice_, width, height, size, stride=1, offset=0, normalize=F
     return out
 
 
-def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=None) -> np.ndarray:
+def _mis_scatter_walk(cube, l, w, dist, vs, dt, T) -> np.ndarray:
+    """transient_reconstruction.cuh:235-250 for one sample of every voxel:
+    the terms w * I / dist^2 over the walk's bins (I > 1e-5), FP64."""
+    ext = 0.5 * float(np.sqrt(vs @ vs))
+    step = dt + float(np.float32(1e-5))
+    d = np.maximum(0.0, dist - ext)
+    dmax = dist + ext
+    wt = w / (dist * dist)
+    acc = np.zeros(dist.shape[0])
+    alive = d < dmax
+    while alive.any():
+        x = d / dt
+        inside = (x > -1) & (x < T)
+        alive &= inside  # the reference's thread returns at the first bin outside [0, T)
+        b = np.clip(x, 0, T - 1).astype(np.int64)
+        I = np.where(alive, cube[l, b], 0.0)
+        acc += np.where(alive & (I > 1e-5), wt * I, 0.0)
+        d = np.where(alive, d + step, d)
+        alive &= d < dmax
+    return acc
+
+
+def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=None,
+                  scatter: bool = False) -> np.ndarray:
     """Sum over samples s < `samples` of backprojectConfocalVoxelMIS
     (FasterBackprojection/transient_reconstruction.cuh:194-260, without the
     race of its `+=`): voxel v, sample s starts its generator at state v + s
@@ -247,7 +270,13 @@ def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=
     the alias or the uniform proposal with the balance weight, all in float32
     as the kernel does; the term weight * I / dist^2 is summed in FP64.
     bins: [V][L] int32 time bins (the GPU's, from fbp_debug_confocal_bins),
-    else FP64 bins.  cube: [L][T].  Returns vol[Vz][Vy][Vx] float64."""
+    else FP64 bins.  scatter: the ACCUMULATE_VOXEL_SCATTERING build
+    (transient_reconstruction.cuh:235-250): each sample adds every bin of the
+    path d = max(0, dist - ext) .. dist + ext (exclusive, steps of
+    timeStep + EPS, ext = |voxelSize| / 2) until a bin leaves [0, T).
+    cube: [L][T].  Returns vol[Vz][Vy][Vx] float64."""
+    if scatter and bins is not None:
+        raise ValueError("mis_reference: given bins and the scattering walk exclude each other")
     if int(info.discard_first_last_bounces) == 0:
         raise NotImplementedError("mis_reference: bounce terms are not restated here")
     f = np.float32
@@ -291,6 +320,9 @@ def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=
                         (inv_l + spatial_pdf[l]).astype(np.float32)).astype(np.float32)
         w = pdf.astype(np.float64) / gpdf.astype(np.float64)
         dist = 2.0 * np.linalg.norm(p - lx[l], axis=1) - float(info.time_offset)
+        if scatter:
+            out += _mis_scatter_walk(cube, l, w, dist, vs, float(info.time_step), T)
+            continue
         if bins is None:
             b = np.floor(dist / float(info.time_step)).astype(np.int64)
         else:

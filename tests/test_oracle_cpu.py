@@ -355,6 +355,46 @@ def test_alias_tables_reproduce_the_distribution():
     assert cpu.build_alias(np.array([0.5, 0.9], np.float32))[0] == 2  # does not sum to 1
 
 
+def test_mis_scatter_walk_counts_the_steps_of_each_sample():
+    """The scattering MIS oracle (transient_reconstruction.cuh:235-250) with a
+    constant capture and every scan point at one place (so the drawn point
+    does not change the path): per voxel it equals the single-bin MIS term
+    times the number of steps of the walk, counted by a scalar loop."""
+    from oracle import numpy_ref
+
+    rng = np.random.default_rng(12)
+    L, T = 16, 96
+    lxyz = np.tile(np.array([[0.05, 0.0, -0.1]], np.float32), (L, 1))
+    o = _info(L, T, 0.03, (3, 2, 4), (-0.4, -1.0, -0.4), (0.25, 0.05, 0.2))
+    cube = np.full((L, T), 2.0, np.float32)
+    cdf = np.cumsum(rng.uniform(0.5, 1.5, L)).astype(np.float32)
+    cdf /= cdf[-1]
+    rc, alias, prob = cpu.build_alias(cdf)
+    assert rc == 0
+    noise = rng.random(4096).astype(np.float32)
+    one = numpy_ref.mis_reference(o, cube, lxyz, cdf, alias, prob, noise, 3)
+    walk = numpy_ref.mis_reference(o, cube, lxyz, cdf, alias, prob, noise, 3, scatter=True)
+    ext = 0.5 * np.sqrt(sum(float(v) ** 2 for v in o.voxel_size))
+    step = float(o.time_step) + float(np.float32(1e-5))
+    Vx, Vy, Vz = o.voxel_res
+    counts = []
+    for v in range(Vx * Vy * Vz):
+        vz, rem = divmod(v, Vx * Vy)
+        vy, vx = divmod(rem, Vx)
+        p = np.array([o.hidden_min[0] + (vx + 0.5) * o.voxel_size[0], o.hidden_min[1] + (vz + 0.5) * o.voxel_size[1],
+                      o.hidden_min[2] + (vy + 0.5) * o.voxel_size[2]])
+        dist = 2.0 * np.linalg.norm(p - lxyz[0].astype(np.float64))
+        d, k = max(0.0, dist - ext), 0
+        while d < dist + ext and d / float(o.time_step) < T:
+            k, d = k + 1, d + step
+        assert walk.ravel()[v] == pytest.approx(k * one.ravel()[v], rel=1e-12)
+        counts.append(k)
+    assert min(counts) >= 2  # the walk visits several bins
+    with pytest.raises(ValueError):
+        numpy_ref.mis_reference(o, cube, lxyz, cdf, alias, prob, noise, 1, bins=np.zeros((24, L), np.int32),
+                                scatter=True)
+
+
 def test_mlp_oracle_gradient_matches_finite_differences():
     """The oracle's backward pass (exact FP64 mode) against central differences."""
     from oracle import mlp_ref
