@@ -21,6 +21,7 @@ FBP_ERR_TIMEOUT = 4
 FBP_ERR_UNSUPPORTED = 5
 FBP_ERR_DEVICE = 6
 FBP_ERR_IO = 7
+FBP_ERR_INTERNAL = 8
 # fbp_dtype
 FBP_F32, FBP_BF16, FBP_F16 = 0, 1, 2
 # fbp_layout

@@ -300,166 +300,176 @@ fbp_status enqueue_run(fbp_batch* b, cudaStream_t s) {
 using namespace fbp;
 
 extern "C" fbp_status fbp_batch_destroy(fbp_batch* b) {
-    clear_error();
-    if (!b) return FBP_OK;
-    if (b->ctx) cudaSetDevice(b->ctx->device);
-    cudaDeviceSynchronize();
-    drop_graph(b);
-    cudaFree(b->rows);
-    cudaFree(b->scan);
-    cudaFree(b->axes);
-    cudaFree(b->d_params);
-    cudaFree(b->d_items);
-    cudaFree(b->d_counters);
-    for (cudaStream_t st : b->side) cudaStreamDestroy(st);
-    for (cudaEvent_t ev : b->join) cudaEventDestroy(ev);
-    if (b->fork) cudaEventDestroy(b->fork);
-    delete b;
-    return FBP_OK;
+    return guarded("fbp_batch_destroy", [&]() -> fbp_status {
+        clear_error();
+        if (!b) return FBP_OK;
+        if (b->ctx) cudaSetDevice(b->ctx->device);
+        cudaDeviceSynchronize();
+        drop_graph(b);
+        cudaFree(b->rows);
+        cudaFree(b->scan);
+        cudaFree(b->axes);
+        cudaFree(b->d_params);
+        cudaFree(b->d_items);
+        cudaFree(b->d_counters);
+        for (cudaStream_t st : b->side) cudaStreamDestroy(st);
+        for (cudaEvent_t ev : b->join) cudaEventDestroy(ev);
+        if (b->fork) cudaEventDestroy(b->fork);
+        delete b;
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_batch_create(fbp_context* ctx, uint32_t n, const fbp_capture_desc* captures,
                                        fbp_batch** out) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!out || !captures || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: empty batch");
-    *out = nullptr;
-    const int dtype = captures[0].dtype;
-    if (dtype != FBP_F32 && dtype != FBP_BF16 && dtype != FBP_F16)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: unknown dtype");
-    for (uint32_t i = 0; i < n; ++i) {
-        const fbp_capture_desc& c = captures[i];
-        FBP_TRY(validate_info(&c.info, false, "fbp_batch_create"));
-        if (c.dtype != dtype) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: captures must share one dtype");
-        if (!c.cube || !c.laser_xyz || !c.volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: null buffer");
-        if (c.layout != FBP_LAYOUT_TIME_MAJOR && c.layout != FBP_LAYOUT_TIME_INNER)
-            return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: unknown layout");
-    }
-    fbp_batch* b = new (std::nothrow) fbp_batch();
-    if (!b) return set_error(FBP_ERR_OOM, "fbp_batch_create: host allocation failed");
-    b->ctx = ctx;
-    b->caps.assign(captures, captures + n);
-    b->dtype = dtype;
-    auto fail = [&](fbp_status st) {
-        const std::string msg = fbp_last_error();
-        fbp_batch_destroy(b);
-        return set_error(st, msg);
-    };
-    size_t scan_total = 0, axes_total = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        b->scan_off.push_back(scan_total);
-        b->axes_off.push_back(axes_total);
-        scan_total += captures[i].info.num_laser_targets;
-        axes_total += (size_t)captures[i].info.voxel_res[0] + captures[i].info.voxel_res[1] + captures[i].info.voxel_res[2];
-    }
-    cudaStream_t s = nullptr;
-    if (cudaMalloc(&b->scan, scan_total * sizeof(float4)) != cudaSuccess ||
-        cudaMalloc(&b->axes, axes_total * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&b->d_params, n * sizeof(ConfocalGatherParams)) != cudaSuccess ||
-        cudaMalloc(&b->d_counters, kMaxGroups * sizeof(unsigned int)) != cudaSuccess)
-        return fail(set_error(FBP_ERR_OOM, "fbp_batch_create: device allocation failed"));
-    for (uint32_t i = 0; i < n; ++i) {
-        const fbp_recon_info& in = captures[i].info;
-        float4* sc = b->scan + b->scan_off[i];
-        float* ax = b->axes + b->axes_off[i];
-        scan_table_kernel<<<cdiv(in.num_laser_targets, 256), 256, 0, s>>>(
-            sc, captures[i].laser_xyz, in.num_laser_targets, (int)in.discard_first_last_bounces, in.laser_position[0],
-            in.laser_position[1], in.laser_position[2], in.sensor_position[0], in.sensor_position[1],
-            in.sensor_position[2], 1);
-        const uint32_t vmax = std::max(in.voxel_res[0], std::max(in.voxel_res[1], in.voxel_res[2]));
-        axis_tables_kernel<<<cdiv(vmax, 256), 256, 0, s>>>(
-            ax, ax + in.voxel_res[0], ax + in.voxel_res[0] + in.voxel_res[2], in.voxel_res[0], in.voxel_res[1],
-            in.voxel_res[2], in.hidden_min[0], in.hidden_min[1], in.hidden_min[2], in.voxel_size[0], in.voxel_size[1],
-            in.voxel_size[2]);
-        if (cudaGetLastError() != cudaSuccess) return fail(set_error(FBP_ERR_CUDA, "fbp_batch_create: table kernels"));
-        ctx->launches += 2;
-    }
-    fbp_status st = plan_config(b, 0, s);
-    if (st != FBP_OK) return fail(st);
-    *out = b;
-    return FBP_OK;
+    return guarded("fbp_batch_create", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!out || !captures || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: empty batch");
+        *out = nullptr;
+        const int dtype = captures[0].dtype;
+        if (dtype != FBP_F32 && dtype != FBP_BF16 && dtype != FBP_F16)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: unknown dtype");
+        for (uint32_t i = 0; i < n; ++i) {
+            const fbp_capture_desc& c = captures[i];
+            FBP_TRY(validate_info(&c.info, false, "fbp_batch_create"));
+            if (c.dtype != dtype) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: captures must share one dtype");
+            if (!c.cube || !c.laser_xyz || !c.volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: null buffer");
+            if (c.layout != FBP_LAYOUT_TIME_MAJOR && c.layout != FBP_LAYOUT_TIME_INNER)
+                return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_create: unknown layout");
+        }
+        fbp_batch* b = new (std::nothrow) fbp_batch();
+        if (!b) return set_error(FBP_ERR_OOM, "fbp_batch_create: host allocation failed");
+        b->ctx = ctx;
+        b->caps.assign(captures, captures + n);
+        b->dtype = dtype;
+        auto fail = [&](fbp_status st) {
+            const std::string msg = fbp_last_error();
+            fbp_batch_destroy(b);
+            return set_error(st, msg);
+        };
+        size_t scan_total = 0, axes_total = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            b->scan_off.push_back(scan_total);
+            b->axes_off.push_back(axes_total);
+            scan_total += captures[i].info.num_laser_targets;
+            axes_total += (size_t)captures[i].info.voxel_res[0] + captures[i].info.voxel_res[1] + captures[i].info.voxel_res[2];
+        }
+        cudaStream_t s = nullptr;
+        if (cudaMalloc(&b->scan, scan_total * sizeof(float4)) != cudaSuccess ||
+            cudaMalloc(&b->axes, axes_total * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&b->d_params, n * sizeof(ConfocalGatherParams)) != cudaSuccess ||
+            cudaMalloc(&b->d_counters, kMaxGroups * sizeof(unsigned int)) != cudaSuccess)
+            return fail(set_error(FBP_ERR_OOM, "fbp_batch_create: device allocation failed"));
+        for (uint32_t i = 0; i < n; ++i) {
+            const fbp_recon_info& in = captures[i].info;
+            float4* sc = b->scan + b->scan_off[i];
+            float* ax = b->axes + b->axes_off[i];
+            scan_table_kernel<<<cdiv(in.num_laser_targets, 256), 256, 0, s>>>(
+                sc, captures[i].laser_xyz, in.num_laser_targets, (int)in.discard_first_last_bounces, in.laser_position[0],
+                in.laser_position[1], in.laser_position[2], in.sensor_position[0], in.sensor_position[1],
+                in.sensor_position[2], 1);
+            const uint32_t vmax = std::max(in.voxel_res[0], std::max(in.voxel_res[1], in.voxel_res[2]));
+            axis_tables_kernel<<<cdiv(vmax, 256), 256, 0, s>>>(
+                ax, ax + in.voxel_res[0], ax + in.voxel_res[0] + in.voxel_res[2], in.voxel_res[0], in.voxel_res[1],
+                in.voxel_res[2], in.hidden_min[0], in.hidden_min[1], in.hidden_min[2], in.voxel_size[0], in.voxel_size[1],
+                in.voxel_size[2]);
+            if (cudaGetLastError() != cudaSuccess) return fail(set_error(FBP_ERR_CUDA, "fbp_batch_create: table kernels"));
+            ctx->launches += 2;
+        }
+        fbp_status st = plan_config(b, 0, s);
+        if (st != FBP_OK) return fail(st);
+        *out = b;
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_batch_run(fbp_batch* b, int use_graph, void* stream) {
-    clear_error();
-    if (!b) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_run: null batch");
-    FBP_TRY(check_ctx(b->ctx));
-    cudaStream_t s = (cudaStream_t)stream;
-    if (!use_graph) return enqueue_run(b, s);
-    if (s == nullptr)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_run: graph replay needs a non-default stream");
-    if (!b->graph_exec) {
-        FBP_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        const uint64_t launches0 = b->ctx->launches;
-        fbp_status st = enqueue_run(b, s);
-        cudaGraph_t g = nullptr;
-        const cudaError_t e = cudaStreamEndCapture(s, &g);
-        if (st != FBP_OK) {
-            if (g) cudaGraphDestroy(g);
-            return st;
+    return guarded("fbp_batch_run", [&]() -> fbp_status {
+        clear_error();
+        if (!b) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_run: null batch");
+        FBP_TRY(check_ctx(b->ctx));
+        cudaStream_t s = (cudaStream_t)stream;
+        if (!use_graph) return enqueue_run(b, s);
+        if (s == nullptr)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_run: graph replay needs a non-default stream");
+        if (!b->graph_exec) {
+            FBP_TRY_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            const uint64_t launches0 = b->ctx->launches;
+            fbp_status st = enqueue_run(b, s);
+            cudaGraph_t g = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(s, &g);
+            if (st != FBP_OK) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (e != cudaSuccess) return cuda_error(e, "fbp_batch_run: cudaStreamEndCapture");
+            b->graph = g;
+            FBP_TRY_CUDA(cudaGraphInstantiate(&b->graph_exec, g, 0));
+            b->graph_launches = b->ctx->launches - launches0;
+            b->ctx->launches = launches0;  // captured, not launched
         }
-        if (e != cudaSuccess) return cuda_error(e, "fbp_batch_run: cudaStreamEndCapture");
-        b->graph = g;
-        FBP_TRY_CUDA(cudaGraphInstantiate(&b->graph_exec, g, 0));
-        b->graph_launches = b->ctx->launches - launches0;
-        b->ctx->launches = launches0;  // captured, not launched
-    }
-    FBP_TRY_CUDA(cudaGraphLaunch(b->graph_exec, s));
-    b->ctx->launches += b->graph_launches;
-    return FBP_OK;
+        FBP_TRY_CUDA(cudaGraphLaunch(b->graph_exec, s));
+        b->ctx->launches += b->graph_launches;
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_batch_autotune(fbp_batch* b, void* stream, int* chosen) {
-    clear_error();
-    if (!b) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_autotune: null batch");
-    FBP_TRY(check_ctx(b->ctx));
-    cudaStream_t s = (cudaStream_t)stream;
-    cudaEvent_t e0, e1;
-    FBP_TRY_CUDA(cudaEventCreate(&e0));
-    FBP_TRY_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int best_cfg = b->cfg;
-    fbp_status st = FBP_OK;
-    // Each shape: one timed run; short batches are re-run until about 20 ms
-    // are timed (at most 8 runs), so the cost stays near 3 runs for large
-    // batches while small ones still get a stable figure.
-    for (int cfg = 0; cfg < kNumTileCfgs && st == FBP_OK; ++cfg) {
-        st = plan_config(b, cfg, s);
-        if (st != FBP_OK) break;
-        int reps = 1;
-        float ms = 0.f;
-        for (int round = 0; round < 2; ++round) {
-            cudaEventRecord(e0, s);
-            for (int r = 0; r < reps && st == FBP_OK; ++r) st = enqueue_run(b, s);
-            cudaEventRecord(e1, s);
+    return guarded("fbp_batch_autotune", [&]() -> fbp_status {
+        clear_error();
+        if (!b) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_autotune: null batch");
+        FBP_TRY(check_ctx(b->ctx));
+        cudaStream_t s = (cudaStream_t)stream;
+        cudaEvent_t e0, e1;
+        FBP_TRY_CUDA(cudaEventCreate(&e0));
+        FBP_TRY_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int best_cfg = b->cfg;
+        fbp_status st = FBP_OK;
+        // Each shape: one timed run; short batches are re-run until about 20 ms
+        // are timed (at most 8 runs), so the cost stays near 3 runs for large
+        // batches while small ones still get a stable figure.
+        for (int cfg = 0; cfg < kNumTileCfgs && st == FBP_OK; ++cfg) {
+            st = plan_config(b, cfg, s);
             if (st != FBP_OK) break;
-            if (cudaEventSynchronize(e1) != cudaSuccess) {
-                st = set_error(FBP_ERR_CUDA, "fbp_batch_autotune: timing failed");
-                break;
+            int reps = 1;
+            float ms = 0.f;
+            for (int round = 0; round < 2; ++round) {
+                cudaEventRecord(e0, s);
+                for (int r = 0; r < reps && st == FBP_OK; ++r) st = enqueue_run(b, s);
+                cudaEventRecord(e1, s);
+                if (st != FBP_OK) break;
+                if (cudaEventSynchronize(e1) != cudaSuccess) {
+                    st = set_error(FBP_ERR_CUDA, "fbp_batch_autotune: timing failed");
+                    break;
+                }
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= (float)reps;
+                if (ms >= 20.f) break;
+                reps = std::min(8, (int)std::ceil(20.f / std::max(ms, 0.01f)));
             }
-            cudaEventElapsedTime(&ms, e0, e1);
-            ms /= (float)reps;
-            if (ms >= 20.f) break;
-            reps = std::min(8, (int)std::ceil(20.f / std::max(ms, 0.01f)));
+            if (st != FBP_OK) break;
+            if (ms < best) {
+                best = ms;
+                best_cfg = cfg;
+            }
         }
-        if (st != FBP_OK) break;
-        if (ms < best) {
-            best = ms;
-            best_cfg = cfg;
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (st != FBP_OK) return st;
-    FBP_TRY(plan_config(b, best_cfg, s));
-    if (chosen) *chosen = best_cfg;
-    return FBP_OK;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (st != FBP_OK) return st;
+        FBP_TRY(plan_config(b, best_cfg, s));
+        if (chosen) *chosen = best_cfg;
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_batch_set_config(fbp_batch* b, int config, void* stream) {
-    clear_error();
-    if (!b) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_set_config: null batch");
-    if (config < 0 || config >= kNumTileCfgs) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_set_config: bad config");
-    FBP_TRY(check_ctx(b->ctx));
-    return plan_config(b, config, (cudaStream_t)stream);
+    return guarded("fbp_batch_set_config", [&]() -> fbp_status {
+        clear_error();
+        if (!b) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_set_config: null batch");
+        if (config < 0 || config >= kNumTileCfgs) return set_error(FBP_ERR_INVALID_ARG, "fbp_batch_set_config: bad config");
+        FBP_TRY(check_ctx(b->ctx));
+        return plan_config(b, config, (cudaStream_t)stream);
+    });
 }

@@ -364,30 +364,34 @@ using namespace fbp;
 extern "C" fbp_status fbp_backproject_confocal_scatter(fbp_context* ctx, const fbp_recon_info* info,
                                                        const void* cube, int dtype, int layout,
                                                        const float* laser_xyz, float* volume, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, false, "fbp_backproject_confocal_scatter"));
-    if (!cube || !laser_xyz || !volume)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal_scatter: null buffer");
-    if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal_scatter: unknown layout");
-    if (!(info->time_step > 1e-4f))
-        return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_confocal_scatter: time_step must exceed 0.1 mm");
-    return confocal_gather_scatter(ctx, *info, cube, dtype, layout, laser_xyz, volume, (cudaStream_t)stream);
+    return guarded("fbp_backproject_confocal_scatter", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, false, "fbp_backproject_confocal_scatter"));
+        if (!cube || !laser_xyz || !volume)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal_scatter: null buffer");
+        if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal_scatter: unknown layout");
+        if (!(info->time_step > 1e-4f))
+            return set_error(FBP_ERR_UNSUPPORTED, "fbp_backproject_confocal_scatter: time_step must exceed 0.1 mm");
+        return confocal_gather_scatter(ctx, *info, cube, dtype, layout, laser_xyz, volume, (cudaStream_t)stream);
+    });
 }
 
 extern "C" fbp_status fbp_backproject_confocal(fbp_context* ctx, const fbp_recon_info* info, const void* cube,
                                                int dtype, int layout, const float* laser_xyz, float* volume,
                                                void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, false, "fbp_backproject_confocal"));
-    if (!cube || !laser_xyz || !volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: null buffer");
-    if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: unknown layout");
-    if (dtype != FBP_F32 && dtype != FBP_BF16 && dtype != FBP_F16)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: unknown dtype");
-    return confocal_gather(ctx, *info, cube, dtype, layout, laser_xyz, volume, (cudaStream_t)stream, nullptr);
+    return guarded("fbp_backproject_confocal", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, false, "fbp_backproject_confocal"));
+        if (!cube || !laser_xyz || !volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: null buffer");
+        if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: unknown layout");
+        if (dtype != FBP_F32 && dtype != FBP_BF16 && dtype != FBP_F16)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_confocal: unknown dtype");
+        return confocal_gather(ctx, *info, cube, dtype, layout, laser_xyz, volume, (cudaStream_t)stream, nullptr);
+    });
 }
 
 // ------------------------------------------------------------ diagnostics --
@@ -446,48 +450,52 @@ __global__ void debug_exhaustive_bins_kernel(fbp_recon_info in, const float4* __
 extern "C" fbp_status fbp_debug_confocal_bins(fbp_context* ctx, const fbp_recon_info* info, const float* laser_xyz,
                                               const int64_t* voxel_idx, uint64_t num_voxels, int32_t* bins,
                                               void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, false, "fbp_debug_confocal_bins"));
-    if (!laser_xyz || !voxel_idx || !bins) return set_error(FBP_ERR_INVALID_ARG, "fbp_debug_confocal_bins: null buffer");
-    cudaStream_t s = (cudaStream_t)stream;
-    const float4* scan;
-    const float *xs, *ys, *zs;
-    FBP_TRY(build_tables(ctx, *info, laser_xyz, s, &scan, &xs, &ys, &zs));
-    const uint64_t n = num_voxels * info->num_laser_targets;
-    if (n == 0) return FBP_OK;
-    debug_confocal_bins_kernel<<<cdiv(n, 256), 256, 0, s>>>(*info, scan, voxel_idx, num_voxels, bins);
-    FBP_CHECK_LAUNCH(ctx, "debug_confocal_bins_kernel");
-    return FBP_OK;
+    return guarded("fbp_debug_confocal_bins", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, false, "fbp_debug_confocal_bins"));
+        if (!laser_xyz || !voxel_idx || !bins) return set_error(FBP_ERR_INVALID_ARG, "fbp_debug_confocal_bins: null buffer");
+        cudaStream_t s = (cudaStream_t)stream;
+        const float4* scan;
+        const float *xs, *ys, *zs;
+        FBP_TRY(build_tables(ctx, *info, laser_xyz, s, &scan, &xs, &ys, &zs));
+        const uint64_t n = num_voxels * info->num_laser_targets;
+        if (n == 0) return FBP_OK;
+        debug_confocal_bins_kernel<<<cdiv(n, 256), 256, 0, s>>>(*info, scan, voxel_idx, num_voxels, bins);
+        FBP_CHECK_LAUNCH(ctx, "debug_confocal_bins_kernel");
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_debug_exhaustive_bins(fbp_context* ctx, const fbp_recon_info* info, const float* laser_xyz,
                                                 const float* sensor_xyz, const int64_t* voxel_idx, uint64_t num_voxels,
                                                 int32_t* bins, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, true, "fbp_debug_exhaustive_bins"));
-    if (!laser_xyz || !sensor_xyz || !voxel_idx || !bins)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_debug_exhaustive_bins: null buffer");
-    cudaStream_t s = (cudaStream_t)stream;
-    const uint32_t L = info->num_laser_targets, Sn = info->num_sensor_targets;
-    void* lp = nullptr;
-    void* sp = nullptr;
-    FBP_TRY(workspace(ctx, WS_SCAN_TABLE, (size_t)L * sizeof(float4), s, &lp));
-    FBP_TRY(workspace(ctx, WS_SENSOR_TABLE, (size_t)Sn * sizeof(float4), s, &sp));
-    scan_table_kernel<<<cdiv(L, 256), 256, 0, s>>>(static_cast<float4*>(lp), laser_xyz, L,
-                                                  (int)info->discard_first_last_bounces, info->laser_position[0],
-                                                  info->laser_position[1], info->laser_position[2], 0.f, 0.f, 0.f, 0);
-    FBP_CHECK_LAUNCH(ctx, "scan_table_kernel");
-    scan_table_kernel<<<cdiv(Sn, 256), 256, 0, s>>>(static_cast<float4*>(sp), sensor_xyz, Sn,
-                                                   (int)info->discard_first_last_bounces, info->sensor_position[0],
-                                                   info->sensor_position[1], info->sensor_position[2], 0.f, 0.f, 0.f, 0);
-    FBP_CHECK_LAUNCH(ctx, "scan_table_kernel");
-    const uint64_t n = num_voxels * L * Sn;
-    if (n == 0) return FBP_OK;
-    debug_exhaustive_bins_kernel<<<cdiv(n, 256), 256, 0, s>>>(*info, static_cast<const float4*>(lp),
-                                                             static_cast<const float4*>(sp), voxel_idx, num_voxels,
-                                                             bins);
-    FBP_CHECK_LAUNCH(ctx, "debug_exhaustive_bins_kernel");
-    return FBP_OK;
+    return guarded("fbp_debug_exhaustive_bins", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, true, "fbp_debug_exhaustive_bins"));
+        if (!laser_xyz || !sensor_xyz || !voxel_idx || !bins)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_debug_exhaustive_bins: null buffer");
+        cudaStream_t s = (cudaStream_t)stream;
+        const uint32_t L = info->num_laser_targets, Sn = info->num_sensor_targets;
+        void* lp = nullptr;
+        void* sp = nullptr;
+        FBP_TRY(workspace(ctx, WS_SCAN_TABLE, (size_t)L * sizeof(float4), s, &lp));
+        FBP_TRY(workspace(ctx, WS_SENSOR_TABLE, (size_t)Sn * sizeof(float4), s, &sp));
+        scan_table_kernel<<<cdiv(L, 256), 256, 0, s>>>(static_cast<float4*>(lp), laser_xyz, L,
+                                                      (int)info->discard_first_last_bounces, info->laser_position[0],
+                                                      info->laser_position[1], info->laser_position[2], 0.f, 0.f, 0.f, 0);
+        FBP_CHECK_LAUNCH(ctx, "scan_table_kernel");
+        scan_table_kernel<<<cdiv(Sn, 256), 256, 0, s>>>(static_cast<float4*>(sp), sensor_xyz, Sn,
+                                                       (int)info->discard_first_last_bounces, info->sensor_position[0],
+                                                       info->sensor_position[1], info->sensor_position[2], 0.f, 0.f, 0.f, 0);
+        FBP_CHECK_LAUNCH(ctx, "scan_table_kernel");
+        const uint64_t n = num_voxels * L * Sn;
+        if (n == 0) return FBP_OK;
+        debug_exhaustive_bins_kernel<<<cdiv(n, 256), 256, 0, s>>>(*info, static_cast<const float4*>(lp),
+                                                                 static_cast<const float4*>(sp), voxel_idx, num_voxels,
+                                                                 bins);
+        FBP_CHECK_LAUNCH(ctx, "debug_exhaustive_bins_kernel");
+        return FBP_OK;
+    });
 }

@@ -171,29 +171,31 @@ extern "C" fbp_status fbp_backproject_depths(fbp_context* ctx, const fbp_recon_i
                                              int layout, const float* laser_xyz, const float* sensor_xyz,
                                              const double* depths, uint32_t num_depths, float* activation,
                                              void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!info) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: null info");
-    const bool exhaustive = info->capture_system == FBP_EXHAUSTIVE;
-    if (info->capture_system != FBP_CONFOCAL && !exhaustive)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: unknown capture system");
-    if (info->num_laser_targets == 0 || info->num_time_bins == 0 || (exhaustive && info->num_sensor_targets == 0))
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: empty capture");
-    if (!(info->time_step > 0.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: time_step must be > 0");
-    if (!cube || !laser_xyz || !depths || !activation || (exhaustive && !sensor_xyz))
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: null buffer");
-    if (num_depths == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: num_depths == 0");
-    if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: unknown layout");
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (dtype) {
-        case FBP_F32:
-            return launch_depths<float>(ctx, *info, cube, layout, laser_xyz, sensor_xyz, depths, num_depths, activation, s);
-        case FBP_BF16:
-            return launch_depths<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, sensor_xyz, depths, num_depths,
-                                                activation, s);
-        case FBP_F16:
-            return launch_depths<__half>(ctx, *info, cube, layout, laser_xyz, sensor_xyz, depths, num_depths, activation, s);
-        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: unknown dtype");
-    }
+    return guarded("fbp_backproject_depths", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!info) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: null info");
+        const bool exhaustive = info->capture_system == FBP_EXHAUSTIVE;
+        if (info->capture_system != FBP_CONFOCAL && !exhaustive)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: unknown capture system");
+        if (info->num_laser_targets == 0 || info->num_time_bins == 0 || (exhaustive && info->num_sensor_targets == 0))
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: empty capture");
+        if (!(info->time_step > 0.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: time_step must be > 0");
+        if (!cube || !laser_xyz || !depths || !activation || (exhaustive && !sensor_xyz))
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: null buffer");
+        if (num_depths == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: num_depths == 0");
+        if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: unknown layout");
+        cudaStream_t s = (cudaStream_t)stream;
+        switch (dtype) {
+            case FBP_F32:
+                return launch_depths<float>(ctx, *info, cube, layout, laser_xyz, sensor_xyz, depths, num_depths, activation, s);
+            case FBP_BF16:
+                return launch_depths<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, sensor_xyz, depths, num_depths,
+                                                    activation, s);
+            case FBP_F16:
+                return launch_depths<__half>(ctx, *info, cube, layout, laser_xyz, sensor_xyz, depths, num_depths, activation, s);
+            default: return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_depths: unknown dtype");
+        }
+    });
 }

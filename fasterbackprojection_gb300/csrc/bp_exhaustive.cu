@@ -421,16 +421,18 @@ using namespace fbp;
 extern "C" fbp_status fbp_backproject_exhaustive(fbp_context* ctx, const fbp_recon_info* info, const void* cube,
                                                  int dtype, const float* laser_xyz, const float* sensor_xyz,
                                                  float* volume, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, true, "fbp_backproject_exhaustive"));
-    if (!cube || !laser_xyz || !sensor_xyz || !volume)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_exhaustive: null buffer");
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (dtype) {
-        case FBP_F32: return launch_exhaustive<float>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
-        case FBP_BF16: return launch_exhaustive<__nv_bfloat16>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
-        case FBP_F16: return launch_exhaustive<__half>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
-        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_exhaustive: unknown dtype");
-    }
+    return guarded("fbp_backproject_exhaustive", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, true, "fbp_backproject_exhaustive"));
+        if (!cube || !laser_xyz || !sensor_xyz || !volume)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_exhaustive: null buffer");
+        cudaStream_t s = (cudaStream_t)stream;
+        switch (dtype) {
+            case FBP_F32: return launch_exhaustive<float>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
+            case FBP_BF16: return launch_exhaustive<__nv_bfloat16>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
+            case FBP_F16: return launch_exhaustive<__half>(ctx, *info, cube, laser_xyz, sensor_xyz, volume, s);
+            default: return set_error(FBP_ERR_INVALID_ARG, "fbp_backproject_exhaustive: unknown dtype");
+        }
+    });
 }

@@ -6,6 +6,8 @@
 #include <cuda_fp16.h>
 #include <cstdint>
 #include <cstddef>
+#include <exception>
+#include <new>
 #include <string>
 
 #include "../../include/fbp.h"
@@ -18,6 +20,23 @@ namespace fbp {
 fbp_status set_error(fbp_status st, const std::string& msg);
 fbp_status cuda_error(cudaError_t e, const char* what);
 void clear_error();
+
+// The body of a C entry point: no C++ exception may cross the C ABI.  A host
+// allocation failure becomes FBP_ERR_OOM, anything else FBP_ERR_INTERNAL,
+// with the message in fbp_last_error() (when there is memory left to keep it).
+fbp_status fail_quietly(fbp_status st, const char* who, const char* what) noexcept;
+template <typename Body>
+fbp_status guarded(const char* who, Body&& body) noexcept {
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        return fail_quietly(FBP_ERR_OOM, who, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail_quietly(FBP_ERR_INTERNAL, who, e.what());
+    } catch (...) {
+        return fail_quietly(FBP_ERR_INTERNAL, who, "unknown exception");
+    }
+}
 
 #define FBP_TRY_CUDA(expr)                                               \
     do {                                                                 \

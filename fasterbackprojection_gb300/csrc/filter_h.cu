@@ -235,11 +235,13 @@ using namespace fbp;
 
 extern "C" fbp_status fbp_filter_h(fbp_context* ctx, float* data, uint64_t num_series, uint32_t num_bins, float delta_t,
                                    float wl_mean, float wl_sigma, int border, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!data || num_series == 0 || num_bins == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_filter_h: empty input");
-    if (!(delta_t > 0.f) || !(wl_mean > 0.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_filter_h: delta_t and wl_mean must be > 0");
-    if (border != FBP_BORDER_ZERO && border != FBP_BORDER_EDGE)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_filter_h: unknown border mode");
-    return filter_h_device(ctx, data, num_series, num_bins, delta_t, wl_mean, wl_sigma, border, (cudaStream_t)stream);
+    return guarded("fbp_filter_h", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!data || num_series == 0 || num_bins == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_filter_h: empty input");
+        if (!(delta_t > 0.f) || !(wl_mean > 0.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_filter_h: delta_t and wl_mean must be > 0");
+        if (border != FBP_BORDER_ZERO && border != FBP_BORDER_EDGE)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_filter_h: unknown border mode");
+        return filter_h_device(ctx, data, num_series, num_bins, delta_t, wl_mean, wl_sigma, border, (cudaStream_t)stream);
+    });
 }

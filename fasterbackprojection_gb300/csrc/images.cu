@@ -366,67 +366,73 @@ extern "C" fbp_status fbp_transient_images(fbp_context* ctx, const float* data, 
                                            uint32_t num_planes, uint64_t pixel_stride, uint64_t plane_stride,
                                            uint32_t out_width, uint32_t out_height, int normalize, uint8_t* rgba,
                                            void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(check_image_args("fbp_transient_images", data, width, height, num_planes, pixel_stride, plane_stride,
-                             out_width, out_height));
-    if (!rgba) return set_error(FBP_ERR_INVALID_ARG, "fbp_transient_images: null output");
-    return transient_images(ctx, data, width, height, num_planes, pixel_stride, plane_stride, out_width, out_height,
-                            normalize, rgba, (cudaStream_t)stream);
+    return guarded("fbp_transient_images", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(check_image_args("fbp_transient_images", data, width, height, num_planes, pixel_stride, plane_stride,
+                                 out_width, out_height));
+        if (!rgba) return set_error(FBP_ERR_INVALID_ARG, "fbp_transient_images: null output");
+        return transient_images(ctx, data, width, height, num_planes, pixel_stride, plane_stride, out_width, out_height,
+                                normalize, rgba, (cudaStream_t)stream);
+    });
 }
 
 // The encoder indexes the filtered rows with 32-bit positions.
 constexpr uint64_t kPngMaxRaw = (uint64_t)1 << 30;
 
 extern "C" fbp_status fbp_write_png(const char* path, const uint8_t* rgba, uint32_t width, uint32_t height) {
-    clear_error();
-    if (!path || !rgba || width == 0 || height == 0 || width > 65535 || height > 65535)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_write_png: bad arguments");
-    if (((uint64_t)width * 4 + 1) * height > kPngMaxRaw)
-        return set_error(FBP_ERR_UNSUPPORTED, "fbp_write_png: image larger than 1 GiB of pixels");
-    if (!write_file(path, encode_png(rgba, width, height)))
-        return set_error(FBP_ERR_IO, std::string("fbp_write_png: cannot write ") + path);
-    return FBP_OK;
+    return guarded("fbp_write_png", [&]() -> fbp_status {
+        clear_error();
+        if (!path || !rgba || width == 0 || height == 0 || width > 65535 || height > 65535)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_write_png: bad arguments");
+        if (((uint64_t)width * 4 + 1) * height > kPngMaxRaw)
+            return set_error(FBP_ERR_UNSUPPORTED, "fbp_write_png: image larger than 1 GiB of pixels");
+        if (!write_file(path, encode_png(rgba, width, height)))
+            return set_error(FBP_ERR_IO, std::string("fbp_write_png: cannot write ") + path);
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_save_transient_images(fbp_context* ctx, const float* data, uint32_t width, uint32_t height,
                                                 uint32_t num_planes, uint64_t pixel_stride, uint64_t plane_stride,
                                                 uint32_t out_width, uint32_t out_height, int normalize,
                                                 const char* prefix, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(check_image_args("fbp_save_transient_images", data, width, height, num_planes, pixel_stride, plane_stride,
-                             out_width, out_height));
-    if (!prefix) return set_error(FBP_ERR_INVALID_ARG, "fbp_save_transient_images: null prefix");
-    if (((uint64_t)out_width * 4 + 1) * out_height > kPngMaxRaw)
-        return set_error(FBP_ERR_UNSUPPORTED, "fbp_save_transient_images: image larger than 1 GiB of pixels");
-    const uint32_t num_depths = num_planes;
-    cudaStream_t s = (cudaStream_t)stream;
-    const size_t plane = (size_t)out_width * out_height * 4, bytes = plane * num_depths;
-    void* dev = nullptr;
-    FBP_TRY(workspace(ctx, WS_MISC, bytes, s, &dev));
-    FBP_TRY(transient_images(ctx, data, width, height, num_planes, pixel_stride, plane_stride, out_width, out_height,
-                             normalize, static_cast<uint8_t*>(dev), s));
-    std::vector<uint8_t> host(bytes);
-    FBP_TRY_CUDA(cudaMemcpyAsync(host.data(), dev, bytes, cudaMemcpyDeviceToHost, s));
-    FBP_TRY_CUDA(cudaStreamSynchronize(s));
-    FBP_TRY(fbp_check_device_status(ctx, stream));
-    // Laser.cu:419-423, NLosData.cpp:172-178: "<prefix>transient_<p>.png", one
-    // file per plane, in parallel.
-    const unsigned nthreads = std::max(1u, std::min(num_depths, std::thread::hardware_concurrency()));
-    std::vector<int> failed(num_depths, 0);
-    std::vector<std::thread> pool;
-    for (unsigned t = 0; t < nthreads; ++t)
-        pool.emplace_back([&, t] {
-            for (uint32_t d = t; d < num_depths; d += nthreads) {
-                const std::string path = std::string(prefix) + "transient_" + std::to_string(d) + ".png";
-                failed[d] = !write_file(path, encode_png(host.data() + d * plane, out_width, out_height));
-            }
-        });
-    for (auto& th : pool) th.join();
-    for (uint32_t d = 0; d < num_depths; ++d)
-        if (failed[d])
-            return set_error(FBP_ERR_IO, std::string("fbp_save_transient_images: cannot write ") + prefix + "transient_" +
-                                             std::to_string(d) + ".png");
-    return FBP_OK;
+    return guarded("fbp_save_transient_images", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(check_image_args("fbp_save_transient_images", data, width, height, num_planes, pixel_stride, plane_stride,
+                                 out_width, out_height));
+        if (!prefix) return set_error(FBP_ERR_INVALID_ARG, "fbp_save_transient_images: null prefix");
+        if (((uint64_t)out_width * 4 + 1) * out_height > kPngMaxRaw)
+            return set_error(FBP_ERR_UNSUPPORTED, "fbp_save_transient_images: image larger than 1 GiB of pixels");
+        const uint32_t num_depths = num_planes;
+        cudaStream_t s = (cudaStream_t)stream;
+        const size_t plane = (size_t)out_width * out_height * 4, bytes = plane * num_depths;
+        void* dev = nullptr;
+        FBP_TRY(workspace(ctx, WS_MISC, bytes, s, &dev));
+        FBP_TRY(transient_images(ctx, data, width, height, num_planes, pixel_stride, plane_stride, out_width, out_height,
+                                 normalize, static_cast<uint8_t*>(dev), s));
+        std::vector<uint8_t> host(bytes);
+        FBP_TRY_CUDA(cudaMemcpyAsync(host.data(), dev, bytes, cudaMemcpyDeviceToHost, s));
+        FBP_TRY_CUDA(cudaStreamSynchronize(s));
+        FBP_TRY(fbp_check_device_status(ctx, stream));
+        // Laser.cu:419-423, NLosData.cpp:172-178: "<prefix>transient_<p>.png", one
+        // file per plane, in parallel.
+        const unsigned nthreads = std::max(1u, std::min(num_depths, std::thread::hardware_concurrency()));
+        std::vector<int> failed(num_depths, 0);
+        std::vector<std::thread> pool;
+        for (unsigned t = 0; t < nthreads; ++t)
+            pool.emplace_back([&, t] {
+                for (uint32_t d = t; d < num_depths; d += nthreads) {
+                    const std::string path = std::string(prefix) + "transient_" + std::to_string(d) + ".png";
+                    failed[d] = !write_file(path, encode_png(host.data() + d * plane, out_width, out_height));
+                }
+            });
+        for (auto& th : pool) th.join();
+        for (uint32_t d = 0; d < num_depths; ++d)
+            if (failed[d])
+                return set_error(FBP_ERR_IO, std::string("fbp_save_transient_images: cannot write ") + prefix + "transient_" +
+                                                 std::to_string(d) + ".png");
+        return FBP_OK;
+    });
 }

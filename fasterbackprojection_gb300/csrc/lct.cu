@@ -337,12 +337,14 @@ using namespace fbp;
 
 extern "C" fbp_status fbp_lct(fbp_context* ctx, const float* data, int layout, uint32_t N, uint32_t M,
                               const fbp_lct_params* params, float* volume, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!data || !params || !volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: null argument");
-    if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: unknown layout");
-    if (params->grid_mode != FBP_LCT_GRID_REFERENCE && params->grid_mode != FBP_LCT_GRID_DEPTH)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: unknown grid mode");
-    return lct_run(ctx, data, layout, N, M, *params, volume, (cudaStream_t)stream);
+    return guarded("fbp_lct", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!data || !params || !volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: null argument");
+        if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: unknown layout");
+        if (params->grid_mode != FBP_LCT_GRID_REFERENCE && params->grid_mode != FBP_LCT_GRID_DEPTH)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: unknown grid mode");
+        return lct_run(ctx, data, layout, N, M, *params, volume, (cudaStream_t)stream);
+    });
 }

@@ -551,42 +551,48 @@ static fbp_status tables_run(fbp_context* ctx, const fbp_recon_info& in, const v
 extern "C" fbp_status fbp_mis_reference_tables(fbp_context* ctx, const fbp_recon_info* info, const void* cube,
                                                int dtype, int layout, float* spatial_cdf, uint32_t* alias, float* prob,
                                                void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, false, "fbp_mis_reference_tables"));
-    if (!cube || !spatial_cdf || !alias || !prob)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_reference_tables: null argument");
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (dtype) {
-        case FBP_F32: return tables_run<float>(ctx, *info, cube, layout, spatial_cdf, alias, prob, s);
-        case FBP_BF16: return tables_run<__nv_bfloat16>(ctx, *info, cube, layout, spatial_cdf, alias, prob, s);
-        case FBP_F16: return tables_run<__half>(ctx, *info, cube, layout, spatial_cdf, alias, prob, s);
-        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_reference_tables: unknown dtype");
-    }
+    return guarded("fbp_mis_reference_tables", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, false, "fbp_mis_reference_tables"));
+        if (!cube || !spatial_cdf || !alias || !prob)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_reference_tables: null argument");
+        cudaStream_t s = (cudaStream_t)stream;
+        switch (dtype) {
+            case FBP_F32: return tables_run<float>(ctx, *info, cube, layout, spatial_cdf, alias, prob, s);
+            case FBP_BF16: return tables_run<__nv_bfloat16>(ctx, *info, cube, layout, spatial_cdf, alias, prob, s);
+            case FBP_F16: return tables_run<__half>(ctx, *info, cube, layout, spatial_cdf, alias, prob, s);
+            default: return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_reference_tables: unknown dtype");
+        }
+    });
 }
 
 extern "C" fbp_status fbp_mis_tile_grid(const fbp_recon_info* info, uint32_t tiles[3]) {
-    clear_error();
-    if (!info || !tiles) return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_tile_grid: null argument");
-    confocal_tile_grid(*info, tiles);
-    return FBP_OK;
+    return guarded("fbp_mis_tile_grid", [&]() -> fbp_status {
+        clear_error();
+        if (!info || !tiles) return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_tile_grid: null argument");
+        confocal_tile_grid(*info, tiles);
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_mis_backproject(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
                                           int layout, const float* laser_xyz, const fbp_mis_params* params,
                                           float* volume, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, false, "fbp_mis_backproject"));
-    if (!cube || !laser_xyz || !params || !volume)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: null argument");
-    if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: unknown layout");
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (dtype) {
-        case FBP_F32: return mis_run<float>(ctx, *info, cube, layout, laser_xyz, *params, volume, s);
-        case FBP_BF16: return mis_run<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, *params, volume, s);
-        case FBP_F16: return mis_run<__half>(ctx, *info, cube, layout, laser_xyz, *params, volume, s);
-        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: unknown dtype");
-    }
+    return guarded("fbp_mis_backproject", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, false, "fbp_mis_backproject"));
+        if (!cube || !laser_xyz || !params || !volume)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: null argument");
+        if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: unknown layout");
+        cudaStream_t s = (cudaStream_t)stream;
+        switch (dtype) {
+            case FBP_F32: return mis_run<float>(ctx, *info, cube, layout, laser_xyz, *params, volume, s);
+            case FBP_BF16: return mis_run<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, *params, volume, s);
+            case FBP_F16: return mis_run<__half>(ctx, *info, cube, layout, laser_xyz, *params, volume, s);
+            default: return set_error(FBP_ERR_INVALID_ARG, "fbp_mis_backproject: unknown dtype");
+        }
+    });
 }

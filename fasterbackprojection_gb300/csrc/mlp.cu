@@ -911,147 +911,161 @@ using namespace fbp::mlp;
 extern "C" uint32_t fbp_mlp_num_params(void) { return (uint32_t)NPARAM; }
 
 extern "C" fbp_status fbp_mlp_create(fbp_context* ctx, uint64_t seed, fbp_mlp** out) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!out) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_create: null output");
-    *out = nullptr;
-    fbp_mlp* m = new (std::nothrow) fbp_mlp();
-    if (!m) return set_error(FBP_ERR_OOM, "fbp_mlp_create: host allocation failed");
-    m->ctx = ctx;
-    const size_t bytes = (size_t)NPARAM * sizeof(float);
-    if (cudaMalloc(&m->params, bytes) != cudaSuccess || cudaMalloc(&m->adam_m, bytes) != cudaSuccess ||
-        cudaMalloc(&m->adam_v, bytes) != cudaSuccess || cudaMalloc(&m->grad, bytes + sizeof(float)) != cudaSuccess) {
+    return guarded("fbp_mlp_create", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!out) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_create: null output");
+        *out = nullptr;
+        fbp_mlp* m = new (std::nothrow) fbp_mlp();
+        if (!m) return set_error(FBP_ERR_OOM, "fbp_mlp_create: host allocation failed");
+        m->ctx = ctx;
+        const size_t bytes = (size_t)NPARAM * sizeof(float);
+        if (cudaMalloc(&m->params, bytes) != cudaSuccess || cudaMalloc(&m->adam_m, bytes) != cudaSuccess ||
+            cudaMalloc(&m->adam_v, bytes) != cudaSuccess || cudaMalloc(&m->grad, bytes + sizeof(float)) != cudaSuccess) {
+            cudaFree(m->params);
+            cudaFree(m->adam_m);
+            cudaFree(m->adam_v);
+            cudaFree(m->grad);
+            delete m;
+            return set_error(FBP_ERR_OOM, "fbp_mlp_create: device allocation failed");
+        }
+        // Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases; the
+        // padded input columns of layer 1 stay zero.
+        std::vector<float> h(NPARAM, 0.f);
+        std::mt19937_64 rng(seed);
+        auto fill = [&](int off, int rows, int cols, int used, float bound) {
+            std::uniform_real_distribution<float> u(-bound, bound);
+            for (int r = 0; r < rows; ++r)
+                for (int c = 0; c < cols; ++c) h[off + r * cols + c] = c < used ? u(rng) : 0.f;
+        };
+        fill(OW1, H, IN_PAD, IN, 1.f / std::sqrt((float)IN));
+        fill(OW2, H, H, H, 1.f / std::sqrt((float)H));
+        fill(OW3, H, H, H, 1.f / std::sqrt((float)H));
+        fill(OW4, 1, H, H, 1.f / std::sqrt((float)H));
+        cudaMemcpy(m->params, h.data(), bytes, cudaMemcpyHostToDevice);
+        cudaMemset(m->adam_m, 0, bytes);
+        cudaMemset(m->adam_v, 0, bytes);
+        if (cudaGetLastError() != cudaSuccess) {
+            fbp_mlp_destroy(m);
+            return set_error(FBP_ERR_CUDA, "fbp_mlp_create: initialisation failed");
+        }
+        *out = m;
+        return FBP_OK;
+    });
+}
+
+extern "C" fbp_status fbp_mlp_destroy(fbp_mlp* m) {
+    return guarded("fbp_mlp_destroy", [&]() -> fbp_status {
+        clear_error();
+        if (!m) return FBP_OK;
         cudaFree(m->params);
         cudaFree(m->adam_m);
         cudaFree(m->adam_v);
         cudaFree(m->grad);
         delete m;
-        return set_error(FBP_ERR_OOM, "fbp_mlp_create: device allocation failed");
-    }
-    // Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases; the
-    // padded input columns of layer 1 stay zero.
-    std::vector<float> h(NPARAM, 0.f);
-    std::mt19937_64 rng(seed);
-    auto fill = [&](int off, int rows, int cols, int used, float bound) {
-        std::uniform_real_distribution<float> u(-bound, bound);
-        for (int r = 0; r < rows; ++r)
-            for (int c = 0; c < cols; ++c) h[off + r * cols + c] = c < used ? u(rng) : 0.f;
-    };
-    fill(OW1, H, IN_PAD, IN, 1.f / std::sqrt((float)IN));
-    fill(OW2, H, H, H, 1.f / std::sqrt((float)H));
-    fill(OW3, H, H, H, 1.f / std::sqrt((float)H));
-    fill(OW4, 1, H, H, 1.f / std::sqrt((float)H));
-    cudaMemcpy(m->params, h.data(), bytes, cudaMemcpyHostToDevice);
-    cudaMemset(m->adam_m, 0, bytes);
-    cudaMemset(m->adam_v, 0, bytes);
-    if (cudaGetLastError() != cudaSuccess) {
-        fbp_mlp_destroy(m);
-        return set_error(FBP_ERR_CUDA, "fbp_mlp_create: initialisation failed");
-    }
-    *out = m;
-    return FBP_OK;
-}
-
-extern "C" fbp_status fbp_mlp_destroy(fbp_mlp* m) {
-    clear_error();
-    if (!m) return FBP_OK;
-    cudaFree(m->params);
-    cudaFree(m->adam_m);
-    cudaFree(m->adam_v);
-    cudaFree(m->grad);
-    delete m;
-    return FBP_OK;
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_mlp_get_params(const fbp_mlp* m, float* host, uint32_t n) {
-    clear_error();
-    if (!m || !host || n != (uint32_t)NPARAM) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_get_params: bad arguments");
-    FBP_TRY_CUDA(cudaMemcpy(host, m->params, n * sizeof(float), cudaMemcpyDeviceToHost));
-    return FBP_OK;
+    return guarded("fbp_mlp_get_params", [&]() -> fbp_status {
+        clear_error();
+        if (!m || !host || n != (uint32_t)NPARAM) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_get_params: bad arguments");
+        FBP_TRY_CUDA(cudaMemcpy(host, m->params, n * sizeof(float), cudaMemcpyDeviceToHost));
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_mlp_set_params(fbp_mlp* m, const float* host, uint32_t n) {
-    clear_error();
-    if (!m || !host || n != (uint32_t)NPARAM) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_set_params: bad arguments");
-    FBP_TRY_CUDA(cudaMemcpy(m->params, host, n * sizeof(float), cudaMemcpyHostToDevice));
-    FBP_TRY_CUDA(cudaMemset(m->adam_m, 0, n * sizeof(float)));
-    FBP_TRY_CUDA(cudaMemset(m->adam_v, 0, n * sizeof(float)));
-    m->step = 0;
-    return FBP_OK;
+    return guarded("fbp_mlp_set_params", [&]() -> fbp_status {
+        clear_error();
+        if (!m || !host || n != (uint32_t)NPARAM) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_set_params: bad arguments");
+        FBP_TRY_CUDA(cudaMemcpy(m->params, host, n * sizeof(float), cudaMemcpyHostToDevice));
+        FBP_TRY_CUDA(cudaMemset(m->adam_m, 0, n * sizeof(float)));
+        FBP_TRY_CUDA(cudaMemset(m->adam_v, 0, n * sizeof(float)));
+        m->step = 0;
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_mlp_features(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
                                        int layout, const float* laser_xyz, uint32_t cluster_side, uint32_t scan_side,
                                        const uint32_t* tiles, uint32_t ntiles, float* features, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_capture(info, cube, dtype, layout, laser_xyz, "fbp_mlp_features"));
-    ClusterGeo cg;
-    FBP_TRY(check_clusters(info, cluster_side, scan_side, &cg, "fbp_mlp_features"));
-    if (!features) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_features: null output");
-    const uint64_t nt = tiles ? ntiles : num_tiles(*info);
-    if (nt == 0) return FBP_OK;
-    if (nt > 0x7FFFFFFFull) return set_error(FBP_ERR_UNSUPPORTED, "fbp_mlp_features: too many tiles");
-    cudaStream_t s = (cudaStream_t)stream;
-    float *prof, *mean;
-    float4* centre;
-    uint32_t J;
-    switch (dtype) {
-        case FBP_F32: FBP_TRY(profiles_typed<float>(ctx, *info, cube, layout, laser_xyz, cg, s, &prof, &centre, &mean, &J)); break;
-        case FBP_BF16: FBP_TRY(profiles_typed<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, cg, s, &prof, &centre, &mean, &J)); break;
-        default: FBP_TRY(profiles_typed<__half>(ctx, *info, cube, layout, laser_xyz, cg, s, &prof, &centre, &mean, &J)); break;
-    }
-    features_kernel<<<(unsigned)nt, 256, 0, s>>>(prof, centre, mean, cg.G, J, tile_geo(*info),
-                                                 (uint32_t)num_tiles(*info), tiles, features, ctx->status_dev);
-    FBP_CHECK_LAUNCH(ctx, "features_kernel");
-    return FBP_OK;
+    return guarded("fbp_mlp_features", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_capture(info, cube, dtype, layout, laser_xyz, "fbp_mlp_features"));
+        ClusterGeo cg;
+        FBP_TRY(check_clusters(info, cluster_side, scan_side, &cg, "fbp_mlp_features"));
+        if (!features) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_features: null output");
+        const uint64_t nt = tiles ? ntiles : num_tiles(*info);
+        if (nt == 0) return FBP_OK;
+        if (nt > 0x7FFFFFFFull) return set_error(FBP_ERR_UNSUPPORTED, "fbp_mlp_features: too many tiles");
+        cudaStream_t s = (cudaStream_t)stream;
+        float *prof, *mean;
+        float4* centre;
+        uint32_t J;
+        switch (dtype) {
+            case FBP_F32: FBP_TRY(profiles_typed<float>(ctx, *info, cube, layout, laser_xyz, cg, s, &prof, &centre, &mean, &J)); break;
+            case FBP_BF16: FBP_TRY(profiles_typed<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, cg, s, &prof, &centre, &mean, &J)); break;
+            default: FBP_TRY(profiles_typed<__half>(ctx, *info, cube, layout, laser_xyz, cg, s, &prof, &centre, &mean, &J)); break;
+        }
+        features_kernel<<<(unsigned)nt, 256, 0, s>>>(prof, centre, mean, cg.G, J, tile_geo(*info),
+                                                     (uint32_t)num_tiles(*info), tiles, features, ctx->status_dev);
+        FBP_CHECK_LAUNCH(ctx, "features_kernel");
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_mlp_labels(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
                                      int layout, const float* laser_xyz, uint32_t cluster_side, uint32_t scan_side,
                                      const uint32_t* tiles, uint32_t ntiles, float* labels, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_capture(info, cube, dtype, layout, laser_xyz, "fbp_mlp_labels"));
-    ClusterGeo cg;
-    FBP_TRY(check_clusters(info, cluster_side, scan_side, &cg, "fbp_mlp_labels"));
-    if (!tiles || !labels) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_labels: null tiles or output");
-    if (ntiles == 0) return FBP_OK;
-    cudaStream_t s = (cudaStream_t)stream;
-    const float4* scan;
-    const float *xs, *ys, *zs;
-    FBP_TRY(build_tables(ctx, *info, laser_xyz, s, &scan, &xs, &ys, &zs));
-    const uint32_t gx = cdiv(info->voxel_res[0], 8), gy = cdiv(info->voxel_res[1], 16);
-    const uint32_t nall = (uint32_t)std::min<uint64_t>(num_tiles(*info), 0xFFFFFFFFull);
-    const int tm = layout == FBP_LAYOUT_TIME_MAJOR;
-    switch (dtype) {
-        case FBP_F32:
-            labels_kernel<float><<<ntiles, 256, 0, s>>>(static_cast<const float*>(cube), tm, *info, scan, cg, gx, gy, nall, tiles, labels, ctx->status_dev);
-            break;
-        case FBP_BF16:
-            labels_kernel<__nv_bfloat16><<<ntiles, 256, 0, s>>>(static_cast<const __nv_bfloat16*>(cube), tm, *info, scan, cg, gx, gy, nall, tiles, labels, ctx->status_dev);
-            break;
-        default:
-            labels_kernel<__half><<<ntiles, 256, 0, s>>>(static_cast<const __half*>(cube), tm, *info, scan, cg, gx, gy, nall, tiles, labels, ctx->status_dev);
-            break;
-    }
-    FBP_CHECK_LAUNCH(ctx, "labels_kernel");
-    return FBP_OK;
+    return guarded("fbp_mlp_labels", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_capture(info, cube, dtype, layout, laser_xyz, "fbp_mlp_labels"));
+        ClusterGeo cg;
+        FBP_TRY(check_clusters(info, cluster_side, scan_side, &cg, "fbp_mlp_labels"));
+        if (!tiles || !labels) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_labels: null tiles or output");
+        if (ntiles == 0) return FBP_OK;
+        cudaStream_t s = (cudaStream_t)stream;
+        const float4* scan;
+        const float *xs, *ys, *zs;
+        FBP_TRY(build_tables(ctx, *info, laser_xyz, s, &scan, &xs, &ys, &zs));
+        const uint32_t gx = cdiv(info->voxel_res[0], 8), gy = cdiv(info->voxel_res[1], 16);
+        const uint32_t nall = (uint32_t)std::min<uint64_t>(num_tiles(*info), 0xFFFFFFFFull);
+        const int tm = layout == FBP_LAYOUT_TIME_MAJOR;
+        switch (dtype) {
+            case FBP_F32:
+                labels_kernel<float><<<ntiles, 256, 0, s>>>(static_cast<const float*>(cube), tm, *info, scan, cg, gx, gy, nall, tiles, labels, ctx->status_dev);
+                break;
+            case FBP_BF16:
+                labels_kernel<__nv_bfloat16><<<ntiles, 256, 0, s>>>(static_cast<const __nv_bfloat16*>(cube), tm, *info, scan, cg, gx, gy, nall, tiles, labels, ctx->status_dev);
+                break;
+            default:
+                labels_kernel<__half><<<ntiles, 256, 0, s>>>(static_cast<const __half*>(cube), tm, *info, scan, cg, gx, gy, nall, tiles, labels, ctx->status_dev);
+                break;
+        }
+        FBP_CHECK_LAUNCH(ctx, "labels_kernel");
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_mlp_forward(fbp_context* ctx, const fbp_mlp* m, const float* features, uint32_t ntiles,
                                       uint32_t G, float* logits, float defensive, float* tile_cdf, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!m || !features || (!logits && !tile_cdf)) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_forward: null argument");
-    if (G == 0 || G > (uint32_t)MAXG) return set_error(FBP_ERR_UNSUPPORTED, "fbp_mlp_forward: G must be in 1..1024");
-    if (!(defensive >= 0.f && defensive <= 1.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_forward: defensive share not in [0, 1]");
-    if (ntiles == 0) return FBP_OK;
-    FBP_TRY(set_smem((const void*)mlp_infer_kernel, SI_BYTES));
-    mlp_infer_kernel<<<ntiles, NTH, SI_BYTES, (cudaStream_t)stream>>>(m->params, features, G, defensive, logits,
-                                                                       tile_cdf, ctx->status_dev);
-    FBP_CHECK_LAUNCH(ctx, "mlp_infer_kernel");
-    return FBP_OK;
+    return guarded("fbp_mlp_forward", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!m || !features || (!logits && !tile_cdf)) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_forward: null argument");
+        if (G == 0 || G > (uint32_t)MAXG) return set_error(FBP_ERR_UNSUPPORTED, "fbp_mlp_forward: G must be in 1..1024");
+        if (!(defensive >= 0.f && defensive <= 1.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_forward: defensive share not in [0, 1]");
+        if (ntiles == 0) return FBP_OK;
+        FBP_TRY(set_smem((const void*)mlp_infer_kernel, SI_BYTES));
+        mlp_infer_kernel<<<ntiles, NTH, SI_BYTES, (cudaStream_t)stream>>>(m->params, features, G, defensive, logits,
+                                                                           tile_cdf, ctx->status_dev);
+        FBP_CHECK_LAUNCH(ctx, "mlp_infer_kernel");
+        return FBP_OK;
+    });
 }
 
 namespace {
@@ -1077,36 +1091,42 @@ fbp_status gradients(fbp_context* ctx, const fbp_mlp* m, const float* features, 
 extern "C" fbp_status fbp_mlp_gradients(fbp_context* ctx, const fbp_mlp* m, const float* features,
                                         const float* labels, const uint32_t* idx, uint32_t nbatch, uint32_t G,
                                         float* grad_loss, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!m) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_gradients: null network");
-    return gradients(ctx, m, features, labels, idx, nbatch, G, grad_loss, (cudaStream_t)stream);
+    return guarded("fbp_mlp_gradients", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!m) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_gradients: null network");
+        return gradients(ctx, m, features, labels, idx, nbatch, G, grad_loss, (cudaStream_t)stream);
+    });
 }
 
 extern "C" fbp_status fbp_mlp_train_step(fbp_context* ctx, fbp_mlp* m, const float* features, const float* labels,
                                          const uint32_t* idx, uint32_t nbatch, uint32_t G, float lr, float* loss,
                                          void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!m) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_train_step: null network");
-    if (!(lr > 0.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_train_step: learning rate must be > 0");
-    cudaStream_t s = (cudaStream_t)stream;
-    FBP_TRY(gradients(ctx, m, features, labels, idx, nbatch, G, m->grad, s));
-    m->step += 1;
-    const float b1 = 0.9f, b2 = 0.999f;
-    const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, (double)m->step)));
-    const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, (double)m->step)));
-    adam_kernel<<<cdiv(NPARAM, 256), 256, 0, s>>>(m->params, m->adam_m, m->adam_v, m->grad, lr, b1, b2, 1e-8f, c1, c2);
-    FBP_CHECK_LAUNCH(ctx, "adam_kernel");
-    if (loss) FBP_TRY_CUDA(cudaMemcpyAsync(loss, m->grad + NPARAM, sizeof(float), cudaMemcpyDeviceToDevice, s));
-    return FBP_OK;
+    return guarded("fbp_mlp_train_step", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!m) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_train_step: null network");
+        if (!(lr > 0.f)) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_train_step: learning rate must be > 0");
+        cudaStream_t s = (cudaStream_t)stream;
+        FBP_TRY(gradients(ctx, m, features, labels, idx, nbatch, G, m->grad, s));
+        m->step += 1;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = (float)(1.0 / (1.0 - std::pow((double)b1, (double)m->step)));
+        const float c2 = (float)(1.0 / (1.0 - std::pow((double)b2, (double)m->step)));
+        adam_kernel<<<cdiv(NPARAM, 256), 256, 0, s>>>(m->params, m->adam_m, m->adam_v, m->grad, lr, b1, b2, 1e-8f, c1, c2);
+        FBP_CHECK_LAUNCH(ctx, "adam_kernel");
+        if (loss) FBP_TRY_CUDA(cudaMemcpyAsync(loss, m->grad + NPARAM, sizeof(float), cudaMemcpyDeviceToDevice, s));
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_mlp_tile_count(const fbp_recon_info* info, uint32_t* ntiles) {
-    clear_error();
-    if (!info || !ntiles) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_tile_count: null argument");
-    const uint64_t n = num_tiles(*info);
-    if (n > 0xFFFFFFFFull) return set_error(FBP_ERR_UNSUPPORTED, "fbp_mlp_tile_count: too many tiles");
-    *ntiles = (uint32_t)n;
-    return FBP_OK;
+    return guarded("fbp_mlp_tile_count", [&]() -> fbp_status {
+        clear_error();
+        if (!info || !ntiles) return set_error(FBP_ERR_INVALID_ARG, "fbp_mlp_tile_count: null argument");
+        const uint64_t n = num_tiles(*info);
+        if (n > 0xFFFFFFFFull) return set_error(FBP_ERR_UNSUPPORTED, "fbp_mlp_tile_count: too many tiles");
+        *ntiles = (uint32_t)n;
+        return FBP_OK;
+    });
 }

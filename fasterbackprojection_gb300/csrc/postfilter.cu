@@ -458,15 +458,19 @@ fbp_status launch_laplacian(fbp_context* ctx, const float* in, float* out, uint3
 using namespace fbp;
 
 extern "C" fbp_status fbp_log_weights(int size, float sigma, float* w) {
-    clear_error();
-    return log_weights_host(size, sigma, w);
+    return guarded("fbp_log_weights", [&]() -> fbp_status {
+        clear_error();
+        return log_weights_host(size, sigma, w);
+    });
 }
 
 extern "C" fbp_status fbp_normalize_minmax(fbp_context* ctx, float* v, uint64_t n, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!v || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_normalize_minmax: null buffer or n == 0");
-    return normalize_device(ctx, v, n, (cudaStream_t)stream);
+    return guarded("fbp_normalize_minmax", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!v || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_normalize_minmax: null buffer or n == 0");
+        return normalize_device(ctx, v, n, (cudaStream_t)stream);
+    });
 }
 
 // ------------------------------------------ allocation-free normalisation --
@@ -510,44 +514,48 @@ static fbp_status noalloc_scratch(float** out) {
 }  // namespace fbp
 
 extern "C" fbp_status fbp_normalize_minmax_noalloc(float* v, uint64_t n, void* stream) {
-    clear_error();
-    if (!v || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_normalize_minmax_noalloc: null buffer or n == 0");
-    if (n > (uint64_t)kNoAllocMaxBlocks * kNoAllocElemsPerBlock)
-        return set_error(FBP_ERR_UNSUPPORTED,
-                         "fbp_normalize_minmax_noalloc: n exceeds 2^30 elements (the static scratch holds 1024 "
-                         "partial min/max pairs of 2^20 elements each); use fbp_normalize_minmax");
-    float* scratch = nullptr;
-    FBP_TRY(noalloc_scratch(&scratch));
-    cudaStream_t s = (cudaStream_t)stream;
-    const int nb = (int)((n + kNoAllocElemsPerBlock - 1) / kNoAllocElemsPerBlock);
-    float* mm = scratch + 2 * kNoAllocMaxBlocks;
-    minmax_partial_kernel<<<nb, kReduceThreads, 0, s>>>(v, n, scratch);
-    FBP_TRY_CUDA(cudaGetLastError());
-    minmax_final_kernel<<<1, kReduceThreads, 0, s>>>(scratch, nb, mm);
-    FBP_TRY_CUDA(cudaGetLastError());
-    const unsigned ab = (unsigned)std::min<uint64_t>(cdiv(n, 256), 1216);
-    normalize_apply_kernel<<<ab, 256, 0, s>>>(v, n, mm);
-    FBP_TRY_CUDA(cudaGetLastError());
-    return FBP_OK;
+    return guarded("fbp_normalize_minmax_noalloc", [&]() -> fbp_status {
+        clear_error();
+        if (!v || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_normalize_minmax_noalloc: null buffer or n == 0");
+        if (n > (uint64_t)kNoAllocMaxBlocks * kNoAllocElemsPerBlock)
+            return set_error(FBP_ERR_UNSUPPORTED,
+                             "fbp_normalize_minmax_noalloc: n exceeds 2^30 elements (the static scratch holds 1024 "
+                             "partial min/max pairs of 2^20 elements each); use fbp_normalize_minmax");
+        float* scratch = nullptr;
+        FBP_TRY(noalloc_scratch(&scratch));
+        cudaStream_t s = (cudaStream_t)stream;
+        const int nb = (int)((n + kNoAllocElemsPerBlock - 1) / kNoAllocElemsPerBlock);
+        float* mm = scratch + 2 * kNoAllocMaxBlocks;
+        minmax_partial_kernel<<<nb, kReduceThreads, 0, s>>>(v, n, scratch);
+        FBP_TRY_CUDA(cudaGetLastError());
+        minmax_final_kernel<<<1, kReduceThreads, 0, s>>>(scratch, nb, mm);
+        FBP_TRY_CUDA(cudaGetLastError());
+        const unsigned ab = (unsigned)std::min<uint64_t>(cdiv(n, 256), 1216);
+        normalize_apply_kernel<<<ab, 256, 0, s>>>(v, n, mm);
+        FBP_TRY_CUDA(cudaGetLastError());
+        return FBP_OK;
+    });
 }
 
 extern "C" fbp_status fbp_postfilter(fbp_context* ctx, int kind, int kernel_size, float sigma, const float* in,
                                      float* out, uint32_t nx, uint32_t ny, uint32_t nz, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    if (!in || !out) return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: null buffer");
-    if (nx == 0 || ny == 0 || nz == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: empty volume");
-    const size_t n = (size_t)nx * ny * nz;
-    if (in == out && kind != FBP_FILTER_NONE)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: in and out must be different buffers");
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (kind) {
-        case FBP_FILTER_NONE:
-            if (in != out) FBP_TRY_CUDA(cudaMemcpyAsync(out, in, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
-            return FBP_OK;
-        case FBP_FILTER_LAPLACIAN: return launch_laplacian(ctx, in, out, nx, ny, nz, kernel_size, s);
-        case FBP_FILTER_LOG: return launch_log(ctx, in, out, nx, ny, nz, kernel_size, sigma, s);
-        case FBP_FILTER_LOG_FFT: return launch_log_fft(ctx, in, out, nx, ny, nz, sigma, s);
-        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: unknown filter kind");
-    }
+    return guarded("fbp_postfilter", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        if (!in || !out) return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: null buffer");
+        if (nx == 0 || ny == 0 || nz == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: empty volume");
+        const size_t n = (size_t)nx * ny * nz;
+        if (in == out && kind != FBP_FILTER_NONE)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: in and out must be different buffers");
+        cudaStream_t s = (cudaStream_t)stream;
+        switch (kind) {
+            case FBP_FILTER_NONE:
+                if (in != out) FBP_TRY_CUDA(cudaMemcpyAsync(out, in, n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+                return FBP_OK;
+            case FBP_FILTER_LAPLACIAN: return launch_laplacian(ctx, in, out, nx, ny, nz, kernel_size, s);
+            case FBP_FILTER_LOG: return launch_log(ctx, in, out, nx, ny, nz, kernel_size, sigma, s);
+            case FBP_FILTER_LOG_FFT: return launch_log_fft(ctx, in, out, nx, ny, nz, sigma, s);
+            default: return set_error(FBP_ERR_INVALID_ARG, "fbp_postfilter: unknown filter kind");
+        }
+    });
 }

@@ -183,21 +183,23 @@ using namespace fbp;
 extern "C" fbp_status fbp_splat_backproject(fbp_context* ctx, const fbp_recon_info* info, const void* cube, int dtype,
                                             int layout, const float* laser_xyz, uint32_t max_bins, uint32_t grid_w,
                                             uint32_t grid_h, float* volume, void* stream) {
-    clear_error();
-    FBP_TRY(check_ctx(ctx));
-    FBP_TRY(validate_info(info, false, "fbp_splat_backproject"));
-    if (!cube || !laser_xyz || !volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: null buffer");
-    if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: unknown layout");
-    if (grid_w == 0 || grid_h == 0 || grid_w > 65536 || grid_h > 65536)
-        return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: grid sides must be in 1..65536");
-    const uint32_t nbins = std::min(info->num_time_bins, max_bins ? max_bins : info->num_time_bins);
-    cudaStream_t s = (cudaStream_t)stream;
-    switch (dtype) {
-        case FBP_F32: return splat_typed<float>(ctx, *info, cube, layout, laser_xyz, nbins, grid_w, grid_h, volume, s);
-        case FBP_BF16:
-            return splat_typed<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, nbins, grid_w, grid_h, volume, s);
-        case FBP_F16: return splat_typed<__half>(ctx, *info, cube, layout, laser_xyz, nbins, grid_w, grid_h, volume, s);
-        default: return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: unknown dtype");
-    }
+    return guarded("fbp_splat_backproject", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, false, "fbp_splat_backproject"));
+        if (!cube || !laser_xyz || !volume) return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: null buffer");
+        if (layout != FBP_LAYOUT_TIME_MAJOR && layout != FBP_LAYOUT_TIME_INNER)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: unknown layout");
+        if (grid_w == 0 || grid_h == 0 || grid_w > 65536 || grid_h > 65536)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: grid sides must be in 1..65536");
+        const uint32_t nbins = std::min(info->num_time_bins, max_bins ? max_bins : info->num_time_bins);
+        cudaStream_t s = (cudaStream_t)stream;
+        switch (dtype) {
+            case FBP_F32: return splat_typed<float>(ctx, *info, cube, layout, laser_xyz, nbins, grid_w, grid_h, volume, s);
+            case FBP_BF16:
+                return splat_typed<__nv_bfloat16>(ctx, *info, cube, layout, laser_xyz, nbins, grid_w, grid_h, volume, s);
+            case FBP_F16: return splat_typed<__half>(ctx, *info, cube, layout, laser_xyz, nbins, grid_w, grid_h, volume, s);
+            default: return set_error(FBP_ERR_INVALID_ARG, "fbp_splat_backproject: unknown dtype");
+        }
+    });
 }

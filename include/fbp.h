@@ -30,7 +30,8 @@ typedef enum {
     FBP_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up (status word set) */
     FBP_ERR_UNSUPPORTED = 5, /* valid but not implemented for these arguments */
     FBP_ERR_DEVICE = 6,      /* a kernel reported an internal check failure */
-    FBP_ERR_IO = 7           /* file could not be read or written */
+    FBP_ERR_IO = 7,          /* file could not be read or written */
+    FBP_ERR_INTERNAL = 8     /* unexpected host-side failure inside the library (message in fbp_last_error) */
 } fbp_status;
 
 /* Storage type of a transient cube. */

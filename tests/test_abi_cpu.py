@@ -191,3 +191,28 @@ def test_device_pointer_checks_reject_host_and_short_tensors():
     assert _plane_span(16, 16, 200, 200, 1) == 256 * 200
     assert _plane_span(12, 40, 5, 1, 480) == 5 * 480
     assert _plane_span(0, 4, 4, 4, 1) == 0
+
+
+def test_host_allocation_failure_is_a_status_not_an_abort(built, tmp_path):
+    """No C++ exception crosses the C ABI: with the address space capped just
+    above what the process uses, a 256 MB PNG encode must come back as
+    FBP_ERR_OOM (an escaping std::bad_alloc would abort the process)."""
+    import subprocess
+    import sys
+
+    resource = pytest.importorskip("resource")
+    del resource
+    code = f"""
+import ctypes, resource, numpy as np
+from fasterbackprojection_gb300 import _lib
+lib = _lib.load()
+img = np.zeros((8192, 8192, 4), np.uint8)
+vm = [int(l.split()[1]) * 1024 for l in open('/proc/self/status') if l.startswith('VmSize')][0]
+resource.setrlimit(resource.RLIMIT_AS, (vm + (96 << 20), resource.getrlimit(resource.RLIMIT_AS)[1]))
+st = lib.fbp_write_png({str(tmp_path / 'big.png')!r}.encode(), img.ctypes.data_as(ctypes.c_void_p), 8192, 8192)
+print(st, lib.fbp_last_error().decode())
+"""
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=str(ROOT), timeout=120)
+    assert out.returncode == 0, out.stderr[-2000:]
+    st, msg = out.stdout.split(" ", 1)
+    assert int(st) == 2 and "fbp_write_png" in msg  # FBP_ERR_OOM
