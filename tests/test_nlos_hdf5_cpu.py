@@ -115,3 +115,14 @@ def test_bad_datasets_are_refused(tmp_path):
     r = nlos_io.read_nlos(tmp_path / "a.nlos")
     np.testing.assert_array_equal(r.data, c.data)
     assert r.dims == c.dims and r.t0 == c.t0
+
+
+def test_read_hdf5_names_its_dependency(tmp_path):
+    import importlib.util
+
+    from fasterbackprojection_gb300 import nlos_io
+
+    if importlib.util.find_spec("h5py") is not None:
+        pytest.skip("h5py is installed here")
+    with pytest.raises(ImportError, match="h5py"):
+        nlos_io.read_hdf5(tmp_path / "capture.hdf5")
