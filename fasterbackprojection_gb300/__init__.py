@@ -24,6 +24,8 @@ from ._lib import (  # noqa: F401
     FBP_MIS_REFERENCE,
     FBP_MIS_SPATIAL,
     FBP_MIS_UNIFORM,
+    FBP_WEIGHTS_BATCHED,
+    FBP_WEIGHTS_REFERENCE,
     FbpError,
     ReconInfo,
     ShapeParams,

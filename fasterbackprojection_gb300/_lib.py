@@ -32,6 +32,8 @@ FBP_CONFOCAL, FBP_EXHAUSTIVE = 0, 1
 FBP_FILTER_NONE, FBP_FILTER_LAPLACIAN, FBP_FILTER_LOG, FBP_FILTER_LOG_FFT = 0, 1, 2, 3
 # fbp_border
 FBP_BORDER_ZERO, FBP_BORDER_EDGE = 0, 1
+# fbp_weight_mode
+FBP_WEIGHTS_BATCHED, FBP_WEIGHTS_REFERENCE = 0, 1
 
 _F3 = c_float * 3
 _U3 = c_uint32 * 3
@@ -126,6 +128,8 @@ SIGNATURES = {
     "fbp_destroy": (c_int, [c_void_p]),
     "fbp_check_device_status": (c_int, [c_void_p, c_void_p]),
     "fbp_kernel_launch_count": (c_uint64, [c_void_p]),
+    "fbp_set_weight_mode": (c_int, [c_void_p, c_int]),
+    "fbp_get_weight_mode": (c_int, [c_void_p, POINTER(c_int)]),
     "fbp_backproject_confocal": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_int, c_void_p, c_void_p,
                                          c_void_p]),
     "fbp_backproject_exhaustive": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_int, c_void_p, c_void_p,

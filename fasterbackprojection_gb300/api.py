@@ -151,6 +151,17 @@ class Context:
     def check_device_status(self, stream=None) -> None:
         check(self._lib.fbp_check_device_status(self._h, self._stream(stream)))
 
+    @property
+    def weight_mode(self) -> int:
+        """fbp_weight_mode of the gathers: FBP_WEIGHTS_BATCHED (default) or FBP_WEIGHTS_REFERENCE."""
+        m = ctypes.c_int()
+        check(self._lib.fbp_get_weight_mode(self._h, byref(m)))
+        return m.value
+
+    @weight_mode.setter
+    def weight_mode(self, mode: int) -> None:
+        check(self._lib.fbp_set_weight_mode(self._h, int(mode)))
+
     # ---------------------------------------------------------- backprojection
     def backproject_confocal(self, info: ReconInfo, cube, laser_xyz, out=None, layout=_lib.FBP_LAYOUT_TIME_INNER,
                              stream=None):

@@ -166,6 +166,7 @@ fbp_status plan_config(fbp_batch* b, int cfg, cudaStream_t s) {
         p.row_pitch = wp.pitch;
         p.slot_w = wp.slot_w;
         p.ch = wp.ch;
+        p.exact_weights = b->ctx->weight_mode == FBP_WEIGHTS_REFERENCE;
         // Group by arithmetic variant and occupancy.
         const int path = path_of(in);
         const bool bounce = in.discard_first_last_bounces == 0;

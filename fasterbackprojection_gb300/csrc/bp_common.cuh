@@ -67,11 +67,17 @@ struct ConfocalGatherParams {
     const void* rows;    // [L][row_pitch] of the storage type
     SampleParams smp;    // used by the sampled (MIS) variant only
     float vs[3];         // voxel size (the voxel-scattering variant's extent)
+    int exact_weights;   // 1: every weight by its own rcp.approx (FBP_WEIGHTS_REFERENCE)
 
+    // Per scan point of a stage, in shared memory: (x, y, z, bounce), (bias,
+    // slot address), the sample weight, three planning ints, and the packed
+    // broadcast copies the pair loop reads as 64-bit register pairs:
+    // (x, x, y, y), (z, z, bias, bias), (bounce, bounce, weight, weight).
+    static constexpr int kPackedGeo = 3;
     // Bytes of per-chunk metadata in front of the window slots (16-byte aligned).
     __host__ __device__ static constexpr size_t meta_bytes(int ch) {
-        return ((size_t)2 * ch * (sizeof(float4) + sizeof(int2) + sizeof(float) + 3 * sizeof(int)) + 2 * sizeof(int) +
-                15) &
+        return ((size_t)2 * ch * (sizeof(float4) * (1 + kPackedGeo) + sizeof(int2) + sizeof(float) + 3 * sizeof(int)) +
+                2 * sizeof(int) + 15) &
                ~size_t(15);
     }
 };

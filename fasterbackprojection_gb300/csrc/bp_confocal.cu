@@ -220,6 +220,7 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     p.slot_w = wp.slot_w;
     p.ch = wp.ch;
     for (int k = 0; k < 3; ++k) p.vs[k] = in.voxel_size[k];
+    p.exact_weights = ctx->weight_mode == FBP_WEIGHTS_REFERENCE;
     if (smp) p.smp = *smp;
     dim3 grid(cdiv(Vx, kKV), cdiv(Vy, 8 * kWY), cdiv(z_end - z_begin, 4 * kWZ));
     const bool bounce = in.discard_first_last_bounces == 0;

@@ -56,8 +56,8 @@ template <> struct ElemShift<__half> { static constexpr int value = 1; };
 // One staged stage of scan points against a thread's KV voxels (consecutive
 // along x, sharing the y/z offsets).
 template <typename S, int KV, int PATH, bool BOUNCE, bool CLAMP, bool SAFE, bool WEIGHTED>
-__device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, const int2* __restrict__ meta,
-                                               const float* __restrict__ wts, int nl, const float (&px)[KV], float py,
+__device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, const ulonglong2* __restrict__ geo2,
+                                               const int2* __restrict__ meta, const float* __restrict__ wts, int nl, const float (&px)[KV], float py,
                                                float pz, float neg_t0, float rcp_dt, uint32_t slot_w,
                                                float (&acc)[KV], float ext = 0.f, float step = 0.f) {
     constexpr int SH = ElemShift<S>::value;
@@ -157,64 +157,106 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
         }
         return;
     }
-    if constexpr (!is_scatter(PATH) && !SAFE && KV % 2 == 0) {
-        // Voxel pairs (k, k + 1) in packed FP32 pairs: the same operations
-        // as the scalar loop below, half the FP32 instructions.
+    if constexpr (!is_scatter(PATH) && !SAFE && KV % 4 == 0) {
+        // Voxel pairs (k, k + 1) in packed FP32 pairs: the bins are the scalar
+        // loop's operations, bit for bit, at half the FP32 instructions.
+        //
+        // Weights by simultaneous inversion (P. L. Montgomery, "Speeding the
+        // Pollard and elliptic curve methods of factorization", Math. Comp. 48
+        // (1987), section 10.3.1): the squared paths s_0..s_{G-1} of G packed
+        // pairs share ONE reciprocal per lane, r = 1 / (s_0 ... s_{G-1}), and
+        // 1 / s_j is r times the product of the others, built from a product
+        // tree (G = 4: 1/s_0 = (r s_2 s_3) s_1).  That is one rcp.approx per
+        // G voxels instead of one per voxel: the bin's sqrt.approx and the
+        // weight's rcp.approx were the only MUFU operations per pair, and the
+        // MUFU pipe bounded the loop.  Each weight carries at most ~3.5 ulp
+        // (the rounded products, the approximate reciprocal, two rounded
+        // multiplies) instead of rcp.approx's own ~1 ulp.  Stages where a
+        // product could leave the normal FP32 range (paths under 3.5 mm or
+        // over 10 km) take the scalar loop with the reference's safeRCP.
+        constexpr int G = (KV / 2) % 4 == 0 ? 4 : 2;
         f32x2_t pxp[KV / 2], accp[KV / 2];
 #pragma unroll
         for (int j = 0; j < KV / 2; ++j) {
             pxp[j] = pack2(px[2 * j], px[2 * j + 1]);
             accp[j] = pack2(acc[2 * j], acc[2 * j + 1]);
         }
+        const f32x2_t pyp = pack2(py, py), pzp = pack2(pz, pz);
         const f32x2_t rcp2p = pack2(rcp2, rcp2), rdp = pack2(rcp_dt, rcp_dt), two = pack2(2.f, 2.f);
         const f32x2_t nt0p = pack2(neg_t0, neg_t0);
 #pragma unroll 2
         for (int i = 0; i < nl; ++i) {
-            const float4 g = geo[i];
-            const int2 m = meta[i];
-            const float dy = sub_rn(py, g.y), dz = sub_rn(pz, g.z);
-            const float dy2 = mul_rn(dy, dy);
-            const f32x2_t gxp = pack2(g.x, g.x), dy2p = pack2(dy2, dy2), dzp = pack2(dz, dz);
-            const f32x2_t biasp = pack2(__int_as_float(m.x), __int_as_float(m.x));
-            const f32x2_t wlp = WEIGHTED ? pack2(wts[i], wts[i]) : 0ull;
-            const f32x2_t gwp = pack2(g.w, g.w);
+            // (x, x, y, y), (z, z, bias, bias), (bounce, bounce, w, w) as register pairs.
+            const ulonglong2 ga = geo2[3 * i], gb = geo2[3 * i + 1];
+            const uint32_t m_addr = (uint32_t)meta[i].y;
+            const int m_bias = meta[i].x;
+            const f32x2_t gxp = ga.x, biasp = gb.y;
+            const f32x2_t dyp = sub_rn2(pyp, ga.y), dzp = sub_rn2(pzp, gb.x);
+            const f32x2_t dy2p = mul_rn2(dyp, dyp);
+            f32x2_t gwp = 0ull, wlp = 0ull;
+            if (BOUNCE || WEIGHTED) {
+                const ulonglong2 gc = geo2[3 * i + 2];
+                gwp = gc.x;
+                wlp = gc.y;
+            }
 #pragma unroll
-            for (int j = 0; j < KV / 2; ++j) {
-                const f32x2_t dx = sub_rn2(pxp[j], gxp);
-                float q0, q1;
-                unpack2(fma_rn2(dzp, dzp, fma_rn2(dx, dx, dy2p)), q0, q1);
-                const f32x2_t d = pack2(sqrt_approx(q0), sqrt_approx(q1));
-                f32x2_t x, dist = 0ull;
-                if (PATH == PATH_2D) {
-                    x = mul_rn2(d, rcp2p);
-                } else {
-                    dist = fma_rn2(d, two, nt0p);
-                    if (BOUNCE) dist = add_rn2(dist, gwp);
-                    x = mul_rn2(dist, rdp);
-                }
-                uint32_t a0, a1;
-                if (PATH == PATH_EXACT) {
-                    float x0, x1;
-                    unpack2(x, x0, x1);
-                    const int b0 = __float2int_rz(x0), b1 = __float2int_rz(x1);  // static_cast<int>
-                    a0 = (uint32_t)m.y + (min((uint32_t)(b0 - m.x), slot_w) << SH);
-                    a1 = (uint32_t)m.y + (min((uint32_t)(b1 - m.x), slot_w) << SH);
-                } else {
-                    float b0, b1;
-                    unpack2(add_rz2(x, biasp), b0, b1);
-                    if (CLAMP) {
-                        a0 = (uint32_t)m.y + (min(__float_as_uint(b0) - 0x4B000000u, slot_w) << SH);
-                        a1 = (uint32_t)m.y + (min(__float_as_uint(b1) - 0x4B000000u, slot_w) << SH);
+            for (int j0 = 0; j0 < KV / 2; j0 += G) {
+                f32x2_t sq[G], Iq[G];
+#pragma unroll
+                for (int jj = 0; jj < G; ++jj) {
+                    const int j = j0 + jj;
+                    const f32x2_t dx = sub_rn2(pxp[j], gxp);
+                    float q0, q1;
+                    unpack2(fma_rn2(dzp, dzp, fma_rn2(dx, dx, dy2p)), q0, q1);
+                    const f32x2_t d = pack2(sqrt_approx(q0), sqrt_approx(q1));
+                    f32x2_t x;
+                    if (PATH == PATH_2D) {
+                        x = mul_rn2(d, rcp2p);
+                        sq[jj] = mul_rn2(d, d);
                     } else {
-                        a0 = (uint32_t)m.y + (__float_as_uint(b0) << SH);  // bias folded into m.y
-                        a1 = (uint32_t)m.y + (__float_as_uint(b1) << SH);
+                        f32x2_t dist = fma_rn2(d, two, nt0p);
+                        if (BOUNCE) dist = add_rn2(dist, gwp);
+                        x = mul_rn2(dist, rdp);
+                        sq[jj] = mul_rn2(dist, dist);
                     }
+                    uint32_t a0, a1;
+                    if (PATH == PATH_EXACT) {
+                        float x0, x1;
+                        unpack2(x, x0, x1);
+                        const int b0 = __float2int_rz(x0), b1 = __float2int_rz(x1);  // static_cast<int>
+                        a0 = m_addr + (min((uint32_t)(b0 - m_bias), slot_w) << SH);
+                        a1 = m_addr + (min((uint32_t)(b1 - m_bias), slot_w) << SH);
+                    } else {
+                        float b0, b1;
+                        unpack2(add_rz2(x, biasp), b0, b1);
+                        if (CLAMP) {
+                            a0 = m_addr + (min(__float_as_uint(b0) - 0x4B000000u, slot_w) << SH);
+                            a1 = m_addr + (min(__float_as_uint(b1) - 0x4B000000u, slot_w) << SH);
+                        } else {
+                            a0 = m_addr + (__float_as_uint(b0) << SH);  // bias folded into the address
+                            a1 = m_addr + (__float_as_uint(b1) << SH);
+                        }
+                    }
+                    Iq[jj] = pack2(lds_elem<S>(a0), lds_elem<S>(a1));
+                    if (WEIGHTED) Iq[jj] = mulf2(Iq[jj], wlp);
                 }
-                f32x2_t I = pack2(lds_elem<S>(a0), lds_elem<S>(a1));
-                if (WEIGHTED) I = mulf2(I, wlp);
-                float s0, s1;
-                unpack2(PATH == PATH_2D ? mul_rn2(d, d) : mul_rn2(dist, dist), s0, s1);
-                accp[j] = fmaf2(I, pack2(rcp_approx(s0), rcp_approx(s1)), accp[j]);
+                if constexpr (G == 4) {
+                    const f32x2_t p01 = mul_rn2(sq[0], sq[1]), p23 = mul_rn2(sq[2], sq[3]);
+                    float m0, m1;
+                    unpack2(mul_rn2(p01, p23), m0, m1);
+                    const f32x2_t r = pack2(rcp_approx(m0), rcp_approx(m1));
+                    const f32x2_t r01 = mul_rn2(r, p23), r23 = mul_rn2(r, p01);  // 1/(s0 s1), 1/(s2 s3)
+                    accp[j0 + 0] = fmaf2(Iq[0], mul_rn2(r01, sq[1]), accp[j0 + 0]);
+                    accp[j0 + 1] = fmaf2(Iq[1], mul_rn2(r01, sq[0]), accp[j0 + 1]);
+                    accp[j0 + 2] = fmaf2(Iq[2], mul_rn2(r23, sq[3]), accp[j0 + 2]);
+                    accp[j0 + 3] = fmaf2(Iq[3], mul_rn2(r23, sq[2]), accp[j0 + 3]);
+                } else {
+                    float m0, m1;
+                    unpack2(mul_rn2(sq[0], sq[1]), m0, m1);
+                    const f32x2_t r = pack2(rcp_approx(m0), rcp_approx(m1));
+                    accp[j0 + 0] = fmaf2(Iq[0], mul_rn2(r, sq[1]), accp[j0 + 0]);
+                    accp[j0 + 1] = fmaf2(Iq[1], mul_rn2(r, sq[0]), accp[j0 + 1]);
+                }
             }
         }
 #pragma unroll
@@ -280,7 +322,9 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const uint32_t slot_stride = p.slot_w + ALIGN;  // sentinel element(s) at slot_w
     float4* s_geo = reinterpret_cast<float4*>(smem_raw);         // [2][CHMAX]
-    int2* s_meta = reinterpret_cast<int2*>(s_geo + 2 * CHMAX);   // [2][CHMAX]
+    ulonglong2* s_geo2 = reinterpret_cast<ulonglong2*>(s_geo + 2 * CHMAX);  // [2][CHMAX][kPackedGeo]
+    constexpr int PG = ConfocalGatherParams::kPackedGeo;
+    int2* s_meta = reinterpret_cast<int2*>(s_geo2 + 2 * CHMAX * PG);  // [2][CHMAX]
     int* s_cnt = reinterpret_cast<int*>(s_meta + 2 * CHMAX);     // [2][CHMAX]
     int* s_src = s_cnt + 2 * CHMAX;                              // [2][CHMAX]
     int* s_row = s_src + 2 * CHMAX;                              // [2][CHMAX]
@@ -418,8 +462,12 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             int cnt = 0, src = 0, near = 0, a = 0;
             bool skip = true;
-            if (item < nitems && l < p.L) {
-                g = p.scan[l];
+            // A point of a ragged edge cluster that lies outside the scan grid:
+            // planned with scan point 0's geometry (finite paths and weights)
+            // and read from the zero slot.
+            const bool ragged = item < nitems && l >= p.L;
+            if (item < nitems) {
+                g = p.scan[ragged ? 0u : l];
                 // Nearest and farthest voxel-centre distance of the tile.
                 const float cx = fminf(fmaxf(g.x, bx0), bx1), cy = fminf(fmaxf(g.y, by0), by1),
                             cz = fminf(fmaxf(g.z, bz0), bz1);
@@ -433,8 +481,10 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                     pmin = fmaxf(0.f, pmin - 1.01f * scat_ext);
                     pmax = pmax + 1.01f * scat_ext + scat_step;
                 }
-                // Paths this short make dist^2 <= EPS possible: use safeRCP's branch.
-                near = pmin < 0.0035f;
+                // Paths this short make dist^2 <= EPS possible: use safeRCP's
+                // branch.  Paths this long (or NaN) could take the batched
+                // reciprocal's products out of the FP32 range: also per voxel.
+                near = pmin < 0.0035f || !(pmax < 1.0e4f);
                 // Conservative bin range with a 2-bin margin for rounding.
                 const int blo = (int)fmaxf(fminf(floorf(pmin * rcp_dt), 1.0e9f), -1.0e9f) - 2;
                 const int bhi = (int)fmaxf(fminf(floorf(pmax * rcp_dt), 1.0e9f), -1.0e9f) + 2;
@@ -459,6 +509,11 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                     }
                     src = a;
                 }
+                if (ragged) {
+                    skip = true;
+                    cnt = 0;
+                    wgt = 0.f;
+                }
             }
             // Slot of this scan point (or the zero slot) as a shared address.
             const uint32_t slot_elem = skip ? zero_slot : (uint32_t)(buf * CH + tid) * slot_stride;
@@ -470,7 +525,7 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                 bias = __float_as_int((float)(8388608 - a));
                 if (!CLAMP) saddr -= (0x4B000000u << SH);
             }
-            if (item >= nitems || l >= p.L) {
+            if (item >= nitems) {
                 // Beyond the last scan point: x + 0 < 2^23 lands on the sentinel
                 // (CLAMP) or, unclamped, reads the zero slot at index 0.
                 bias = PATH == PATH_EXACT ? 0x40000000 : 0;
@@ -480,10 +535,17 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                 wgt = 0.f;
             }
             s_geo[buf * CHMAX + tid] = g;
+            {
+                ulonglong2* g2 = s_geo2 + (buf * CHMAX + tid) * PG;
+                const float bf = __int_as_float(bias);
+                g2[0] = make_ulonglong2(pack2(g.x, g.x), pack2(g.y, g.y));
+                g2[1] = make_ulonglong2(pack2(g.z, g.z), pack2(bf, bf));
+                g2[2] = make_ulonglong2(pack2(g.w, g.w), pack2(wgt, wgt));
+            }
             s_meta[buf * CHMAX + tid] = make_int2(bias, (int)saddr);
             s_cnt[buf * CHMAX + tid] = cnt;
             s_src[buf * CHMAX + tid] = src;
-            s_row[buf * CHMAX + tid] = (int)l;
+            s_row[buf * CHMAX + tid] = ragged ? 0 : (int)l;
             s_w[buf * CHMAX + tid] = wgt;
             const unsigned any_near = __ballot_sync(CH >= 32 ? 0xffffffffu : ((1u << CH) - 1u), near);
             if (tid == 0) s_flag[buf] = any_near != 0;
@@ -529,17 +591,18 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
         __syncthreads();  // stage c's windows visible
 
         const float4* geo = s_geo + buf * CHMAX;
+        const ulonglong2* geo2 = s_geo2 + buf * CHMAX * PG;
         const int2* meta = s_meta + buf * CHMAX;
         const float* wts = s_w + buf * CHMAX;
-        const bool safe = s_flag[buf] != 0;
+        const bool safe = s_flag[buf] != 0 || p.exact_weights;
         const int nl = (int)min((uint32_t)CH, nitems - c * CH);
         float scale = 1.f;
         if (!safe) {
-            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, false, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
+            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, false, SAMPLED>(geo, geo2, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
                                                                         p.slot_w, acc, scat_ext, scat_step);
             if (PATH == PATH_2D) scale = 0.25f;  // w was rcp(d^2) = 4 rcp(dist^2)
         } else {
-            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, true, SAMPLED>(geo, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
+            confocal_stage<S, KV, PATH, BOUNCE, CLAMP, true, SAMPLED>(geo, geo2, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
                                                                        p.slot_w, acc, scat_ext, scat_step);
         }
 

@@ -136,6 +136,22 @@ fbp_status fbp_check_device_status(fbp_context* ctx, void* stream) {
 
 uint64_t fbp_kernel_launch_count(const fbp_context* ctx) { return ctx ? ctx->launches : 0; }
 
+extern "C" fbp_status fbp_set_weight_mode(fbp_context* ctx, int mode) {
+    clear_error();
+    if (!ctx) return set_error(FBP_ERR_INVALID_ARG, "fbp_set_weight_mode: null context");
+    if (mode != FBP_WEIGHTS_BATCHED && mode != FBP_WEIGHTS_REFERENCE)
+        return set_error(FBP_ERR_INVALID_ARG, "fbp_set_weight_mode: unknown mode");
+    ctx->weight_mode = mode;
+    return FBP_OK;
+}
+
+extern "C" fbp_status fbp_get_weight_mode(const fbp_context* ctx, int* mode) {
+    clear_error();
+    if (!ctx || !mode) return set_error(FBP_ERR_INVALID_ARG, "fbp_get_weight_mode: null argument");
+    *mode = ctx->weight_mode;
+    return FBP_OK;
+}
+
 fbp_status fbp_linear_space(double min_value, double max_value, int n, double* out) {
     return guarded("fbp_linear_space", [&]() -> fbp_status {
         clear_error();

@@ -94,6 +94,7 @@ struct fbp_context {
     void* ws[fbp::WS_NUM_SLOTS] = {};
     size_t ws_bytes[fbp::WS_NUM_SLOTS] = {};
     int* status_dev = nullptr;  // device status word: 0 ok, else an fbp_status
+    int weight_mode = FBP_WEIGHTS_BATCHED;  // fbp_weight_mode of the gathers
     uint64_t launches = 0;
     // FFT twiddle tables, one per power-of-two length (index log2 n): the
     // half table exp(-2 pi i k / n) and the per-pass tables of the LCT kernels.

@@ -93,6 +93,24 @@ fbp_status fbp_check_device_status(fbp_context* ctx, void* stream);
 /* Number of kernels this context launched since creation (instrumentation). */
 uint64_t fbp_kernel_launch_count(const fbp_context* ctx);
 
+/* How the voxel gathers compute the per-pair weight safeRCP(dist^2)
+ * (math.cuh:23-29, transient_reconstruction.cuh:131), which the reference
+ * evaluates with one fast-math reciprocal per (voxel, scan point) pair.
+ *   FBP_WEIGHTS_BATCHED   (default) groups of voxels of one thread share one
+ *                         reciprocal (Montgomery's simultaneous inversion):
+ *                         each weight within ~4 ulp of the reference's, the
+ *                         bins still bit for bit; volumes within 1e-6 relative
+ *                         L2 of the reference-weight result.
+ *   FBP_WEIGHTS_REFERENCE every weight is the reference's own reciprocal, so a
+ *                         single-scan-point volume equals the reference kernel's
+ *                         bit for bit (slower: one reciprocal per pair).
+ * Applies to fbp_backproject_confocal, _slab, _exhaustive, fbp_mis_backproject
+ * (unbiased modes) and batches created afterwards.  No counterpart in the
+ * reference (an option of this library). */
+typedef enum { FBP_WEIGHTS_BATCHED = 0, FBP_WEIGHTS_REFERENCE = 1 } fbp_weight_mode;
+fbp_status fbp_set_weight_mode(fbp_context* ctx, int mode);
+fbp_status fbp_get_weight_mode(const fbp_context* ctx, int* mode);
+
 /* ---- backprojection ------------------------------------------------------ */
 
 /* Confocal voxel backprojection.  Replaces Laser::reconstructAABBConfocal

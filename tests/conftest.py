@@ -1,3 +1,4 @@
+import contextlib
 import os
 import sys
 from pathlib import Path
@@ -48,3 +49,17 @@ def rel_l2(a, b) -> float:
     b = np.asarray(b, dtype=np.float64)
     nb = np.linalg.norm(b.ravel())
     return float(np.linalg.norm((a - b).ravel()) / (nb if nb > 0 else 1.0))
+
+
+@contextlib.contextmanager
+def reference_weights(ctx):
+    """Run the gathers with the reference's own reciprocal per pair (bitwise
+    single-scan parity) and restore the context's weight mode afterwards."""
+    from fasterbackprojection_gb300 import FBP_WEIGHTS_REFERENCE
+
+    old = ctx.weight_mode
+    ctx.weight_mode = FBP_WEIGHTS_REFERENCE
+    try:
+        yield ctx
+    finally:
+        ctx.weight_mode = old

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import cpu
-from tests.conftest import rel_l2
+from tests.conftest import reference_weights, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -51,6 +51,27 @@ def test_confocal_f32_vs_fp64_oracle(ctx, cuda, discard, t0):
     # Fully independent FP64 bins.
     want64 = cpu.confocal_voxel(info, cap.cube, cap.laser_xyz)
     assert rel_l2(got, want64) < 1e-3
+
+
+@pytest.mark.parametrize("discard,t0,dtype", [(1, 0.0, "f32"), (0, 0.0, "f32"), (1, 0.3, "f32"), (1, 0.0, "bf16")])
+def test_confocal_batched_weights_match_reference_weights(ctx, cuda, discard, t0, dtype):
+    """The default batched reciprocal against one reciprocal per pair on the
+    same bins: 1e-6 relative L2 over the volume, 2e-6 relative per voxel."""
+    import torch
+
+    cap, info = _confocal_case(n=16, vres=(40, 36, 44), seed=29, discard=discard, t0=t0)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    if dtype == "bf16":
+        cube = cube.to(torch.bfloat16)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    got = ctx.backproject_confocal(info, cube, lx).double()
+    with reference_weights(ctx):
+        want = ctx.backproject_confocal(info, cube, lx).double()
+    ctx.check_device_status()
+    assert float(want.abs().max()) > 0
+    assert rel_l2(got.cpu().numpy(), want.cpu().numpy()) < 1e-6
+    nz = want.abs() > 1e-3 * float(want.abs().max())
+    assert float(((got - want).abs()[nz] / want.abs()[nz]).max()) < 2e-6
 
 
 @pytest.mark.parametrize("dtype", ["bf16", "f16"])

@@ -140,6 +140,24 @@ def test_control_variate_with_every_cluster_is_the_full_backprojection(ctx, cuda
     assert rel_l2(got.cpu().numpy(), full) < 1e-5
 
 
+def test_ragged_edge_clusters_with_every_cluster_are_the_full_backprojection(ctx, cuda):
+    """A 20 x 20 scan in 8 x 8 clusters: the last row and column of clusters
+    reach past the grid; their missing points are read as zeros.  With
+    K = G = 9 uniform draws every cluster is gathered once with weight 1."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_LEARNED
+
+    cap, info = _case(n=20, seed=27)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    full = ctx.backproject_confocal(info, cube, lx).cpu().numpy()
+    got = ctx.mis_backproject(info, cube, lx, FBP_MIS_LEARNED, 9, seed=5, cluster_side=8, scan_side=20)
+    ctx.check_device_status()
+    got = got.cpu().numpy()
+    assert np.isfinite(got).all()
+    assert rel_l2(got, full) < 1e-5
+
+
 def test_control_variate_lowers_the_error(ctx, cuda):
     """Dense scan (64^2 points, 3.1 cm pitch): the 2 x 2-point block sums
     track the real contributions, so the residual estimator beats plain

@@ -3,8 +3,11 @@ sources into oracle/_ref (the reference-kernel harness), on the same GPU.
 
 * Time bins and weights: with one scan point every voxel receives exactly one
   term, so the reference's atomically accumulated volume equals I[bin] * w
-  and must match the gather bit for bit; I[b] = 2^(b mod 3) makes a bin
-  mismatch visible even where the weight matches.
+  and must match the gather bit for bit with the reference's weights
+  (FBP_WEIGHTS_REFERENCE); I[b] = 2^(b mod 3) makes a bin mismatch visible
+  even where the weight matches.  With the default batched weights the bins
+  are still the reference's (a wrong bin is off by a factor of 2) and each
+  weight is within 6 ulp of the reference's reciprocal.
 * Multi-scan volumes differ only by summation order (FP32 atomics in the
   reference vs blocked Kahan here): relative L2 <= 1e-5.
 * LoG, Laplacian and normalisation keep the reference's per-output operation
@@ -13,7 +16,7 @@ sources into oracle/_ref (the reference-kernel harness), on the same GPU.
 import numpy as np
 import pytest
 
-from tests.conftest import rel_l2
+from tests.conftest import reference_weights, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -57,12 +60,39 @@ def test_confocal_single_scan_bitwise(ctx, harness, cuda, mode):
                               res=(48, 40, 56))
         lxyz = torch.tensor([[rng.uniform(-1, 1), 0.0, rng.uniform(-1, 1)]], dtype=torch.float32, device=cuda)
         ref = harness.confocal_voxel(info, cube, lxyz)
-        got = ctx.backproject_confocal(info, cube.view(1, T), lxyz)
+        with reference_weights(ctx):
+            got = ctx.backproject_confocal(info, cube.view(1, T), lxyz)
         torch.cuda.synchronize()
         mismatch += int((ref.view(torch.int32) != got.view(torch.int32)).sum())
         total += ref.numel()
     ctx.check_device_status()
     assert mismatch == 0, f"{mismatch} of {total} voxels differ from the reference kernel"
+
+
+@pytest.mark.parametrize("mode", ["plain", "bounces", "t0", "bounces_t0"])
+def test_confocal_single_scan_batched_weights_error_bound(ctx, harness, cuda, mode):
+    """Default (batched, Montgomery) weights: the same voxels are non-zero and
+    each differs from the reference kernel's I[bin] * rcp.approx(dist^2) by at
+    most 6 ulp (the batched weight's ~3.5 ulp plus rcp.approx's own), far
+    below the factor 2 a neighbouring bin would give."""
+    import torch
+
+    rng = np.random.default_rng({"plain": 31, "bounces": 32, "t0": 33, "bounces_t0": 34}[mode])
+    T = 2048
+    cube = torch.from_numpy((2.0 ** (np.arange(T) % 3)).astype(np.float32)).to(cuda)
+    worst = 0.0
+    for trial in range(12):
+        info = _rand_geometry(rng, 48, T, 0 if "bounces" in mode else 1, 0.6 if "t0" in mode else 0.0,
+                              res=(48, 40, 56))
+        lxyz = torch.tensor([[rng.uniform(-1, 1), 0.0, rng.uniform(-1, 1)]], dtype=torch.float32, device=cuda)
+        ref = harness.confocal_voxel(info, cube, lxyz).double()
+        got = ctx.backproject_confocal(info, cube.view(1, T), lxyz).double()
+        assert torch.equal(ref != 0, got != 0)
+        nz = ref != 0
+        if bool(nz.any()):
+            worst = max(worst, float(((got[nz] - ref[nz]).abs() / ref[nz]).max()))
+    ctx.check_device_status()
+    assert worst <= 6 * 2.0 ** -23, worst
 
 
 def test_confocal_matches_reference_kernel_multi_scan(ctx, harness, cuda):
