@@ -800,14 +800,39 @@ def exhaustive_leg(ctx, dev):
     vol, ms = timed_ms(lambda: ctx.backproject_exhaustive(info, cube16, cap.laser_xyz, cap.sensor_xyz), reps=3)
     triples = 128 ** 3 * L * S
     idx = np.sort(np.random.default_rng(3).choice(128 ** 3, 128, replace=False)).astype(np.int64)
-    want = cpu.exhaustive_voxel_subset(info, cube16.float().cpu().numpy().reshape(L * S, 1024),
-                                       cap.laser_xyz.cpu().numpy(), cap.sensor_xyz.cpu().numpy(), idx)
+    cube_np = cube16.float().cpu().numpy().reshape(L * S, 1024)
+    lx_np, sx_np = cap.laser_xyz.cpu().numpy(), cap.sensor_xyz.cpu().numpy()
+    want = cpu.exhaustive_voxel_subset(info, cube_np, lx_np, sx_np, idx)
+    # The same voxels with the GPU's own bins: isolates the accumulation (FP32
+    # blocks + Kahan, the weights) from bins that flip at FP32 bin edges.
+    gbins = ctx.debug_exhaustive_bins(info, cap.laser_xyz, cap.sensor_xyz, torch.from_numpy(idx).to(dev))
+    gbins = gbins.cpu().numpy().reshape(len(idx), L * S)
+    want_same = cpu.exhaustive_voxel_subset(info, cube_np, lx_np, sx_np, idx, bins=gbins)
     got = vol.reshape(-1)[torch.from_numpy(idx).to(dev)].double().cpu().numpy()
+    # FP64 bins of the same triples: how many differ from the GPU's, and how
+    # much of the independent-bins error those flips alone account for.
+    vxs, vys, vzs = idx % 128, (idx // 128) % 128, idx // (128 * 128)
+    vsz = np.array(info.voxel_size, dtype=np.float64)
+    pts = np.array(info.hidden_min, dtype=np.float64) + np.stack([vxs, vzs, vys], 1) * vsz + 0.5 * vsz
+    rl = np.linalg.norm(lx_np.astype(np.float64)[None, :, None, :] - pts[:, None, None, :], axis=3)
+    rs = np.linalg.norm(sx_np.astype(np.float64)[None, None, :, :] - pts[:, None, None, :], axis=3)
+    b64 = np.floor((rl + rs) / float(info.time_step)).reshape(len(idx), L * S)
+    b64 = np.where((b64 >= 0) & (b64 < 1024), b64, -1).astype(np.int64)
+    nz = cube_np[np.arange(L * S)[None, :], np.clip(gbins, 0, 1023)] > 1e-5
+    flipped = (b64 != gbins)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     return {
         "workload": "exhaustive 16^2 x 32^2 x 1024 (16 ps) FP16 -> 128^3, 500 points",
         "ms": ms, "value": triples / (ms / 1e3), "unit": "voxel-samples/s (voxel, laser, SPAD)",
         "achieved_gbs_2B_per_sample": triples * 2 / (ms / 1e3) / 1e9,
-        "rel_l2_vs_fp64": float(np.linalg.norm(got - want) / np.linalg.norm(want)), "error_voxels": 128,
+        "rel_l2_vs_fp64": rel(got, want), "error_voxels": 128,
+        "rel_l2_vs_fp64_same_bins": rel(got, want_same),
+        "bin_flips": {"triples": int(flipped.size), "flipped": int(flipped.sum()),
+                      "flipped_on_nonzero_samples": int((flipped & nz).sum()),
+                      "rel_l2_fp64_gpu_bins_vs_fp64_bins": rel(want_same, want),
+                      "note": "flips are triples whose path lies within an FP32 rounding of a bin edge; "
+                              "the FP64-vs-FP64 difference with the two bin sets is the whole "
+                              "independent-bins error"},
         "reference_cuda": {"unavailable": "the reference kernel splits the pair index by L (l = ls/L, "
                                           "s = ls%L) and reads laserTargets out of bounds when L != S"},
     }

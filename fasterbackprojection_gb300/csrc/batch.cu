@@ -73,8 +73,6 @@ struct fbp_batch {
 namespace fbp {
 namespace {
 
-size_t esize(int dtype) { return dtype == FBP_F32 ? 4 : 2; }
-
 int path_of(const fbp_recon_info& in) {
     if (in.time_offset > 0.f) return PATH_EXACT;
     if (in.discard_first_last_bounces != 0 && in.time_offset == 0.f) return PATH_2D;
@@ -88,43 +86,31 @@ void drop_graph(fbp_batch* b) {
     b->graph = nullptr;
 }
 
-template <typename S>
-fbp_status prepare_kernel(const BatchLaunch& l, int* occ) {
-    return batch_prepare_kernel<S>(l, occ);
-}
+// Rows are FP32 for every storage type (16-bit captures are widened when the
+// rows are made), so one set of kernels serves all of them.
+constexpr size_t kRowBytes = sizeof(float);
 
-fbp_status prepare_any(int dtype, const BatchLaunch& l, int* occ) {
-    switch (dtype) {
-        case FBP_F32: return prepare_kernel<float>(l, occ);
-        case FBP_BF16: return prepare_kernel<__nv_bfloat16>(l, occ);
-        default: return prepare_kernel<__half>(l, occ);
-    }
-}
+fbp_status prepare_any(const BatchLaunch& l, int* occ) { return batch_prepare_kernel<float>(l, occ); }
 
-fbp_status launch_any(fbp_context* ctx, int dtype, const BatchLaunch& l, int ctas, cudaStream_t s) {
-    switch (dtype) {
-        case FBP_F32: return batch_launch<float>(ctx, l, ctas, s);
-        case FBP_BF16: return batch_launch<__nv_bfloat16>(ctx, l, ctas, s);
-        default: return batch_launch<__half>(ctx, l, ctas, s);
-    }
+fbp_status launch_any(fbp_context* ctx, const BatchLaunch& l, int ctas, cudaStream_t s) {
+    return batch_launch<float>(ctx, l, ctas, s);
 }
 
 fbp_status rows_any(fbp_context* ctx, int dtype, const fbp_capture_desc& c, uint32_t pitch, void* dst,
                     cudaStream_t s) {
     const uint32_t L = c.info.num_laser_targets, T = c.info.num_time_bins;
+    float* rows = static_cast<float*>(dst);
     switch (dtype) {
-        case FBP_F32: return prepare_rows_into<float>(ctx, c.cube, c.layout, L, T, pitch, static_cast<float*>(dst), s);
-        case FBP_BF16:
-            return prepare_rows_into<__nv_bfloat16>(ctx, c.cube, c.layout, L, T, pitch,
-                                                    static_cast<__nv_bfloat16*>(dst), s);
-        default: return prepare_rows_into<__half>(ctx, c.cube, c.layout, L, T, pitch, static_cast<__half*>(dst), s);
+        case FBP_F32: return prepare_rows_into<float>(ctx, c.cube, c.layout, L, T, pitch, rows, s);
+        case FBP_BF16: return prepare_rows_into<__nv_bfloat16>(ctx, c.cube, c.layout, L, T, pitch, rows, s);
+        default: return prepare_rows_into<__half>(ctx, c.cube, c.layout, L, T, pitch, rows, s);
     }
 }
 
 // (Re)plan windows, parameters and work items for tile configuration `cfg`.
 fbp_status plan_config(fbp_batch* b, int cfg, cudaStream_t s) {
     const TileCfg tc = kTileCfgs[cfg];
-    const int align = (int)(16 / esize(b->dtype));
+    const int align = (int)(16 / kRowBytes);
     const size_t meta = ConfocalGatherParams::meta_bytes(32);
     const uint32_t n = (uint32_t)b->caps.size();
     b->params.assign(n, ConfocalGatherParams{});
@@ -138,17 +124,17 @@ fbp_status plan_config(fbp_batch* b, int cfg, cudaStream_t s) {
         const double ey = (double)std::min<uint32_t>(4 * tc.wz, in.voxel_res[2]) * std::fabs(in.voxel_size[1]);
         const double ez = (double)std::min<uint32_t>(8 * tc.wy, in.voxel_res[1]) * std::fabs(in.voxel_size[2]);
         WindowPlan wp;
-        FBP_TRY(plan_window(b->ctx, ex, ey, ez, in.time_step, in.num_time_bins, align, esize(b->dtype), meta, &wp,
+        FBP_TRY(plan_window(b->ctx, ex, ey, ez, in.time_step, in.num_time_bins, align, kRowBytes, meta, &wp,
                             "fbp_batch"));
         // Leave room for the persistent kernel's own static shared memory
         // (replanning only the windows that fill the SM, so the others keep
         // the single-capture gather's plan).
         if (wp.smem + kBatchStaticSmem > (size_t)b->ctx->smem_optin)
-            FBP_TRY(plan_window(b->ctx, ex, ey, ez, in.time_step, in.num_time_bins, align, esize(b->dtype),
+            FBP_TRY(plan_window(b->ctx, ex, ey, ez, in.time_step, in.num_time_bins, align, kRowBytes,
                                 meta + kBatchStaticSmem, &wp, "fbp_batch"));
         pitches[i] = wp.pitch;
         rows_off[i] = rows_total;
-        rows_total += ((size_t)in.num_laser_targets * wp.pitch * esize(b->dtype) + 255) & ~size_t(255);
+        rows_total += ((size_t)in.num_laser_targets * wp.pitch * kRowBytes + 255) & ~size_t(255);
         ConfocalGatherParams& p = b->params[i];
         p.scan = b->scan + b->scan_off[i];
         p.xs = b->axes + b->axes_off[i];
@@ -179,7 +165,7 @@ fbp_status plan_config(fbp_batch* b, int cfg, cudaStream_t s) {
         probe.clamp = clamp;
         probe.cfg = cfg;
         int occ = 0;
-        FBP_TRY(prepare_any(b->dtype, probe, &occ));
+        FBP_TRY(prepare_any(probe, &occ));
         if (occ < 1) return set_error(FBP_ERR_UNSUPPORTED, "fbp_batch: a capture's tile does not fit on an SM");
         BatchGroup* g = nullptr;
         for (auto& gg : b->groups)
@@ -251,7 +237,7 @@ fbp_status plan_config(fbp_batch* b, int cfg, cudaStream_t s) {
         BatchLaunch l{b->d_params, g.d_items, g.nitems, nullptr, g.smem, g.path, g.bounce, g.clamp, cfg,
                       (size_t)b->ctx->smem_optin};
         int occ = 0;
-        FBP_TRY(prepare_any(b->dtype, l, &occ));
+        FBP_TRY(prepare_any(l, &occ));
         g.ctas = (int)std::min<uint64_t>((uint64_t)std::max(1, occ) * b->ctx->sm_count, g.nitems);
     }
     // Side streams and events for the groups after the first.
@@ -286,7 +272,7 @@ fbp_status enqueue_run(fbp_batch* b, cudaStream_t s) {
         const auto& g = b->groups[gi];
         BatchLaunch l{b->d_params, g.d_items, g.nitems, b->d_counters + gi, g.smem, g.path, g.bounce, g.clamp, b->cfg,
                       (size_t)b->ctx->smem_optin};
-        FBP_TRY(launch_any(b->ctx, b->dtype, l, g.ctas, gi == 0 ? s : b->side[gi - 1]));
+        FBP_TRY(launch_any(b->ctx, l, g.ctas, gi == 0 ? s : b->side[gi - 1]));
     }
     for (size_t gi = 1; gi < ng; ++gi) {
         FBP_TRY_CUDA(cudaEventRecord(b->join[gi - 1], b->side[gi - 1]));

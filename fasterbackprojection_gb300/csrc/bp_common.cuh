@@ -11,6 +11,13 @@ __device__ __forceinline__ void cp_async_16(void* smem_dst, const void* gmem_src
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
 }
+// One FP32 element of shared memory at a shared-state-space byte address.
+__device__ __forceinline__ float lds_f32(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -64,7 +71,7 @@ struct ConfocalGatherParams {
     uint32_t row_pitch;  // elements per padded row
     uint32_t slot_w;     // window width in elements (the sentinel zero sits at slot_w)
     int ch;              // scan points per pipeline stage (<= 32)
-    const void* rows;    // [L][row_pitch] of the storage type
+    const void* rows;    // [L][row_pitch] FP32
     SampleParams smp;    // used by the sampled (MIS) variant only
     float vs[3];         // voxel size (the voxel-scattering variant's extent)
     int exact_weights;   // 1: every weight by its own rcp.approx (FBP_WEIGHTS_REFERENCE)
@@ -107,10 +114,11 @@ fbp_status confocal_gather(fbp_context* ctx, const fbp_recon_info& in, const voi
                            const float* laser_xyz, float* volume, cudaStream_t s, const SampleParams* smp);
 void confocal_tile_grid(const fbp_recon_info& in, uint32_t out[3]);
 
-// Padded, thresholded rows [L][pitch] of a confocal cube, written to dst.
+// Padded, thresholded FP32 rows [L][pitch] of a confocal cube of storage type
+// S (16-bit values widened exactly), written to dst.
 template <typename S>
 fbp_status prepare_rows_into(fbp_context* ctx, const void* cube, int layout, uint32_t L, uint32_t T, uint32_t pitch,
-                             S* dst, cudaStream_t stream);
+                             float* dst, cudaStream_t stream);
 
 __global__ void axis_tables_kernel(float* __restrict__ xs, float* __restrict__ ys, float* __restrict__ zs,
                                    uint32_t Vx, uint32_t Vy, uint32_t Vz, float mnx, float mny, float mnz, float sx,

@@ -10,9 +10,12 @@
 // sum order is fixed (reproducible run to run).
 //
 // Data layout in HBM (per call, in the context's scratch):
-//   rows   [L][row_pitch] of the storage type: one padded row per scan point,
-//          time innermost, values <= 1e-5 already replaced by 0 (the
-//          reference skips them), zeros in [T, row_pitch).
+//   rows   [L][row_pitch] FP32: one padded row per scan point, time
+//          innermost, values <= 1e-5 already replaced by 0 (the reference
+//          skips them), zeros in [T, row_pitch).  BF16 / FP16 captures are
+//          widened here (exactly), so the pair loop reads FP32 with no
+//          per-pair conversion; the gather is bound by instruction issue, not
+//          by the bytes of its windows.
 //   scan   [L] float4 (x, y, z, bounce)   bounce = |l-laser|+|l-sensor| or 0
 //   axes   xs[Vx], ys[Vz], zs[Vy]         voxel-centre coordinates
 #include "fbp_internal.cuh"
@@ -52,17 +55,17 @@ __global__ void scan_table_kernel(float4* __restrict__ out, const float* __restr
     out[i] = make_float4(x, y, z, b);
 }
 
-// Rows from a time-innermost cube: copy, threshold, pad.
+// Rows from a time-innermost cube: copy (widened to FP32), threshold, pad.
 template <typename S>
-__global__ void rows_from_time_inner_kernel(S* __restrict__ rows, const S* __restrict__ cube, uint32_t L, uint32_t T,
-                                            uint32_t pitch) {
+__global__ void rows_from_time_inner_kernel(float* __restrict__ rows, const S* __restrict__ cube, uint32_t L,
+                                            uint32_t T, uint32_t pitch) {
     const uint64_t n = (uint64_t)L * pitch;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t l = (uint32_t)(i / pitch), t = (uint32_t)(i % pitch);
-        S v = from_f32<S>(0.f);
+        float v = 0.f;
         if (t < T) {
-            const S c = cube[(uint64_t)l * T + t];
-            if (to_f32(c) > FBP_EPS) v = c;
+            const float c = to_f32(cube[(uint64_t)l * T + t]);
+            if (c > FBP_EPS) v = c;
         }
         rows[i] = v;
     }
@@ -71,8 +74,8 @@ __global__ void rows_from_time_inner_kernel(S* __restrict__ rows, const S* __res
 // Rows from a time-major cube (cube[t*L + l]): tiled transpose through shared
 // memory so both the read and the write are coalesced.
 template <typename S>
-__global__ void rows_from_time_major_kernel(S* __restrict__ rows, const S* __restrict__ cube, uint32_t L, uint32_t T,
-                                            uint32_t pitch) {
+__global__ void rows_from_time_major_kernel(float* __restrict__ rows, const S* __restrict__ cube, uint32_t L,
+                                            uint32_t T, uint32_t pitch) {
     __shared__ float tile[32][33];
     const uint32_t l0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
@@ -87,24 +90,23 @@ __global__ void rows_from_time_major_kernel(S* __restrict__ rows, const S* __res
     __syncthreads();
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
         const uint32_t l = l0 + j, t = t0 + threadIdx.x;
-        if (l < L && t < pitch) rows[(uint64_t)l * pitch + t] = from_f32<S>(tile[threadIdx.x][j]);
+        if (l < L && t < pitch) rows[(uint64_t)l * pitch + t] = tile[threadIdx.x][j];
     }
 }
 
 // Zero the padding columns [roundup(T,32), pitch) the transpose grid does not cover.
-template <typename S>
-__global__ void rows_zero_tail_kernel(S* __restrict__ rows, uint32_t L, uint32_t from, uint32_t pitch) {
+__global__ void rows_zero_tail_kernel(float* __restrict__ rows, uint32_t L, uint32_t from, uint32_t pitch) {
     const uint32_t w = pitch - from;
     const uint64_t n = (uint64_t)L * w;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        rows[(i / w) * pitch + from + (i % w)] = from_f32<S>(0.f);
+        rows[(i / w) * pitch + from + (i % w)] = 0.f;
 }
 
 // ------------------------------------------------------------ host driver --
 
 template <typename S>
 fbp_status prepare_rows_into(fbp_context* ctx, const void* cube, int layout, uint32_t L, uint32_t T, uint32_t pitch,
-                             S* r, cudaStream_t stream) {
+                             float* r, cudaStream_t stream) {
     const S* c = static_cast<const S*>(cube);
     if (layout == FBP_LAYOUT_TIME_INNER) {
         const uint64_t n = (uint64_t)L * pitch;
@@ -119,7 +121,7 @@ fbp_status prepare_rows_into(fbp_context* ctx, const void* cube, int layout, uin
         if (tcover < pitch) {
             const uint64_t n = (uint64_t)L * (pitch - tcover);
             const unsigned blocks = (unsigned)std::min<uint64_t>(cdiv(n, 256), (uint64_t)ctx->sm_count * 16);
-            rows_zero_tail_kernel<S><<<blocks, 256, 0, stream>>>(r, L, tcover, pitch);
+            rows_zero_tail_kernel<<<blocks, 256, 0, stream>>>(r, L, tcover, pitch);
             FBP_CHECK_LAUNCH(ctx, "rows_zero_tail_kernel");
         }
     }
@@ -128,18 +130,18 @@ fbp_status prepare_rows_into(fbp_context* ctx, const void* cube, int layout, uin
 template fbp_status prepare_rows_into<float>(fbp_context*, const void*, int, uint32_t, uint32_t, uint32_t, float*,
                                              cudaStream_t);
 template fbp_status prepare_rows_into<__nv_bfloat16>(fbp_context*, const void*, int, uint32_t, uint32_t, uint32_t,
-                                                     __nv_bfloat16*, cudaStream_t);
-template fbp_status prepare_rows_into<__half>(fbp_context*, const void*, int, uint32_t, uint32_t, uint32_t, __half*,
+                                                     float*, cudaStream_t);
+template fbp_status prepare_rows_into<__half>(fbp_context*, const void*, int, uint32_t, uint32_t, uint32_t, float*,
                                               cudaStream_t);
 
 namespace {
 
 template <typename S>
 fbp_status prepare_rows(fbp_context* ctx, const void* cube, int layout, uint32_t L, uint32_t T, uint32_t pitch,
-                        cudaStream_t stream, S** rows_out) {
+                        cudaStream_t stream, float** rows_out) {
     void* rows = nullptr;
-    FBP_TRY(workspace(ctx, WS_CUBE_ROWS, (size_t)L * pitch * sizeof(S), stream, &rows));
-    *rows_out = static_cast<S*>(rows);
+    FBP_TRY(workspace(ctx, WS_CUBE_ROWS, (size_t)L * pitch * sizeof(float), stream, &rows));
+    *rows_out = static_cast<float*>(rows);
     return prepare_rows_into<S>(ctx, cube, layout, L, T, pitch, *rows_out, stream);
 }
 
@@ -185,7 +187,7 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     const uint32_t Vx = in.voxel_res[0], Vy = in.voxel_res[1], Vz = in.voxel_res[2];
     if (z_end > Vz) z_end = Vz;
     if (z_begin >= z_end) return FBP_OK;
-    constexpr int ALIGN = 16 / sizeof(S);
+    constexpr int ALIGN = 4;  // FP32 rows
 
     // World extents of the largest tile (clamped to the volume).
     const double ex = (double)std::min<uint32_t>(kKV, Vx) * std::fabs(in.voxel_size[0]);
@@ -199,12 +201,12 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
                                    (double)in.voxel_size[1] * in.voxel_size[1] +
                                    (double)in.voxel_size[2] * in.voxel_size[2]);
     const double extra = scatter ? 1.02 * vdiag + 2.0 * std::fabs((double)in.time_step) : 0.0;
-    FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(S),
+    FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(float),
                         ConfocalGatherParams::meta_bytes(32) + (smp ? kSampledStaticSmem : 0), &wp,
                         "fbp_backproject_confocal", extra));
     if (smp) wp.smem -= kSampledStaticSmem;
 
-    S* rows = nullptr;
+    float* rows = nullptr;
     FBP_TRY(prepare_rows<S>(ctx, cube, layout, L, T, wp.pitch, stream, &rows));
 
     ConfocalGatherParams p{};
@@ -231,18 +233,18 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
         const double steps = std::ceil(vdiag / ((double)in.time_step + (double)FBP_EPS));
         const int sp = (int)std::min(std::max(steps, 2.0), (double)kScatterMaxPrefix);
         if (sp == 2) {
-            if (bounce) return go_confocal<S, PATH_SCATTER, true, false, true>(ctx, p, grid, wp.smem, stream);
-            return go_confocal<S, PATH_SCATTER, false, false, true>(ctx, p, grid, wp.smem, stream);
+            if (bounce) return go_confocal<float, PATH_SCATTER, true, false, true>(ctx, p, grid, wp.smem, stream);
+            return go_confocal<float, PATH_SCATTER, false, false, true>(ctx, p, grid, wp.smem, stream);
         }
         if (sp == 3) {
-            if (bounce) return go_confocal<S, PATH_SCATTER + 1, true, false, true>(ctx, p, grid, wp.smem, stream);
-            return go_confocal<S, PATH_SCATTER + 1, false, false, true>(ctx, p, grid, wp.smem, stream);
+            if (bounce) return go_confocal<float, PATH_SCATTER + 1, true, false, true>(ctx, p, grid, wp.smem, stream);
+            return go_confocal<float, PATH_SCATTER + 1, false, false, true>(ctx, p, grid, wp.smem, stream);
         }
-        if (bounce) return go_confocal<S, PATH_SCATTER + 2, true, false, true>(ctx, p, grid, wp.smem, stream);
-        return go_confocal<S, PATH_SCATTER + 2, false, false, true>(ctx, p, grid, wp.smem, stream);
+        if (bounce) return go_confocal<float, PATH_SCATTER + 2, true, false, true>(ctx, p, grid, wp.smem, stream);
+        return go_confocal<float, PATH_SCATTER + 2, false, false, true>(ctx, p, grid, wp.smem, stream);
     }
-    if (smp) return dispatch_confocal<S, true>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
-    return dispatch_confocal<S, false>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
+    if (smp) return dispatch_confocal<float, true>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
+    return dispatch_confocal<float, false>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
 }
 
 }  // namespace

@@ -163,18 +163,20 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
         //
         // Weights by simultaneous inversion (P. L. Montgomery, "Speeding the
         // Pollard and elliptic curve methods of factorization", Math. Comp. 48
-        // (1987), section 10.3.1): the squared paths s_0..s_{G-1} of G packed
-        // pairs share ONE reciprocal per lane, r = 1 / (s_0 ... s_{G-1}), and
-        // 1 / s_j is r times the product of the others, built from a product
-        // tree (G = 4: 1/s_0 = (r s_2 s_3) s_1).  That is one rcp.approx per
-        // G voxels instead of one per voxel: the bin's sqrt.approx and the
+        // (1987), section 10.3.1): the squared paths s_0, s_1 of two packed
+        // pairs share ONE reciprocal per lane, r = 1 / (s_0 s_1), and
+        // 1 / s_0 = r s_1, 1 / s_1 = r s_0 (G = 4 pairs would use a product
+        // tree: 1 / s_0 = (r s_2 s_3) s_1).  That is one rcp.approx per two
+        // voxels instead of one per voxel: the bin's sqrt.approx and the
         // weight's rcp.approx were the only MUFU operations per pair, and the
-        // MUFU pipe bounded the loop.  Each weight carries at most ~3.5 ulp
-        // (the rounded products, the approximate reciprocal, two rounded
-        // multiplies) instead of rcp.approx's own ~1 ulp.  Stages where a
-        // product could leave the normal FP32 range (paths under 3.5 mm or
-        // over 10 km) take the scalar loop with the reference's safeRCP.
-        constexpr int G = (KV / 2) % 4 == 0 ? 4 : 2;
+        // MUFU pipe bounded the loop.  Each weight carries at most ~2 ulp (the
+        // rounded product, the approximate reciprocal, one rounded multiply)
+        // instead of rcp.approx's own ~1 ulp.  G = 2 measured faster than
+        // G = 4 (whose extra multiplies load the FMA pipe, which the packed
+        // pairs already keep busy).  Stages where a product could leave the
+        // normal FP32 range (paths under 3.5 mm or over 10 km) take the scalar
+        // loop with the reference's safeRCP.
+        constexpr int G = 2;
         f32x2_t pxp[KV / 2], accp[KV / 2];
 #pragma unroll
         for (int j = 0; j < KV / 2; ++j) {

@@ -131,13 +131,20 @@ def exhaustive_voxel(info, cube, laser_xyz, sensor_xyz, bins=None) -> np.ndarray
     return vol
 
 
-def exhaustive_voxel_subset(info, cube, laser_xyz, sensor_xyz, idx) -> np.ndarray:
+def exhaustive_voxel_subset(info, cube, laser_xyz, sensor_xyz, idx, bins=None) -> np.ndarray:
+    """Voxels idx of the exhaustive volume; bins (optional) are the GPU's,
+    bins[(i*L + l)*S + s] for voxel idx[i] (fbp_debug_exhaustive_bins' order)."""
     lib = load()
     o = to_oracle_info(info)
     idx = np.ascontiguousarray(idx, dtype=np.int64)
     out = np.empty(idx.shape[0], dtype=np.float64)
-    assert lib.oracle_exhaustive_voxel_subset(ctypes.byref(o), _p(_f32(cube)), _p(_f32(laser_xyz)),
-                                              _p(_f32(sensor_xyz)), _p(idx), c_int64(idx.shape[0]), _p(out)) == 0
+    b = None
+    if bins is not None:
+        b = np.ascontiguousarray(bins, dtype=np.int32)
+        assert b.size == idx.shape[0] * o.num_laser_targets * o.num_sensor_targets
+    assert lib.oracle_exhaustive_voxel_subset_bins(ctypes.byref(o), _p(_f32(cube)), _p(_f32(laser_xyz)),
+                                                   _p(_f32(sensor_xyz)), _p(idx), c_int64(idx.shape[0]),
+                                                   None if b is None else _p(b), _p(out)) == 0
     return out
 
 

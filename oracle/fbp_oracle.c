@@ -236,9 +236,10 @@ int oracle_confocal_voxel_f32_subset(const oracle_info* in, const float* cube, i
     return 0;
 }
 
+/* vbins: this voxel's bins [l*S + s] (ORACLE_BINS_GIVEN) or NULL. */
 static double exhaustive_voxel_value(const oracle_info* in, const float* cube, const float* laser_xyz,
                                      const float* sensor_xyz, const double* bl, const double* bs, int64_t v,
-                                     int bins_mode, const int32_t* bins) {
+                                     int bins_mode, const int32_t* vbins) {
     const uint32_t Vx = in->voxel_res[0], Vy = in->voxel_res[1];
     const uint32_t L = in->num_laser_targets, S = in->num_sensor_targets, T = in->num_time_bins;
     const uint32_t slice = Vx * Vy;
@@ -256,8 +257,7 @@ static double exhaustive_voxel_value(const oracle_info* in, const float* cube, c
             load3(sensor_xyz + 3 * (size_t)s, sp);
             const double dist = dl + dist3(sp, p) - (double)in->time_offset + bl[l] + bs[s];
             const size_t pair = (size_t)l * S + s;
-            const int32_t b = bins_mode == ORACLE_BINS_GIVEN ? bins[((size_t)v * L * S) + pair]
-                                                             : bin_of(dist, in->time_step, T);
+            const int32_t b = bins_mode == ORACLE_BINS_GIVEN ? vbins[pair] : bin_of(dist, in->time_step, T);
             if (b < 0 || (uint32_t)b >= T) continue;
             /* transient_utils.cuh:11-14 */
             const float I = cube[pair * T + (uint32_t)b];
@@ -297,7 +297,10 @@ int oracle_exhaustive_voxel(const oracle_info* in, const float* cube, const floa
     if (exhaustive_bounces(in, laser_xyz, sensor_xyz, &bl, &bs)) return 1;
 #pragma omp parallel for schedule(dynamic, 16)
     for (int64_t v = 0; v < V; ++v)
-        vol[v] = exhaustive_voxel_value(in, cube, laser_xyz, sensor_xyz, bl, bs, v, bins_mode, bins);
+        vol[v] = exhaustive_voxel_value(in, cube, laser_xyz, sensor_xyz, bl, bs, v, bins_mode,
+                                        bins_mode == ORACLE_BINS_GIVEN
+                                            ? bins + (size_t)v * in->num_laser_targets * in->num_sensor_targets
+                                            : NULL);
     free(bl);
     free(bs);
     return 0;
@@ -305,11 +308,22 @@ int oracle_exhaustive_voxel(const oracle_info* in, const float* cube, const floa
 
 int oracle_exhaustive_voxel_subset(const oracle_info* in, const float* cube, const float* laser_xyz,
                                    const float* sensor_xyz, const int64_t* idx, int64_t n, double* out) {
+    return oracle_exhaustive_voxel_subset_bins(in, cube, laser_xyz, sensor_xyz, idx, n, NULL, out);
+}
+
+/* bins: NULL (FP64 bins) or the GPU's bins of voxel idx[i] at
+ * bins[(i*L + l)*S + s] (fbp_debug_exhaustive_bins' order). */
+int oracle_exhaustive_voxel_subset_bins(const oracle_info* in, const float* cube, const float* laser_xyz,
+                                        const float* sensor_xyz, const int64_t* idx, int64_t n, const int32_t* bins,
+                                        double* out) {
+    const size_t LS = (size_t)in->num_laser_targets * in->num_sensor_targets;
     double *bl, *bs;
     if (exhaustive_bounces(in, laser_xyz, sensor_xyz, &bl, &bs)) return 1;
 #pragma omp parallel for schedule(dynamic, 4)
     for (int64_t i = 0; i < n; ++i)
-        out[i] = exhaustive_voxel_value(in, cube, laser_xyz, sensor_xyz, bl, bs, idx[i], ORACLE_BINS_F64, NULL);
+        out[i] = exhaustive_voxel_value(in, cube, laser_xyz, sensor_xyz, bl, bs, idx[i],
+                                        bins ? ORACLE_BINS_GIVEN : ORACLE_BINS_F64,
+                                        bins ? bins + (size_t)i * LS : NULL);
     free(bl);
     free(bs);
     return 0;

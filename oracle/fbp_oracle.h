@@ -83,6 +83,10 @@ int oracle_exhaustive_voxel(const oracle_info* info, const float* cube, const fl
                             const float* sensor_xyz, int bins_mode, const int32_t* bins, double* vol);
 int oracle_exhaustive_voxel_subset(const oracle_info* info, const float* cube, const float* laser_xyz,
                                    const float* sensor_xyz, const int64_t* idx, int64_t n, double* out);
+/* The same with given bins: bins[(i*L + l)*S + s] for voxel idx[i] (NULL: FP64 bins). */
+int oracle_exhaustive_voxel_subset_bins(const oracle_info* info, const float* cube, const float* laser_xyz,
+                                        const float* sensor_xyz, const int64_t* idx, int64_t n, const int32_t* bins,
+                                        double* out);
 
 /* backprojectConfocal / backprojectExhaustive depth planes
  * (transient_reconstruction.cuh:41-91): act[c*D + d], unweighted. */

@@ -170,20 +170,25 @@ def test_confocal_empty_and_invalid_inputs(ctx, cuda):
         ctx.backproject_confocal(info, cube, lx)
 
 
-@pytest.mark.parametrize("nl,ns,discard", [(3, 4, 1), (4, 3, 0), (2, 5, 1)])
-def test_exhaustive_vs_fp64_oracle(ctx, cuda, nl, ns, discard):
-    """Including L != S, where the reference's own pair split is out of range."""
+@pytest.mark.parametrize("nl,ns,discard,t0,T", [(3, 4, 1, 0.0, 512), (4, 3, 0, 0.0, 512), (2, 5, 1, 0.0, 512),
+                                                 (4, 4, 1, -0.05, 512), (4, 4, 0, 0.2, 512), (3, 4, 1, 0.0, 64),
+                                                 (4, 4, 0, 0.0, 64)])
+def test_exhaustive_vs_fp64_oracle(ctx, cuda, nl, ns, discard, t0, T):
+    """Including L != S, where the reference's own pair split is out of range;
+    laser blocks of 4 (L % 4 == 0) and single lasers; time offsets of zero
+    (the subtraction skipped), negative and positive (conversion bins); and
+    64 bins, where the tile's bin window is capped at the whole row."""
     import torch
     from fasterbackprojection_gb300 import FBP_EXHAUSTIVE, make_info, scenes
 
-    cap = scenes.exhaustive_points(nl, ns, 512, 32e-12, n_points=25, seed=nl * 10 + ns)
+    cap = scenes.exhaustive_points(nl, ns, T, 32e-12, n_points=25, seed=nl * 10 + ns)
     L, S, T = cap.cube.shape
     vres = (20, 18, 22)
     hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 2.0))
     info = make_info(num_laser_targets=L, num_sensor_targets=S, num_time_bins=T, time_step=cap.time_step,
                      voxel_res=vres, hidden_min=hmin, voxel_size=vs, capture_system=FBP_EXHAUSTIVE,
                      discard_first_last_bounces=discard, laser_position=(0.0, -0.2, 0.1),
-                     sensor_position=(0.1, -0.3, 0.0))
+                     sensor_position=(0.1, -0.3, 0.0), time_offset=t0)
     cube = torch.from_numpy(cap.cube).to(cuda)
     lx = torch.from_numpy(cap.laser_xyz).to(cuda)
     sx = torch.from_numpy(cap.sensor_xyz).to(cuda)
@@ -193,6 +198,29 @@ def test_exhaustive_vs_fp64_oracle(ctx, cuda, nl, ns, discard):
     want = cpu.exhaustive_voxel(info, cap.cube, cap.laser_xyz, cap.sensor_xyz, bins=bins)
     assert rel_l2(got, want) < 1e-6
     assert rel_l2(got, cpu.exhaustive_voxel(info, cap.cube, cap.laser_xyz, cap.sensor_xyz)) < 1e-3
+
+
+@pytest.mark.parametrize("nl,ns", [(4, 4), (3, 5)])
+def test_exhaustive_batched_weights_match_reference_weights(ctx, cuda, nl, ns):
+    """Shared reciprocals (the default) against one reciprocal per triple."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_EXHAUSTIVE, make_info, scenes
+
+    cap = scenes.exhaustive_points(nl, ns, 512, 32e-12, n_points=25, seed=77 + nl)
+    L, S, T = cap.cube.shape
+    vres = (24, 20, 28)
+    hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, 2.0))
+    info = make_info(num_laser_targets=L, num_sensor_targets=S, num_time_bins=T, time_step=cap.time_step,
+                     voxel_res=vres, hidden_min=hmin, voxel_size=vs, capture_system=FBP_EXHAUSTIVE)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    sx = torch.from_numpy(cap.sensor_xyz).to(cuda)
+    got = ctx.backproject_exhaustive(info, cube, lx, sx).double()
+    with reference_weights(ctx):
+        want = ctx.backproject_exhaustive(info, cube, lx, sx).double()
+    ctx.check_device_status()
+    assert float(want.abs().max()) > 0
+    assert rel_l2(got.cpu().numpy(), want.cpu().numpy()) < 1e-6
 
 
 def test_exhaustive_fp16_storage(ctx, cuda):

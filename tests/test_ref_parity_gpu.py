@@ -131,7 +131,8 @@ def test_exhaustive_single_pair_bitwise(ctx, harness, cuda):
         lxyz = torch.tensor([[rng.uniform(-1, 1), 0.0, rng.uniform(-1, 1)]], dtype=torch.float32, device=cuda)
         sxyz = torch.tensor([[rng.uniform(-1, 1), 0.0, rng.uniform(-1, 1)]], dtype=torch.float32, device=cuda)
         ref = harness.exhaustive_voxel(info, cube, lxyz, sxyz)
-        got = ctx.backproject_exhaustive(info, cube.view(1, 1, T), lxyz, sxyz)
+        with reference_weights(ctx):
+            got = ctx.backproject_exhaustive(info, cube.view(1, 1, T), lxyz, sxyz)
         torch.cuda.synchronize()
         bad += int((ref.view(torch.int32) != got.view(torch.int32)).sum())
     assert bad == 0
