@@ -1,5 +1,6 @@
-// Launcher of the persistent multi-capture gather for one storage type,
-// instantiated per type in batch_inst_*.cu so the variants compile in parallel.
+// Launcher of the persistent multi-capture gather (FP32 rows for every
+// storage type), instantiated in batch_inst_f32.cu so its variants compile in
+// parallel with the rest of the library.
 #pragma once
 
 #include "bp_gather.cuh"
@@ -11,8 +12,8 @@ namespace fbp {
 struct TileCfg {
     int kv, wy, wz;
 };
-constexpr int kNumTileCfgs = 3;
-constexpr TileCfg kTileCfgs[kNumTileCfgs] = {{8, 2, 4}, {8, 4, 4}, {4, 4, 4}};
+constexpr int kNumTileCfgs = 4;
+constexpr TileCfg kTileCfgs[kNumTileCfgs] = {{16, 2, 4}, {8, 2, 4}, {8, 4, 4}, {4, 4, 4}};
 
 struct BatchLaunch {
     const ConfocalGatherParams* caps;  // device
@@ -76,6 +77,7 @@ static fbp_status batch_dispatch(fbp_context* ctx, const BatchLaunch& b, int cta
         case 0: return batch_dispatch_cfg<S, kTileCfgs[0].kv, kTileCfgs[0].wy, kTileCfgs[0].wz>(ctx, b, ctas, s, occ);
         case 1: return batch_dispatch_cfg<S, kTileCfgs[1].kv, kTileCfgs[1].wy, kTileCfgs[1].wz>(ctx, b, ctas, s, occ);
         case 2: return batch_dispatch_cfg<S, kTileCfgs[2].kv, kTileCfgs[2].wy, kTileCfgs[2].wz>(ctx, b, ctas, s, occ);
+        case 3: return batch_dispatch_cfg<S, kTileCfgs[3].kv, kTileCfgs[3].wy, kTileCfgs[3].wz>(ctx, b, ctas, s, occ);
         default: return set_error(FBP_ERR_INVALID_ARG, "batch: unknown tile configuration");
     }
 }

@@ -351,7 +351,9 @@ fbp_status fbp_batch_run(fbp_batch* batch, int use_graph, void* stream);
 /* Times every voxel-tile shape on this batch and keeps the fastest (index in
  * *chosen).  Synchronises `stream`; drops a captured graph. */
 fbp_status fbp_batch_autotune(fbp_batch* batch, void* stream, int* chosen);
-/* Selects tile shape `config` (0..2) explicitly. */
+/* Selects tile shape `config` (0..3) explicitly: 16 x 16 x 16, 8 x 16 x 16,
+ * 8 x 32 x 16 or 4 x 32 x 16 voxels (x, y, depth); 0 is the single-capture
+ * gather's tile. */
 fbp_status fbp_batch_set_config(fbp_batch* batch, int config, void* stream);
 fbp_status fbp_batch_destroy(fbp_batch* batch);
 

@@ -85,7 +85,7 @@ def test_batch_tile_shapes_agree_with_oracle(ctx, cuda):
         idx = torch.arange(V, dtype=torch.int64, device=cuda)
         bins = ctx.debug_confocal_bins(info, c["lx"], idx).cpu().numpy()
         ref.append(cpu.confocal_voxel(info, c["host"].cube, c["host"].laser_xyz, bins=bins))
-    for cfg in range(3):
+    for cfg in range(4):
         b.set_config(cfg)
         b.run()
         torch.cuda.synchronize()
