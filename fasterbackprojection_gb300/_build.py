@@ -102,7 +102,9 @@ def build_oracle(verbose: bool = False) -> None:
     """CPU oracle + reference-kernel harness (test infrastructure)."""
     oracle = ROOT / "oracle"
     _run(["make", "-s", "-C", str(oracle), "all"])
-    ref_dir = Path(os.environ.get("FBP_REFERENCE_DIR", "/root/reference/FasterBackprojection"))
+    # The reference checkout beside this repository (../reference), unless
+    # FBP_REFERENCE_DIR names its FasterBackprojection/ directory.
+    ref_dir = Path(os.environ.get("FBP_REFERENCE_DIR", str(ROOT.parent / "reference" / "FasterBackprojection")))
     if ref_dir.is_dir():
         _run(["make", "-s", "-C", str(oracle), "ref", f"REF_DIR={ref_dir}"])
 

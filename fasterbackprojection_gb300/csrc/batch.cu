@@ -290,7 +290,7 @@ extern "C" fbp_status fbp_batch_destroy(fbp_batch* b) {
     return guarded("fbp_batch_destroy", [&]() -> fbp_status {
         clear_error();
         if (!b) return FBP_OK;
-        if (b->ctx) cudaSetDevice(b->ctx->device);
+        if (b->ctx) use_device(b->ctx->device);
         cudaDeviceSynchronize();
         drop_graph(b);
         cudaFree(b->rows);

@@ -8,6 +8,7 @@ namespace fbp {
 
 namespace {
 thread_local std::string t_last_error;
+thread_local int t_caller_device = -1;  // the caller's device while a call runs on another
 }
 
 fbp_status set_error(fbp_status st, const std::string& msg) {
@@ -31,12 +32,26 @@ fbp_status fail_quietly(fbp_status st, const char* who, const char* what) noexce
     return st;
 }
 
-fbp_status check_ctx(fbp_context* ctx) {
-    if (!ctx) return set_error(FBP_ERR_INVALID_ARG, "null context");
+fbp_status use_device(int device) {
     int cur = -1;
     FBP_TRY_CUDA(cudaGetDevice(&cur));
-    if (cur != ctx->device) FBP_TRY_CUDA(cudaSetDevice(ctx->device));
+    if (cur != device) {
+        FBP_TRY_CUDA(cudaSetDevice(device));
+        if (t_caller_device < 0) t_caller_device = cur;
+    }
     return FBP_OK;
+}
+
+fbp_status check_ctx(fbp_context* ctx) {
+    if (!ctx) return set_error(FBP_ERR_INVALID_ARG, "null context");
+    return use_device(ctx->device);
+}
+
+void restore_device() noexcept {
+    if (t_caller_device >= 0) {
+        cudaSetDevice(t_caller_device);
+        t_caller_device = -1;
+    }
 }
 
 fbp_status workspace(fbp_context* ctx, int slot, size_t bytes, cudaStream_t stream, void** out) {
@@ -79,7 +94,7 @@ fbp_status fbp_create(fbp_context** out, int device) {
         int n = 0;
         FBP_TRY_CUDA(cudaGetDeviceCount(&n));
         if (device < 0 || device >= n) return set_error(FBP_ERR_INVALID_ARG, "fbp_create: no such device");
-        FBP_TRY_CUDA(cudaSetDevice(device));
+        FBP_TRY(use_device(device));
         cudaDeviceProp prop;
         FBP_TRY_CUDA(cudaGetDeviceProperties(&prop, device));
         if (prop.major < 10) return set_error(FBP_ERR_UNSUPPORTED, "fbp_create: libfbp is built for sm_103a (GB300)");
@@ -104,7 +119,7 @@ fbp_status fbp_destroy(fbp_context* ctx) {
     return guarded("fbp_destroy", [&]() -> fbp_status {
         clear_error();
         if (!ctx) return FBP_OK;
-        cudaSetDevice(ctx->device);
+        use_device(ctx->device);
         cudaDeviceSynchronize();
         for (int i = 0; i < WS_NUM_SLOTS; ++i)
             if (ctx->ws[i]) cudaFree(ctx->ws[i]);

@@ -25,17 +25,23 @@ void clear_error();
 // allocation failure becomes FBP_ERR_OOM, anything else FBP_ERR_INTERNAL,
 // with the message in fbp_last_error() (when there is memory left to keep it).
 fbp_status fail_quietly(fbp_status st, const char* who, const char* what) noexcept;
+// check_ctx makes the context's device current for the call; this puts the
+// caller's device back (a no-op when check_ctx did not switch).
+void restore_device() noexcept;
 template <typename Body>
 fbp_status guarded(const char* who, Body&& body) noexcept {
+    fbp_status st;
     try {
-        return body();
+        st = body();
     } catch (const std::bad_alloc&) {
-        return fail_quietly(FBP_ERR_OOM, who, "host allocation failed");
+        st = fail_quietly(FBP_ERR_OOM, who, "host allocation failed");
     } catch (const std::exception& e) {
-        return fail_quietly(FBP_ERR_INTERNAL, who, e.what());
+        st = fail_quietly(FBP_ERR_INTERNAL, who, e.what());
     } catch (...) {
-        return fail_quietly(FBP_ERR_INTERNAL, who, "unknown exception");
+        st = fail_quietly(FBP_ERR_INTERNAL, who, "unknown exception");
     }
+    restore_device();
+    return st;
 }
 
 #define FBP_TRY_CUDA(expr)                                               \
@@ -110,7 +116,10 @@ struct fbp_context {
 
 namespace fbp {
 
+// Makes ctx's device (or `device`) current for the rest of the call; the
+// guard of the entry point (guarded) restores the caller's device afterwards.
 fbp_status check_ctx(fbp_context* ctx);
+fbp_status use_device(int device);
 // Returns a device buffer of at least `bytes` in slot `slot`.
 fbp_status workspace(fbp_context* ctx, int slot, size_t bytes, cudaStream_t stream, void** out);
 

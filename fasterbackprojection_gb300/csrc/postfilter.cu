@@ -11,7 +11,6 @@
 #include "fbp_internal.cuh"
 
 #include <cmath>
-#include <mutex>
 #include <vector>
 
 namespace fbp {
@@ -479,36 +478,27 @@ extern "C" fbp_status fbp_normalize_minmax(fbp_context* ctx, float* v, uint64_t 
 // but its scratch (one min/max pair per reduction block plus the final pair)
 // lives in this file-scope array instead of context workspace, so the call
 // allocates nothing and needs no fbp_context.  Every device that loads the
-// library holds the array (8 KiB) until the process exits.  One block reduces
-// up to 2^20 elements and there are at most 1024 partial slots, so inputs are
-// limited to 2^30 elements.  All calls on a device share the array: each call
-// overwrites every slot it reads before reading it, and two calls that overlap
-// on the GPU (different streams, no ordering between them) race on it.
+// library holds the array (8 KiB) until the process exits.  The partial pass
+// strides over the input with up to 1024 blocks (4 per SM, like the context
+// entry point), one partial slot each; inputs are limited to 2^30 elements.
+// All calls on a device share the array: each call overwrites every slot it
+// reads before reading it, and two calls that overlap on the GPU (different
+// streams, no ordering between them) race on it.
 namespace fbp {
 constexpr int kNoAllocMaxBlocks = 1024;
-constexpr uint64_t kNoAllocElemsPerBlock = 1ull << 20;
-constexpr int kNoAllocMaxDevices = 64;
+constexpr uint64_t kNoAllocMaxElems = 1ull << 30;
 static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocMaxBlocks + 2];
 
-// Device address of g_noalloc_scratch, resolved once per device (host code
-// must not pass the symbol itself to a kernel: on the host it only names a
-// stand-in object).
-static std::mutex g_noalloc_mu;
-static float* g_noalloc_addr[kNoAllocMaxDevices] = {};
-
+// Device address of g_noalloc_scratch on the current device, looked up on
+// every call (the first call on a device loads the module; later lookups are
+// cheap, and a module reloaded after a device reset gets its new address).
+// Host code must not pass the symbol itself to a kernel: on the host it only
+// names a stand-in object.
 static fbp_status noalloc_scratch(float** out) {
-    int dev = -1;
-    FBP_TRY_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return set_error(FBP_ERR_UNSUPPORTED, "fbp_normalize_minmax_noalloc: device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_error(e, "fbp_normalize_minmax_noalloc: cudaGetSymbolAddress");
-        g_noalloc_addr[dev] = static_cast<float*>(p);
-    }
-    *out = g_noalloc_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_error(e, "fbp_normalize_minmax_noalloc: cudaGetSymbolAddress");
+    *out = static_cast<float*>(p);
     return FBP_OK;
 }
 }  // namespace fbp
@@ -517,14 +507,30 @@ extern "C" fbp_status fbp_normalize_minmax_noalloc(float* v, uint64_t n, void* s
     return guarded("fbp_normalize_minmax_noalloc", [&]() -> fbp_status {
         clear_error();
         if (!v || n == 0) return set_error(FBP_ERR_INVALID_ARG, "fbp_normalize_minmax_noalloc: null buffer or n == 0");
-        if (n > (uint64_t)kNoAllocMaxBlocks * kNoAllocElemsPerBlock)
+        if (n > kNoAllocMaxElems)
             return set_error(FBP_ERR_UNSUPPORTED,
                              "fbp_normalize_minmax_noalloc: n exceeds 2^30 elements (the static scratch holds 1024 "
-                             "partial min/max pairs of 2^20 elements each); use fbp_normalize_minmax");
+                             "partial min/max pairs); use fbp_normalize_minmax");
+        // An error left pending by earlier work is reported as such, not as
+        // this call's launch failure (and left for the caller to clear).
+        const cudaError_t pending = cudaPeekAtLastError();
+        if (pending != cudaSuccess)
+            return cuda_error(pending, "fbp_normalize_minmax_noalloc: a CUDA error was pending before the call");
+        int dev = -1;
+        FBP_TRY_CUDA(cudaGetDevice(&dev));
+        cudaPointerAttributes attr{};
+        FBP_TRY_CUDA(cudaPointerGetAttributes(&attr, v));
+        if ((attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) || attr.device != dev)
+            return set_error(FBP_ERR_INVALID_ARG,
+                             "fbp_normalize_minmax_noalloc: v is not device memory of the current device");
         float* scratch = nullptr;
         FBP_TRY(noalloc_scratch(&scratch));
+        int sms = 0;
+        FBP_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         cudaStream_t s = (cudaStream_t)stream;
-        const int nb = (int)((n + kNoAllocElemsPerBlock - 1) / kNoAllocElemsPerBlock);
+        const uint64_t want = (n + 4ull * kReduceThreads - 1) / (4ull * kReduceThreads);
+        const uint64_t cap = std::min<uint64_t>(kNoAllocMaxBlocks, 4ull * (uint64_t)std::max(sms, 1));
+        const int nb = (int)std::max<uint64_t>(1, std::min(want, cap));
         float* mm = scratch + 2 * kNoAllocMaxBlocks;
         minmax_partial_kernel<<<nb, kReduceThreads, 0, s>>>(v, n, scratch);
         FBP_TRY_CUDA(cudaGetLastError());

@@ -9,6 +9,8 @@
  *
  * Each entry point names the reference interface it replaces
  * (paths relative to the reference's FasterBackprojection/ directory).
+ * A call that takes a context runs on the context's device and leaves the
+ * calling thread's current device as it found it.
  */
 #ifndef FBP_H
 #define FBP_H
@@ -382,11 +384,15 @@ fbp_status fbp_normalize_minmax(fbp_context* ctx, float* v, uint64_t n, void* st
  * For callers that cannot let a library call cudaMalloc — an acquisition
  * loop that reserves the whole device memory budget up front, or a host
  * application whose own allocator owns every device byte.  Needs no
- * context; its scratch is a fixed 8 KiB array inside libfbp on each device,
- * so n is limited to 2^30 elements (FBP_ERR_UNSUPPORTED beyond).  The first
- * call on a device looks up that array's device address; make that first call
- * before any stream capture.  Calls that overlap on the GPU share the array
- * and race; order them (one stream, or events). */
+ * context; runs on the current device, and v must be device memory of that
+ * device (FBP_ERR_INVALID_ARG otherwise).  Its scratch is a fixed 8 KiB array
+ * inside libfbp on each device, so n is limited to 2^30 elements
+ * (FBP_ERR_UNSUPPORTED beyond).  Each call looks up that array's device
+ * address; the first call on a device also loads the library's device code
+ * there, so make that first call before any stream capture.  A CUDA error
+ * already pending when the call starts is returned as FBP_ERR_CUDA without
+ * launching anything (and is not cleared).  Calls that overlap on the GPU
+ * share the array and race; order them (one stream, or events). */
 fbp_status fbp_normalize_minmax_noalloc(float* v, uint64_t n, void* stream);
 
 /* ---- temporal filter ------------------------------------------------------ */

@@ -69,7 +69,8 @@ def reference_lct(lct, data: np.ndarray, width: float, bin_length: float, snr: f
 
 
 def main() -> None:
-    ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    # The reference checkout beside this repository unless given.
+    ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path(__file__).resolve().parents[3] / "reference"
     lct = import_reference_lct(ref_root)
     out = {}
     for U, V, slope in [(4, 8, 0.3), (8, 16, 0.1), (8, 32, 0.05), (16, 16, 0.25)]:

@@ -47,3 +47,13 @@ def test_noalloc_rejects_oversized_input(built, cuda):
     assert st == _lib.FBP_ERR_UNSUPPORTED
     assert b"2^30" in lib.fbp_last_error()
     assert lib.fbp_normalize_minmax_noalloc(None, 16, None) == _lib.FBP_ERR_INVALID_ARG
+
+
+def test_noalloc_rejects_host_memory(built, cuda):
+    from fasterbackprojection_gb300 import _lib
+
+    lib = _lib.load()
+    host = (ctypes.c_float * 64)()
+    st = lib.fbp_normalize_minmax_noalloc(ctypes.cast(host, ctypes.c_void_p), 64, None)
+    assert st == _lib.FBP_ERR_INVALID_ARG
+    assert b"device memory" in lib.fbp_last_error()
