@@ -174,6 +174,53 @@ def profiled_traffic():
     return float(m.group(1)) if m else None
 
 
+# Multi-function unit (XU) of an sm_100-class SM: 16 results per clock (4 per
+# SM sub-partition).  The confocal pair loop issues one sqrt.approx per pair
+# (the reference's bin, irreducible for bit-exact bins) and, with the batched
+# weights, one rcp.approx per two pairs.
+XU_PER_CLK_SM = 16
+MUFU_PER_PAIR = 1.5
+MUFU_PER_PAIR_FLOOR = 1.0
+
+
+def gather_roofline(samples, bp_ms, clocks, hbm_peak, hbm_kind):
+    """Roofline of the dominant kernel (the confocal gather).  It is bound by
+    the XU (MUFU) pipe and instruction issue, not by HBM: the bound is stated
+    in voxel-samples per clock per SM against the XU ceiling of its own
+    arithmetic, at the SM clock sampled during the timed region.  The
+    bytes-per-sample accounting (4 B, the cube element the reference gathers
+    per pair) is kept as a separate, labelled figure."""
+    rate = samples / (bp_ms / 1e3)
+    sms = 152
+    try:
+        import torch
+
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    except Exception:
+        pass
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    per_clk_sm = rate / (sms * mhz * 1e6)
+    peak = XU_PER_CLK_SM / MUFU_PER_PAIR
+    floor = XU_PER_CLK_SM / MUFU_PER_PAIR_FLOOR
+    hbm_achieved = samples * 4 / (bp_ms / 1e3) / 1e9
+    return {
+        "bound": "mufu", "achieved": per_clk_sm, "peak": peak, "unit": "voxel-samples/clk/SM",
+        "frac": per_clk_sm / peak, "traffic": profiled_traffic(),
+        "peak_basis": f"{XU_PER_CLK_SM} XU results/clk/SM / {MUFU_PER_PAIR} MUFU ops per pair (sqrt.approx + "
+                      f"rcp.approx per two pairs) at the sampled {mhz:.0f} MHz x {sms} SMs = "
+                      f"{peak * sms * mhz * 1e6:.3e} voxel-samples/s",
+        "frac_of_bitwise_bin_floor": per_clk_sm / floor,
+        "bitwise_bin_floor_note": f"{floor:.0f} voxel-samples/clk/SM: one sqrt.approx per pair, the least any "
+                                  "kernel with the reference's bins needs",
+        "hbm_accounting": {"achieved_gbs": hbm_achieved, "peak_gbs": hbm_peak, "frac": hbm_achieved / hbm_peak,
+                           "peak_source": hbm_kind,
+                           "note": "4 B per voxel-sample (the element the reference gathers per pair) / gather "
+                                   "launch time; windows are served from shared memory, so this exceeds HBM and "
+                                   "is not the limiter"},
+        "traffic_note": "dram read + write bytes per gather launch from the committed ncu summary (profiles/)",
+    }
+
+
 # --------------------------------------------------------------- workloads
 
 def make_workload(device, seed: int, size: str):
@@ -330,7 +377,7 @@ def run_ours(args):
             extras["exhaustive"] = exhaustive_leg(ctx, dev)
 
     peak, peak_kind = measured_peaks()
-    achieved = samples * 4 / (bp_ms / 1e3) / 1e9
+    clocks = clk.summary()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -340,17 +387,14 @@ def run_ours(args):
                    "volume": list(info.voxel_res), "storage": "f32", "postfilter": "LoG k=5 sigma=1",
                    "l2": "inputs larger than L2 (cube 256 MiB)", "per_gpu": "one capture per rank"},
         "e2e": e2e,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": profiled_traffic(), "peak_source": peak_kind,
-                     "note": "achieved = 4 B per voxel-sample / gather launch time; the gather is "
-                             "FP32/MUFU issue-bound, see profiles/"},
+        "roofline": gather_roofline(samples, bp_ms, clocks, peak, peak_kind),
         "bp_ms_per_launch": bp_ms,
         "gpu_launches": launches,
     }
     if not args.no_extras and rank == 0 and ws == 1:
         line["cpu_baseline"] = cpu_baseline(info, cube, lx)
         line.update(extras)
-    line["clocks"] = clk.summary()
+    line["clocks"] = clocks
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -851,16 +895,57 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
     _, log_ms = timed_ms(lambda: ctx.postfilter(FBP_FILTER_LOG, vol, 5, 1.0, out=out))
     tmp = out.clone()
     _, norm_ms = timed_ms(lambda: ctx.normalize_(tmp))
+    # The allocation-free entry point on the same volume (same result bits).
+    import ctypes
+
+    from fasterbackprojection_gb300 import _lib
+
+    lib = _lib.load()
+    tmp2 = out.clone()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _, na_ms = timed_ms(lambda: lib.fbp_normalize_minmax_noalloc(ctypes.c_void_p(tmp2.data_ptr()), V, sp))
     res = {"log": {"ms": log_ms, "bytes": 8 * V, "achieved_gbs": 8 * V / (log_ms / 1e3) / 1e9,
                    "frac": 8 * V / (log_ms / 1e3) / 1e9 / peak},
            "normalize": {"ms": norm_ms, "bytes": 12 * V, "achieved_gbs": 12 * V / (norm_ms / 1e3) / 1e9,
-                         "frac": 12 * V / (norm_ms / 1e3) / 1e9 / peak}}
+                         "frac": 12 * V / (norm_ms / 1e3) / 1e9 / peak,
+                         "noalloc_ms": na_ms, "noalloc_bitwise_equal": bool(torch.equal(tmp, tmp2))}}
     c = cube.clone()
     nb = c.numel()
     _, fh_ms = timed_ms(lambda: ctx.filter_h_(c, time_step))
     res["filter_h"] = {"ms": fh_ms, "bytes": 8 * nb, "achieved_gbs": 8 * nb / (fh_ms / 1e3) / 1e9,
                        "frac": 8 * nb / (fh_ms / 1e3) / 1e9 / peak,
                        "workload": "256^2 series x 1024 bins, wavelength 10 bins (taps over 1106 padded bins)"}
+    # The reference's filter_H arithmetic path (Laser.cu:174-234) on the same
+    # GPU: zero-padded series, batched C2C FFT (cuFFT through torch), the
+    # product with the filter's spectrum, unnormalised inverse, real part.
+    try:
+        import numpy as np
+
+        from oracle import numpy_ref
+
+        T = cube.shape[-1]
+        Ls = nb // T
+        sigma, _t6, npad = numpy_ref.filter_h_params(T, time_step, 10 * time_step)
+        K = numpy_ref.filter_h_kernel(npad, float(np.float32(time_step)), float(np.float32(10 * time_step)), sigma)
+        pad = (npad - T) // 2
+        Kf = torch.fft.fft(torch.from_numpy(K.astype(np.complex64)).to(cube.device))
+        Hs = torch.zeros((Ls, npad), dtype=torch.complex64, device=cube.device)
+        src = cube.reshape(Ls, T)
+        ref_c = torch.empty_like(src)
+
+        def cufft_filter_h():
+            Hs.zero_()
+            Hs[:, pad:pad + T] = src
+            ref_c.copy_(torch.fft.ifft(torch.fft.fft(Hs, dim=1) * Kf[None], dim=1, norm="forward")[:, pad:pad + T].real)
+
+        _, rf_ms = timed_ms(cufft_filter_h)
+        res["filter_h"]["reference_cufft_c2c_ms"] = rf_ms
+        res["filter_h"]["speedup_vs_cufft_pipeline"] = rf_ms / fh_ms
+        res["filter_h"]["rel_l2_vs_cufft_pipeline"] = float(
+            torch.linalg.vector_norm((c.reshape(Ls, T) - ref_c).double()) / torch.linalg.vector_norm(ref_c.double()))
+        del Hs
+    except RuntimeError as e:  # pragma: no cover
+        res["filter_h"]["reference_cufft_unavailable"] = str(e)
     # LoG-FFT (LoGFFT::compute): ours against the reference's own arithmetic
     # path, an R2C FFT, the half-grid response and a C2R FFT through cuFFT
     # (the library the reference calls), on the same volume.
@@ -1015,7 +1100,10 @@ def run_reference(args):
     V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": V * L / value * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": V * L / value * 1e3, "ms_per_step_kind":
+            "extrapolated: each step times a bounded voxel sample (cpu_baseline.sample) and scales its rate to "
+            "the full workload; no full step ran",
+        "measured_wall_s_per_step": dt, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "volume": list(info.voxel_res), "scan": [int(round(L ** 0.5))] * 2,
                    "bins": N_BINS},

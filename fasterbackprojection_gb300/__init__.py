@@ -20,8 +20,11 @@ from ._lib import (  # noqa: F401
     FBP_LAYOUT_TIME_MAJOR,
     FBP_LCT_GRID_DEPTH,
     FBP_LCT_GRID_REFERENCE,
+    FBP_LCT_OUTPUT_CLAMPED_REAL,
+    FBP_LCT_OUTPUT_MAGNITUDE,
     FBP_MIS_LEARNED,
     FBP_MIS_REFERENCE,
+    FBP_MIS_REFERENCE_SCATTER,
     FBP_MIS_SPATIAL,
     FBP_MIS_UNIFORM,
     FBP_WEIGHTS_BATCHED,

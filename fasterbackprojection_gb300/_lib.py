@@ -73,10 +73,12 @@ class LctParams(ctypes.Structure):
         ("snr", c_float),
         ("diffuse", c_int),
         ("grid_mode", c_int),
+        ("output", c_int),
     ]
 
 
 FBP_LCT_GRID_REFERENCE, FBP_LCT_GRID_DEPTH = 0, 1
+FBP_LCT_OUTPUT_CLAMPED_REAL, FBP_LCT_OUTPUT_MAGNITUDE = 0, 1
 
 
 class MisParams(ctypes.Structure):
@@ -93,7 +95,7 @@ class MisParams(ctypes.Structure):
     ]
 
 
-FBP_MIS_UNIFORM, FBP_MIS_SPATIAL, FBP_MIS_LEARNED, FBP_MIS_REFERENCE = 0, 1, 2, 3
+FBP_MIS_UNIFORM, FBP_MIS_SPATIAL, FBP_MIS_LEARNED, FBP_MIS_REFERENCE, FBP_MIS_REFERENCE_SCATTER = 0, 1, 2, 3, 4
 FBP_MLP_FEATURES = 20
 
 
@@ -140,6 +142,8 @@ SIGNATURES = {
                                         c_void_p]),
     "fbp_debug_exhaustive_bins": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_void_p, c_void_p, c_uint64,
                                           c_void_p, c_void_p]),
+    "fbp_debug_confocal_paths": (c_int, [c_void_p, POINTER(ReconInfo), c_void_p, c_void_p, c_uint64, c_void_p,
+                                         c_void_p, c_void_p]),
     "fbp_linear_space": (c_int, [c_double, c_double, c_int, POINTER(c_double)]),
     "fbp_postfilter": (c_int, [c_void_p, c_int, c_int, c_float, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32,
                                c_void_p]),

@@ -301,6 +301,17 @@ class Context:
                                                 voxel_idx.numel(), _ptr(out), self._stream(stream)))
         return out
 
+    def debug_confocal_paths(self, info: ReconInfo, laser_xyz, voxel_idx, stream=None):
+        """(paths [n][L] float32, (rcp_dt, half voxel diagonal)) in the gathers' FP32 arithmetic."""
+        import torch
+
+        out = torch.empty((voxel_idx.numel(), info.num_laser_targets), dtype=torch.float32, device=laser_xyz.device)
+        consts = torch.empty(2, dtype=torch.float32, device=laser_xyz.device)
+        check(self._lib.fbp_debug_confocal_paths(self._h, byref(info), _ptr(laser_xyz), _ptr(voxel_idx),
+                                                 voxel_idx.numel(), _ptr(out), _ptr(consts), self._stream(stream)))
+        c = consts.cpu()
+        return out, (float(c[0]), float(c[1]))
+
     def debug_exhaustive_bins(self, info: ReconInfo, laser_xyz, sensor_xyz, voxel_idx, stream=None):
         import torch
 
@@ -368,8 +379,9 @@ class Context:
     # ------------------------------------------------------------------- LCT
     def lct(self, data, width: float, bin_length: float, snr: float = 0.8, diffuse: bool = True,
             grid_mode: int = _lib.FBP_LCT_GRID_REFERENCE, layout: int = _lib.FBP_LAYOUT_TIME_MAJOR, out=None,
-            stream=None):
-        """Confocal LCT.  data: [M][N][N] (time-major) or [N][N][M] (time-inner), float32."""
+            stream=None, output: int = _lib.FBP_LCT_OUTPUT_CLAMPED_REAL):
+        """Confocal LCT.  data: [M][N][N] (time-major) or [N][N][M] (time-inner), float32.
+        python/lct_2.py's variant: grid_mode=FBP_LCT_GRID_DEPTH, output=FBP_LCT_OUTPUT_MAGNITUDE."""
         import torch
 
         if layout == _lib.FBP_LAYOUT_TIME_MAJOR:
@@ -378,7 +390,7 @@ class Context:
             N, _, M = data.shape
         if out is None:
             out = torch.empty((M, N, N), dtype=torch.float32, device=data.device)
-        prm = LctParams(width, bin_length, snr, int(diffuse), grid_mode)
+        prm = LctParams(width, bin_length, snr, int(diffuse), grid_mode, output)
         check(self._lib.fbp_lct(self._h, _ptr(data, M * N * N, _f32(), "data"), layout, N, M, byref(prm),
                                 _ptr(out, M * N * N, _f32(), "out"), self._stream(stream)))
         return out

@@ -145,15 +145,23 @@ def views(vol: np.ndarray) -> dict[str, np.ndarray]:
 
 
 def reconstruct(ctx, rect_data, width: float, s: Settings = Settings(),
-                grid_mode: int = _lib.FBP_LCT_GRID_REFERENCE, crop: bool = True, device=None, stream=None):
+                grid_mode: int = _lib.FBP_LCT_GRID_REFERENCE, crop: bool = True, device=None, stream=None,
+                variant: str = "lct"):
     """cnlos_reconstruction without the plots: the host preparation, the LCT
     on the GPU (fbp_lct on the [M][N][N] time-major data), then the display
-    crop.  Returns a tensor on the context's device."""
+    crop.  variant "lct_2" is python/lct_2.py's form: per-depth radiometry
+    and abs(vol) (grid_mode is then ignored).  Returns a tensor on the
+    context's device."""
     import torch
 
+    if variant not in ("lct", "lct_2"):
+        raise ValueError("variant must be 'lct' or 'lct_2'")
     p = prepare(rect_data, s)
     dev = device if device is not None else torch.device("cuda", ctx.device)
     data = torch.from_numpy(p.data).to(dev)
+    if variant == "lct_2":
+        grid_mode = _lib.FBP_LCT_GRID_DEPTH
+    output = _lib.FBP_LCT_OUTPUT_MAGNITUDE if variant == "lct_2" else _lib.FBP_LCT_OUTPUT_CLAMPED_REAL
     vol = ctx.lct(data, width, p.bin_length, snr=s.snr, diffuse=s.isdiffuse, grid_mode=grid_mode,
-                  layout=_lib.FBP_LAYOUT_TIME_MAJOR, stream=stream)
+                  layout=_lib.FBP_LAYOUT_TIME_MAJOR, stream=stream, output=output)
     return display_crop(vol, p, width) if crop else vol

@@ -10,6 +10,19 @@
 #include <mutex>
 #include <sys/stat.h>
 
+
+// The reference selects its voxel-scattering kernels at compile time
+// (ACCUMULATE_VOXEL_SCATTERING, transient_reconstruction.cuh:112-126,
+// 235-250); building this file with the same macro selects the matching
+// entry points.
+#ifdef ACCUMULATE_VOXEL_SCATTERING
+static constexpr auto kConfocalGather = fbp_backproject_confocal_scatter;
+static constexpr int kMisReferenceProposal = FBP_MIS_REFERENCE_SCATTER;
+#else
+static constexpr auto kConfocalGather = fbp_backproject_confocal;
+static constexpr int kMisReferenceProposal = FBP_MIS_REFERENCE;
+#endif
+
 namespace {
 
 void check(fbp_status st, const char* what) {
@@ -309,8 +322,8 @@ void Laser::reconstructShape(const TransientParameters& tp) {
             check(exhaustive ? fbp_backproject_exhaustive(ctx, &in, buf._intensity, FBP_F32,
                                                           reinterpret_cast<float*>(buf._laserTargets),
                                                           reinterpret_cast<float*>(buf._sensorTargets), vol, nullptr)
-                             : fbp_backproject_confocal(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
-                                                        reinterpret_cast<float*>(buf._laserTargets), vol, nullptr),
+                             : kConfocalGather(ctx, &in, buf._intensity, FBP_F32, FBP_LAYOUT_TIME_INNER,
+                                               reinterpret_cast<float*>(buf._laserTargets), vol, nullptr),
                   "backprojection");
             postprocessingFilter(tp._postprocessingFilterType)
                 ->compute(vol, fbpref::uvec3(in.voxel_res[0], in.voxel_res[1], in.voxel_res[2]), tp);
@@ -371,7 +384,7 @@ void Laser::reconstructAABBConfocalMIS(float* volume, const ReconstructionInfo& 
     DeviceArray<float> cube(_nlosData->_data.data(), _nlosData->_data.size());
     DeviceArray<fbpref::vec3> lx(_nlosData->_laserGridPositions.data(), _nlosData->_laserGridPositions.size());
     fbp_mis_params prm{};
-    prm.proposal = FBP_MIS_REFERENCE;
+    prm.proposal = kMisReferenceProposal;
     prm.samples = 0;  // L / 4 (Laser.cu:590)
     check(fbp_mis_backproject(fbp_default_context(), &recInfo, cube.get(), FBP_F32, FBP_LAYOUT_TIME_INNER,
                               reinterpret_cast<const float*>(lx.get()), &prm, volume, nullptr),

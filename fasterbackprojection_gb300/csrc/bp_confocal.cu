@@ -432,6 +432,31 @@ __global__ void debug_confocal_bins_kernel(fbp_recon_info in, const float4* __re
     bins[i] = (b >= 0 && b < (int)in.num_time_bins) ? b : -1;
 }
 
+// The path (dist) of each pair in the gathers' FP32 expression, and the two
+// per-call constants of the scattering walk: rcp.approx(timeStep) and half the
+// voxel diagonal.
+__global__ void debug_confocal_paths_kernel(fbp_recon_info in, const float4* __restrict__ scan,
+                                            const int64_t* __restrict__ vidx, uint64_t nv, float* __restrict__ paths,
+                                            float* __restrict__ consts) {
+    const uint64_t L = in.num_laser_targets;
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i == 0 && consts) {
+        consts[0] = rcp_approx(in.time_step);
+        consts[1] = mul_rn(0.5f, sqrt_approx(ref_dot3(in.voxel_size[0], in.voxel_size[1], in.voxel_size[2])));
+    }
+    if (i >= nv * L) return;
+    const uint64_t vi = i / L, l = i % L;
+    uint32_t vx, vy, vz;
+    voxel_of(vidx[vi], in.voxel_res[0], in.voxel_res[1], vx, vy, vz);
+    const float px = ref_voxel_coord(vx, in.voxel_size[0], in.hidden_min[0]);
+    const float py = ref_voxel_coord(vz, in.voxel_size[1], in.hidden_min[1]);
+    const float pz = ref_voxel_coord(vy, in.voxel_size[2], in.hidden_min[2]);
+    const float4 g = scan[l];
+    float dist = fma_rn(sqrt_approx(ref_dot3(sub_rn(px, g.x), sub_rn(py, g.y), sub_rn(pz, g.z))), 2.f, -in.time_offset);
+    if (in.discard_first_last_bounces == 0) dist = add_rn(dist, g.w);
+    paths[i] = dist;
+}
+
 __global__ void debug_exhaustive_bins_kernel(fbp_recon_info in, const float4* __restrict__ lscan,
                                              const float4* __restrict__ sscan, const int64_t* __restrict__ vidx,
                                              uint64_t nv, int32_t* __restrict__ bins) {
@@ -471,6 +496,26 @@ extern "C" fbp_status fbp_debug_confocal_bins(fbp_context* ctx, const fbp_recon_
         if (n == 0) return FBP_OK;
         debug_confocal_bins_kernel<<<cdiv(n, 256), 256, 0, s>>>(*info, scan, voxel_idx, num_voxels, bins);
         FBP_CHECK_LAUNCH(ctx, "debug_confocal_bins_kernel");
+        return FBP_OK;
+    });
+}
+
+extern "C" fbp_status fbp_debug_confocal_paths(fbp_context* ctx, const fbp_recon_info* info, const float* laser_xyz,
+                                               const int64_t* voxel_idx, uint64_t num_voxels, float* paths,
+                                               float* consts, void* stream) {
+    return guarded("fbp_debug_confocal_paths", [&]() -> fbp_status {
+        clear_error();
+        FBP_TRY(check_ctx(ctx));
+        FBP_TRY(validate_info(info, false, "fbp_debug_confocal_paths"));
+        if (!laser_xyz || !voxel_idx || !paths || !consts)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_debug_confocal_paths: null buffer");
+        cudaStream_t s = (cudaStream_t)stream;
+        const float4* scan;
+        const float *xs, *ys, *zs;
+        FBP_TRY(build_tables(ctx, *info, laser_xyz, s, &scan, &xs, &ys, &zs));
+        const uint64_t n = std::max<uint64_t>(num_voxels * info->num_laser_targets, 1);
+        debug_confocal_paths_kernel<<<cdiv(n, 256), 256, 0, s>>>(*info, scan, voxel_idx, num_voxels, paths, consts);
+        FBP_CHECK_LAUNCH(ctx, "debug_confocal_paths_kernel");
         return FBP_OK;
     });
 }

@@ -70,6 +70,7 @@ struct LctFusedInputs {
     int power, tiled;
     const float2* wiener;         // [2M][2N][2N]
     float* volume;                // [M][N][N]
+    int magnitude;                // 1: |vol| (lct_2.py), 0: max(real(vol), 0) (lct.py)
 };
 // The LoG-FFT filter on the half spectrum (log_fft.cu): every axis a power of
 // two in [32, 1024].

@@ -9,7 +9,8 @@
 //      PSF, inverse 3-D FFT                           -> 5 line-FFT passes, the
 //      z pass doing forward * filter * inverse at once; lines that are zero
 //      padding or not needed in the output are skipped
-//   3. unpad, inverse resample with mtxi = mtx^T, max(real, 0).
+//   3. unpad, inverse resample with mtxi = mtx^T, max(real, 0) (lct.py) or
+//      the magnitude (lct_2.py).
 // The PSF's Wiener filter and the resampling operator depend only on
 // (N, M, slope, snr) and stay cached in the context.  FP64 is used for the
 // PSF construction and the Wiener normalisation; the transforms are FP32.
@@ -57,18 +58,22 @@ __global__ void lct_wiener_kernel(float2* __restrict__ f, size_t n, const unsign
     }
 }
 
-// Step 3: vol[z', y, x] = max(Re(sum_k val[k] * buf[col[k], y, x]) * scale, 0).
+// Step 3: with c = sum_k val[k] * buf[col[k], y, x] * scale (mtxi is real),
+// vol[z', y, x] = max(Re c, 0) (lct.py) or |c| (magnitude, lct_2.py).
 __global__ void lct_unresample_kernel(const float2* __restrict__ buf, const int* __restrict__ rowptr,
                                       const int* __restrict__ colidx, const float* __restrict__ val, int N, int M,
-                                      int X, float scale, float* __restrict__ vol) {
+                                      int X, float scale, int magnitude, float* __restrict__ vol) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= (size_t)M * N * N) return;
     const int zp = (int)(i / ((size_t)N * N));
     const int y = (int)((i / N) % N), x = (int)(i % N);
-    float acc = 0.f;
-    for (int k = rowptr[zp]; k < rowptr[zp + 1]; ++k)
-        acc = fmaf(val[k], buf[((size_t)colidx[k] * X + y) * X + x].x, acc);
-    vol[i] = fmaxf(acc * scale, 0.f);
+    float re = 0.f, im = 0.f;
+    for (int k = rowptr[zp]; k < rowptr[zp + 1]; ++k) {
+        const float2 b = buf[((size_t)colidx[k] * X + y) * X + x];
+        re = fmaf(val[k], b.x, re);
+        im = fmaf(val[k], b.y, im);
+    }
+    vol[i] = magnitude ? sqrtf(re * re + im * im) * scale : fmaxf(re * scale, 0.f);
 }
 
 namespace {
@@ -261,6 +266,7 @@ fbp_status lct_run(fbp_context* ctx, const float* data, int layout, uint32_t N, 
         fi.tiled = prm.grid_mode == FBP_LCT_GRID_REFERENCE;
         fi.wiener = invpsf;
         fi.volume = volume;
+        fi.magnitude = prm.output == FBP_LCT_OUTPUT_MAGNITUDE;
         return lct_fused_run(ctx, fi, s);
     }
     void* a = nullptr;
@@ -326,7 +332,8 @@ fbp_status lct_run(fbp_context* ctx, const float* data, int layout, uint32_t N, 
     // 6. unpad, inverse resample (mtxi = mtx^T), normalise the inverse FFT, clamp.
     const size_t nout = (size_t)M * N * N;
     lct_unresample_kernel<<<cdiv(nout, 256), 256, 0, s>>>(buf, op.rpt, op.cit, op.vt, (int)N, (int)M, X,
-                                                          (float)(1.0 / (double)nfull), volume);
+                                                          (float)(1.0 / (double)nfull),
+                                                          prm.output == FBP_LCT_OUTPUT_MAGNITUDE, volume);
     FBP_CHECK_LAUNCH(ctx, "lct_unresample_kernel");
     return FBP_OK;
 }
@@ -345,6 +352,8 @@ extern "C" fbp_status fbp_lct(fbp_context* ctx, const float* data, int layout, u
             return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: unknown layout");
         if (params->grid_mode != FBP_LCT_GRID_REFERENCE && params->grid_mode != FBP_LCT_GRID_DEPTH)
             return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: unknown grid mode");
+        if (params->output != FBP_LCT_OUTPUT_CLAMPED_REAL && params->output != FBP_LCT_OUTPUT_MAGNITUDE)
+            return set_error(FBP_ERR_INVALID_ARG, "fbp_lct: unknown output mode");
         return lct_run(ctx, data, layout, N, M, *params, volume, (cudaStream_t)stream);
     });
 }

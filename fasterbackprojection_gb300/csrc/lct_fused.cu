@@ -17,7 +17,8 @@
 //      filter, inverse column and row FFTs; stores the N x N corner back.
 //   3. lct_zinv_kernel: per (y, x), inverse 2M-point FFT along z, then rows
 //      z < M of mtx^T (the inverse resample), the 1/(2M 2N 2N) normalisation
-//      and max(., 0); stores vol[z][y][x].
+//      and max(real, 0) (lct.py) or the magnitude (lct_2.py); stores
+//      vol[z][y][x].
 // The FFTs are Stockham passes (radix 16 or 8, then 4 or 2) with compile-time
 // sizes; each pass reads its twiddles from a per-stage table
 // exp(-2 pi i r jm / (Ns R)) built in double precision on the host.
@@ -47,6 +48,7 @@ struct LctFusedParams {
     float2* pad;                  // [2M][N][2N]: rows of the padded planes (N > 64 only)
     float* vol;                   // [M][N][N]
     float scale;                  // 1 / (2M * 2N * 2N)
+    int magnitude;                // 1: |vol| (lct_2.py), 0: max(real(vol), 0) (lct.py)
 };
 
 constexpr int kZThreads = 512;
@@ -208,9 +210,14 @@ __global__ void __launch_bounds__(kZThreads, 2) lct_zinv_kernel(LctFusedParams p
     for (int e = threadIdx.x; e < C * M; e += kZThreads) {
         const int i = e % C, z = e / C;
         if (x0 + i >= N) continue;
-        float acc = 0.f;
-        for (int k = p.rpt[z]; k < p.rpt[z + 1]; ++k) acc = fmaf(p.vt[k], lines[i * LS + pidx(p.cit[k])].x, acc);
-        p.vol[((size_t)z * N + y) * N + x0 + i] = fmaxf(acc * p.scale, 0.f);
+        float re = 0.f, im = 0.f;
+        for (int k = p.rpt[z]; k < p.rpt[z + 1]; ++k) {
+            const float2 b = lines[i * LS + pidx(p.cit[k])];
+            re = fmaf(p.vt[k], b.x, re);
+            im = fmaf(p.vt[k], b.y, im);
+        }
+        p.vol[((size_t)z * N + y) * N + x0 + i] =
+            p.magnitude ? sqrtf(re * re + im * im) * p.scale : fmaxf(re * p.scale, 0.f);
     }
 }
 
@@ -446,6 +453,7 @@ fbp_status lct_fused_run(fbp_context* ctx, const LctFusedInputs& in, cudaStream_
     p.tiled = in.tiled;
     p.wiener = in.wiener;
     p.vol = in.volume;
+    p.magnitude = in.magnitude;
     p.scale = (float)(1.0 / ((double)(2 * M) * (double)(2 * N) * (double)(2 * N)));
     FBP_TRY(stage_twiddles(ctx, log2z, s, &p.tw_z));
     FBP_TRY(stage_twiddles(ctx, log2x, s, &p.tw_x));

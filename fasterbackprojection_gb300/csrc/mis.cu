@@ -81,6 +81,7 @@ struct MisRefParams {
     float t0, dt;
     int bounce;
     float* volume;
+    float vs[3];  // voxel size: the scattering walk's extent |vs| / 2
 };
 
 __device__ __forceinline__ float noise_next(const float* noise, uint32_t n, uint32_t& state) {
@@ -116,7 +117,13 @@ __device__ __forceinline__ void mis_draw(const MisRefParams& p, uint32_t state, 
     a = pdf * ref_safe_rcp(gpdf);  // the balance weight
 }
 
-template <typename S>
+// SCATTER: the reference's ACCUMULATE_VOXEL_SCATTERING build of the kernel
+// (transient_reconstruction.cuh:235-250): each sample adds
+// (weight * I) * safeRCP(dist^2) for every bin of d = max(0, dist - e),
+// d += timeStep + EPS while d < dist + e (e half the voxel diagonal), and
+// stops at the first bin outside [0, T); the reference adds each term with an
+// atomic, one rounding per add, so the terms are added (not fused) in order.
+template <typename S, bool SCATTER>
 __global__ void __launch_bounds__(kMisVoxels) mis_reference_kernel(MisRefParams p) {
     __shared__ float4 s_scan[kMisVoxels + kMisChunk - 1];
     __shared__ float2 s_draw[kMisVoxels + kMisChunk - 1];  // (weight, scan point index bits)
@@ -135,6 +142,12 @@ __global__ void __launch_bounds__(kMisVoxels) mis_reference_kernel(MisRefParams 
     const float invL = ref_safe_rcp((float)p.L);
     const S* rows = static_cast<const S*>(p.rows);
     float ksum = 0.f, kcomp = 0.f, acc = 0.f;
+    // length(voxelSize) / 2 and the step timeStep + EPS in the reference's FP32.
+    const float ext = SCATTER ? mul_rn(0.5f, sqrt_approx(ref_dot3(p.vs[0], p.vs[1], p.vs[2]))) : 0.f;
+    const float step = SCATTER ? add_rn(p.dt, FBP_EPS) : 0.f;
+    // A bound on the walk's steps (only a path so long that adding the step
+    // no longer changes it could exceed it; such a path reaches no bin).
+    const int max_it = SCATTER ? (int)(2.f * ext / step) + 4 : 0;
     for (uint32_t s0 = 0; s0 < p.samples; s0 += kMisChunk) {
         const uint32_t ce = min(kMisChunk, p.samples - s0), ntab = kMisVoxels + ce - 1;
         __syncthreads();  // the previous chunk's table is no longer read
@@ -148,6 +161,36 @@ __global__ void __launch_bounds__(kMisVoxels) mis_reference_kernel(MisRefParams 
         __syncthreads();
         if (!live) continue;
         const uint32_t r = t % ce;
+        if constexpr (SCATTER) {
+            for (uint32_t k = 0; k < ce; ++k) {
+                const uint32_t e = t + (k >= r ? k - r : k + ce - r);
+                const float4 g = s_scan[e];
+                const float2 d = s_draw[e];
+                float dist = fma_rn(sqrt_approx(ref_dot3(sub_rn(px, g.x), sub_rn(py, g.y), sub_rn(pz, g.z))), 2.f,
+                                    -p.t0);
+                if (p.bounce) dist = add_rn(dist, g.w);
+                const float w = ref_safe_rcp(mul_rn(dist, dist));
+                const S* row = rows + (uint64_t)__float_as_uint(d.y) * p.pitch;
+                float dd = fmaxf(0.f, sub_rn(dist, ext));
+                const float dmax = add_rn(dist, ext);
+                for (int it = 0; dd < dmax && it < max_it; ++it) {
+                    const int b = __float2int_rz(ref_bin_ratio(dd, rcp_dt));
+                    if (b < 0 || b >= (int)p.T) break;
+                    const float I = to_f32(row[b]);
+                    if (I > FBP_EPS) acc = add_rn(acc, mul_rn(mul_rn(d.x, I), w));
+                    dd = add_rn(dd, step);
+                }
+                const uint32_t n = s0 + k;
+                if ((n & 63) == 63 || n + 1 == p.samples) {
+                    const float y = sub_rn(acc, kcomp);
+                    const float tt = add_rn(ksum, y);
+                    kcomp = sub_rn(sub_rn(tt, ksum), y);
+                    ksum = tt;
+                    acc = 0.f;
+                }
+            }
+            continue;
+        }
         // U steps at a time: their cube reads are in flight together; the
         // terms are added in step order.
         constexpr int U = 4;
@@ -438,7 +481,7 @@ static fbp_status mis_run(fbp_context* ctx, const fbp_recon_info& in, const void
     float* d_spatial = d_pl + L;
     uint32_t* d_alias = reinterpret_cast<uint32_t*>(d_spatial + L);
 
-    if (prm.proposal == FBP_MIS_REFERENCE) {
+    if (prm.proposal == FBP_MIS_REFERENCE || prm.proposal == FBP_MIS_REFERENCE_SCATTER) {
         std::vector<float> cdf, prob;
         std::vector<uint32_t> alias;
         FBP_TRY(reference_tables(raw, cdf, alias, prob));
@@ -487,7 +530,14 @@ static fbp_status mis_run(fbp_context* ctx, const fbp_recon_info& in, const void
         p.dt = in.time_step;
         p.bounce = in.discard_first_last_bounces == 0;
         p.volume = volume;
-        mis_reference_kernel<S><<<cdiv(V, kMisVoxels), kMisVoxels, 0, s>>>(p);
+        for (int k = 0; k < 3; ++k) p.vs[k] = in.voxel_size[k];
+        if (prm.proposal == FBP_MIS_REFERENCE_SCATTER) {
+            if (!(in.time_step > 1e-4f))
+                return set_error(FBP_ERR_UNSUPPORTED, "fbp_mis_backproject: the scattering walk needs time_step > 0.1 mm");
+            mis_reference_kernel<S, true><<<cdiv(V, kMisVoxels), kMisVoxels, 0, s>>>(p);
+        } else {
+            mis_reference_kernel<S, false><<<cdiv(V, kMisVoxels), kMisVoxels, 0, s>>>(p);
+        }
         FBP_CHECK_LAUNCH(ctx, "mis_reference_kernel");
         return FBP_OK;
     }

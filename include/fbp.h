@@ -187,6 +187,15 @@ fbp_status fbp_debug_confocal_bins(fbp_context* ctx, const fbp_recon_info* info,
 fbp_status fbp_debug_exhaustive_bins(fbp_context* ctx, const fbp_recon_info* info, const float* laser_xyz,
                                      const float* sensor_xyz, const int64_t* voxel_idx, uint64_t num_voxels,
                                      int32_t* bins, void* stream);
+/* Diagnostic: the path length dist = 2|l - p| - time_offset (+ bounce terms)
+ * of each confocal (voxel, scan point) pair in the gathers' FP32 expression
+ * (transient_reconstruction.cuh:127-130), paths[i*L + l], and in consts[0..1]
+ * (device) rcp.approx(time_step) and half the voxel diagonal: with these a CPU
+ * replays the voxel-scattering walk's bins (transient_reconstruction.cuh:112-126)
+ * exactly.  Used by the parity tests. */
+fbp_status fbp_debug_confocal_paths(fbp_context* ctx, const fbp_recon_info* info, const float* laser_xyz,
+                                    const int64_t* voxel_idx, uint64_t num_voxels, float* paths, float* consts,
+                                    void* stream);
 
 /* ---- sampled (MIS) backprojection ----------------------------------------- */
 
@@ -195,7 +204,11 @@ typedef enum {
     FBP_MIS_SPATIAL = 1,   /* unbiased, p(l) proportional to scan point l's total intensity */
     FBP_MIS_LEARNED = 2,   /* unbiased, whole scan clusters drawn per tile (systematic sampling) from a
                               per-tile cluster distribution (fbp_mlp_forward), uniform when none is given */
-    FBP_MIS_REFERENCE = 3  /* the reference kernel's one-sample balance-heuristic MIS */
+    FBP_MIS_REFERENCE = 3, /* the reference kernel's one-sample balance-heuristic MIS */
+    FBP_MIS_REFERENCE_SCATTER = 4 /* FBP_MIS_REFERENCE as the reference's ACCUMULATE_VOXEL_SCATTERING build
+                                     computes it (transient_reconstruction.cuh:235-250): each sample adds every
+                                     bin of dist -/+ half the voxel diagonal, stepped by time_step + 1e-5, until a
+                                     bin leaves [0, T); time_step must exceed 1e-4 m */
 } fbp_mis_proposal;
 
 typedef struct {
@@ -416,12 +429,22 @@ fbp_status fbp_filter_h(fbp_context* ctx, float* data, uint64_t num_series, uint
  * the per-depth grid the surrounding comments describe. */
 typedef enum { FBP_LCT_GRID_REFERENCE = 0, FBP_LCT_GRID_DEPTH = 1 } fbp_lct_grid;
 
+/* What the LCT keeps of the complex volume after the inverse resampling.
+ *   FBP_LCT_OUTPUT_CLAMPED_REAL  max(real(vol), 0)   (python/lct.py:154)
+ *   FBP_LCT_OUTPUT_MAGNITUDE     abs(vol)            (python/lct_2.py:154)
+ * python/lct_2.py is lct.py with this output, FBP_LCT_GRID_DEPTH's radiometry
+ * (lct_2.py:103) and the PSF normalised by its column at (U, U) instead of
+ * (U-1, U-1) (lct_2.py:202 against lct.py:333); that last difference cancels,
+ * since the PSF is then normalised by its L2 norm. */
+typedef enum { FBP_LCT_OUTPUT_CLAMPED_REAL = 0, FBP_LCT_OUTPUT_MAGNITUDE = 1 } fbp_lct_output;
+
 typedef struct {
     float width;      /* half-width of the scanned wall area in metres (lct.py `width`) */
     float bin_length; /* metres of path per bin (c * bin resolution) */
     float snr;        /* Wiener filter SNR (lct.py: 0.8) */
     int diffuse;      /* 1: grid_z^4 radiometry (diffuse), 0: grid_z^2 */
     int grid_mode;    /* fbp_lct_grid */
+    int output;       /* fbp_lct_output */
 } fbp_lct_params;
 
 /* Confocal LCT reconstruction (python/lct.py:97-211 without the file loading,

@@ -181,3 +181,15 @@ def confocal_voxel_scatter(info, cube_time_major, laser_xyz):
         return confocal_voxel(info, cube_time_major, laser_xyz)
     finally:
         _chk(lib.refk_select(0))
+
+
+def confocal_voxel_mis_scatter(info, cube_time_major, laser_xyz, spatial_sum, noise, alias, prob, num_samples):
+    """backprojectConfocalVoxelMIS of the ACCUMULATE_VOXEL_SCATTERING build
+    (transient_reconstruction.cuh:235-250; atomic adds per bin)."""
+    lib = load()
+    _chk(lib.refk_load_variant(str(CUBIN_SCATTER).encode()))
+    _chk(lib.refk_select(1))
+    try:
+        return confocal_voxel_mis(info, cube_time_major, laser_xyz, spatial_sum, noise, alias, prob, num_samples)
+    finally:
+        _chk(lib.refk_select(0))

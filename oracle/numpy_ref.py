@@ -69,14 +69,17 @@ def filter_h(data: np.ndarray, delta_t: float, wl_mean: float | None = None, wl_
     return out[:, pad:pad + T].real.reshape(data.shape)
 
 
-def define_psf(U: int, V: int, slope: float) -> np.ndarray:
+def define_psf(U: int, V: int, slope: float, center: int | None = None) -> np.ndarray:
+    """python/lct.py:295-347; center: the column whose sum normalises the PSF
+    before its L2 normalisation, U - 1 in lct.py (default), U in lct_2.py:202."""
     x = np.linspace(-1, 1, 2 * U)
     y = np.linspace(-1, 1, 2 * U)
     z = np.linspace(0, 2, 2 * V)
     gz, gy, gx = np.meshgrid(z, y, x, indexing="ij")
     psf = np.abs(((4.0 * slope) ** 2) * (gx ** 2 + gy ** 2) - gz)
     psf = (psf == np.min(psf, axis=0, keepdims=True)).astype(np.float64)
-    psf = psf / np.sum(psf[:, U - 1, U - 1])
+    c = U - 1 if center is None else center
+    psf = psf / np.sum(psf[:, c, c])
     psf = psf / np.linalg.norm(psf.ravel())
     return np.roll(psf, shift=(0, U, U), axis=(0, 1, 2))
 
@@ -111,10 +114,14 @@ def radiometric_grid(M: int, N: int, mode: str = "reference") -> np.ndarray:
 
 
 def lct(data_tmajor: np.ndarray, width: float, bin_length: float, snr: float = 0.8, diffuse: bool = True,
-        psf: np.ndarray | None = None, mtx=None, mtxi=None, grid: str = "reference") -> np.ndarray:
+        psf: np.ndarray | None = None, mtx=None, mtxi=None, grid: str = "reference",
+        output: str = "clamped_real") -> np.ndarray:
     """Confocal LCT of data[M][N][N] (time-major; python/lct.py:129 order).
 
     bin_length: path length per bin in metres (c * bin_resolution).
+    output: "clamped_real" max(real(vol), 0) (python/lct.py:154) or
+    "magnitude" abs(vol) (python/lct_2.py:154; lct_2.py also uses the per-depth
+    grid, grid="depth", lct_2.py:103).
     Returns vol[M][N][N] float64 (depth, y, x)."""
     M, N, N2 = data_tmajor.shape
     assert N == N2
@@ -131,6 +138,8 @@ def lct(data_tmajor: np.ndarray, width: float, bin_length: float, snr: float = 0
     tdata[:M, :N, :N] = (mtx @ data.reshape(M, N * N)).reshape(M, N, N)
     tvol = np.fft.ifftn(np.fft.fftn(tdata) * invpsf)[:M, :N, :N]
     vol = (mtxi @ tvol.reshape(M, N * N)).reshape(M, N, N)
+    if output == "magnitude":
+        return np.abs(vol)
     return np.maximum(np.real(vol), 0)
 
 
@@ -260,8 +269,51 @@ def _mis_scatter_walk(cube, l, w, dist, vs, dt, T) -> np.ndarray:
     return acc
 
 
+def scatter_walk_f32(cube, l, dist, rcp_dt: float, ext: float, dt: float, T: int) -> np.ndarray:
+    """The voxel-scattering walk (transient_reconstruction.cuh:112-126, 235-250)
+    replayed in float32 from given FP32 paths `dist` (the GPU's, from
+    fbp_debug_confocal_paths) and the GPU's rcp.approx(timeStep) and half
+    voxel diagonal: d = max(0, dist - ext), d += timeStep + EPS while
+    d < dist + ext, bin = int(d * rcp_dt), stop at the first bin outside
+    [0, T).  Every step is an IEEE float32 operation, so the bins are the
+    GPU's bit for bit.  Returns the sum of I (> 1e-5) over each walk, FP64
+    (the caller applies the weight)."""
+    f = np.float32
+    dist = np.asarray(dist, dtype=np.float32)
+    step = f(f(dt) + f(1e-5))
+    d = np.maximum(f(0), (dist - f(ext)).astype(np.float32))
+    dmax = (dist + f(ext)).astype(np.float32)
+    acc = np.zeros(dist.shape, dtype=np.float64)
+    alive = d < dmax
+    while alive.any():
+        b = np.trunc((d * f(rcp_dt)).astype(np.float32)).astype(np.int64)
+        alive &= (b >= 0) & (b < T)  # the reference's thread returns at the first bin outside [0, T)
+        I = np.where(alive, cube[l, np.clip(b, 0, T - 1)], 0.0)
+        acc += np.where(alive & (I > 1e-5), I, 0.0)
+        d = np.where(alive, (d + step).astype(np.float32), d)
+        alive &= d < dmax
+    return acc
+
+
+def safe_rcp_sq(dist) -> np.ndarray:
+    """safeRCP(dist^2) (math.cuh:23-29) in FP64."""
+    dd = np.asarray(dist, dtype=np.float64) ** 2
+    return np.where(dd > 1e-5, 1.0 / np.where(dd > 1e-5, dd, 1.0), float(np.finfo(np.float32).max))
+
+
+def confocal_scatter_given_paths(cube, paths, rcp_dt: float, ext: float, dt: float) -> np.ndarray:
+    """backprojectConfocalVoxel of the ACCUMULATE_VOXEL_SCATTERING build for
+    the voxels whose GPU paths [n][L] are given: sum over scan points of
+    I(bin) * safeRCP(dist^2) over each walk, FP64 sums of the FP32 walk."""
+    cube = np.asarray(cube, dtype=np.float32)
+    L, T = cube.shape
+    paths = np.asarray(paths, dtype=np.float32).reshape(-1, L)
+    l = np.broadcast_to(np.arange(L), paths.shape)
+    return (scatter_walk_f32(cube, l, paths, rcp_dt, ext, dt, T) * safe_rcp_sq(paths)).sum(axis=1)
+
+
 def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=None,
-                  scatter: bool = False) -> np.ndarray:
+                  scatter: bool = False, paths=None, consts=None) -> np.ndarray:
     """Sum over samples s < `samples` of backprojectConfocalVoxelMIS
     (FasterBackprojection/transient_reconstruction.cuh:194-260, without the
     race of its `+=`): voxel v, sample s starts its generator at state v + s
@@ -273,7 +325,10 @@ def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=
     else FP64 bins.  scatter: the ACCUMULATE_VOXEL_SCATTERING build
     (transient_reconstruction.cuh:235-250): each sample adds every bin of the
     path d = max(0, dist - ext) .. dist + ext (exclusive, steps of
-    timeStep + EPS, ext = |voxelSize| / 2) until a bin leaves [0, T).
+    timeStep + EPS, ext = |voxelSize| / 2) until a bin leaves [0, T); in FP64
+    by default, or, with the GPU's FP32 paths [V][L] and consts
+    (rcp_dt, ext) from fbp_debug_confocal_paths, replayed in float32 with the
+    GPU's bins (scatter_walk_f32).
     cube: [L][T].  Returns vol[Vz][Vy][Vx] float64."""
     if scatter and bins is not None:
         raise ValueError("mis_reference: given bins and the scattering walk exclude each other")
@@ -320,6 +375,11 @@ def mis_reference(info, cube, laser_xyz, cdf, alias, prob, noise, samples, bins=
                         (inv_l + spatial_pdf[l]).astype(np.float32)).astype(np.float32)
         w = pdf.astype(np.float64) / gpdf.astype(np.float64)
         dist = 2.0 * np.linalg.norm(p - lx[l], axis=1) - float(info.time_offset)
+        if scatter and paths is not None:
+            d32 = np.asarray(paths, dtype=np.float32).reshape(V, L)[v, l]
+            out += w * safe_rcp_sq(d32) * scatter_walk_f32(cube, l, d32, consts[0], consts[1],
+                                                           float(info.time_step), T)
+            continue
         if scatter:
             out += _mis_scatter_walk(cube, l, w, dist, vs, float(info.time_step), T)
             continue

@@ -74,6 +74,30 @@ def test_confocal_batched_weights_match_reference_weights(ctx, cuda, discard, t0
     assert float(((got - want).abs()[nz] / want.abs()[nz]).max()) < 2e-6
 
 
+@pytest.mark.parametrize("discard,t0,vres", [(1, 0.0, (28, 24, 32)), (0, 0.0, (20, 18, 44)), (1, 0.3, (24, 40, 16))])
+def test_confocal_scatter_vs_fp64_oracle(ctx, cuda, discard, t0, vres):
+    """The voxel-scattering gather (ACCUMULATE_VOXEL_SCATTERING,
+    transient_reconstruction.cuh:112-126) against the FP64 oracle: the oracle's
+    float32 replay of every walk from the GPU's FP32 paths (the GPU's bins,
+    FP64 sums) within 1e-6; the independent FP64 walk (oracle/fbp_oracle.c)
+    within 1e-2, where walk ends within an FP32 rounding of a bin edge differ."""
+    import torch
+    from oracle import numpy_ref
+
+    cap, info = _confocal_case(vres=vres, seed=37, discard=discard, t0=t0)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    got = ctx.backproject_confocal_scatter(info, cube, lx).cpu().numpy().ravel()
+    V = vres[0] * vres[1] * vres[2]
+    paths, (rcp_dt, ext) = ctx.debug_confocal_paths(info, lx, torch.arange(V, device=cuda))
+    ctx.check_device_status()
+    want = numpy_ref.confocal_scatter_given_paths(cap.cube, paths.cpu().numpy(), rcp_dt, ext, info.time_step)
+    assert float(np.abs(want).max()) > 0
+    assert rel_l2(got, want) < 1e-6
+    want64 = cpu.confocal_scatter_voxel(info, cap.cube, cap.laser_xyz).ravel()
+    assert rel_l2(got, want64) < 1e-2
+
+
 @pytest.mark.parametrize("dtype", ["bf16", "f16"])
 def test_confocal_16bit_storage_vs_oracle(ctx, cuda, dtype):
     import torch

@@ -102,14 +102,15 @@ def test_display_crop_axes_and_views():
 def test_reconstruct_hands_the_prepared_capture_to_the_lct():
     import torch
 
-    from fasterbackprojection_gb300 import FBP_LAYOUT_TIME_MAJOR, cnlos
+    from fasterbackprojection_gb300 import (FBP_LAYOUT_TIME_MAJOR, FBP_LCT_GRID_DEPTH, FBP_LCT_OUTPUT_CLAMPED_REAL,
+                                            FBP_LCT_OUTPUT_MAGNITUDE, cnlos)
 
     class RecordingContext:
         device = 0
 
-        def lct(self, data, width, bin_length, snr, diffuse, grid_mode, layout, stream):
+        def lct(self, data, width, bin_length, snr, diffuse, grid_mode, layout, stream, output):
             self.args = dict(data=data.clone(), width=width, bin_length=bin_length, snr=snr, diffuse=diffuse,
-                             grid_mode=grid_mode, layout=layout)
+                             grid_mode=grid_mode, layout=layout, output=output)
             return torch.arange(data.numel(), dtype=torch.float32).reshape(data.shape)
 
     rect = np.random.default_rng(2).poisson(1.0, (8, 8, 64)).astype(np.float64)
@@ -123,3 +124,9 @@ def test_reconstruct_hands_the_prepared_capture_to_the_lct():
     assert a["width"] == 0.4 and a["bin_length"] == pytest.approx(3e8 * 8e-12)
     full = torch.arange(p.data.size, dtype=torch.float32).reshape(p.data.shape).numpy()
     np.testing.assert_array_equal(vol.numpy(), cnlos.display_crop(full, p, 0.4))
+    assert a["output"] == FBP_LCT_OUTPUT_CLAMPED_REAL
+    # python/lct_2.py's variant: per-depth radiometry, magnitude output.
+    cnlos.reconstruct(ctx, rect, 0.4, s, device="cpu", variant="lct_2")
+    assert ctx.args["output"] == FBP_LCT_OUTPUT_MAGNITUDE and ctx.args["grid_mode"] == FBP_LCT_GRID_DEPTH
+    with pytest.raises(ValueError):
+        cnlos.reconstruct(ctx, rect, 0.4, s, device="cpu", variant="lct3")

@@ -51,6 +51,28 @@ def test_lct_64x64x512_vs_fp64(ctx, cuda, grid):
     assert rel_l2(got, want) < 1e-4
 
 
+@pytest.mark.parametrize("n,m", [(64, 512), (128, 32), (4, 8)])
+def test_lct2_variant_vs_fp64(ctx, cuda, n, m):
+    """python/lct_2.py's variant: per-depth radiometry and abs(vol) instead of
+    max(real(vol), 0), through the three-pass (N <= 64), row/column (N > 64)
+    and line-pipeline (N < 8) paths, against the FP64 restatement with the
+    same two changes."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_LCT_GRID_DEPTH, FBP_LCT_OUTPUT_MAGNITUDE, scenes
+
+    cap = scenes.confocal_points(n, m, 32e-12 * (512 // m if m < 512 else 1), n_points=60, seed=n + m)
+    data = cap.cube.reshape(n, n, m).transpose(2, 0, 1).copy()
+    d = torch.from_numpy(data).to(cuda)
+    got = ctx.lct(d, 1.0, cap.time_step, 0.8, True, grid_mode=FBP_LCT_GRID_DEPTH,
+                  output=FBP_LCT_OUTPUT_MAGNITUDE).cpu().numpy()
+    want = numpy_ref.lct(data.astype(np.float64), 1.0, cap.time_step, 0.8, True, grid="depth", output="magnitude")
+    assert float(np.abs(want).max()) > 0
+    assert rel_l2(got, want) < 1e-4
+    # The magnitude bounds the clamped real part voxel by voxel.
+    clamped = ctx.lct(d, 1.0, cap.time_step, 0.8, True, grid_mode=FBP_LCT_GRID_DEPTH).cpu().numpy()
+    assert (got >= clamped - 1e-6 * float(np.abs(got).max())).all()
+
+
 @pytest.mark.parametrize("n,m", [(4, 8), (128, 32), (256, 16), (8, 2048), (16, 1024), (64, 16)])
 def test_lct_sizes_vs_fp64(ctx, cuda, n, m):
     """Scan grids and bin counts across the LCT paths (plane pass for

@@ -77,6 +77,91 @@ def test_reference_mis_many_samples_match_oracle(ctx, cuda, samples):
     assert rel_l2(got, want) < 1e-6
 
 
+def _scatter_case(seed=11):
+    # 2.4 m deep volume in 28 slices: a voxel diagonal of ~12 cm, walks of
+    # 10-13 bins of 9.6 mm.
+    return _case(seed=seed)
+
+
+def test_reference_mis_scatter_matches_reference_build_one_sample(ctx, cuda):
+    """The voxel-scattering build of the reference's MIS kernel: with one
+    sample per voxel each voxel's atomic adds come from one thread in bin
+    order, so its volume is deterministic and must match bit for bit."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE_SCATTER
+    from oracle import harness
+
+    if not harness.scatter_available():
+        pytest.skip("reference scatter build not present")
+    harness.load()
+    cap, info = _scatter_case()
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    cdf, alias, prob = ctx.mis_reference_tables(info, cube)
+    V = 24 * 20 * 28
+    noise = torch.rand(V, generator=torch.Generator().manual_seed(7)).to(cuda)
+    got = ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE_SCATTER, 1, noise=noise)
+    ref = harness.confocal_voxel_mis_scatter(info, cube.t().contiguous(), lx, torch.from_numpy(cdf).to(cuda), noise,
+                                             torch.from_numpy(alias.astype(np.int32)).to(cuda),
+                                             torch.from_numpy(prob).to(cuda), 1)
+    ctx.check_device_status()
+    assert float(ref.abs().max()) > 0
+    assert torch.equal(got, ref)
+
+
+@pytest.mark.parametrize("samples", [16, 64])
+def test_reference_mis_scatter_many_samples_match_reference_build(ctx, cuda, samples):
+    """Many samples: the reference adds with atomics (any order), so the
+    volumes agree to 1e-5 relative L2."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE_SCATTER
+    from oracle import harness
+
+    if not harness.scatter_available():
+        pytest.skip("reference scatter build not present")
+    harness.load()
+    cap, info = _scatter_case(seed=12)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    cdf, alias, prob = ctx.mis_reference_tables(info, cube)
+    V = 24 * 20 * 28
+    noise = torch.rand(V + 5, generator=torch.Generator().manual_seed(8)).to(cuda)
+    got = ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE_SCATTER, samples, noise=noise)
+    ref = harness.confocal_voxel_mis_scatter(info, cube.t().contiguous(), lx, torch.from_numpy(cdf).to(cuda), noise,
+                                             torch.from_numpy(alias.astype(np.int32)).to(cuda),
+                                             torch.from_numpy(prob).to(cuda), samples)
+    ctx.check_device_status()
+    assert rel_l2(got.cpu().numpy(), ref.cpu().numpy()) < 1e-5
+
+
+@pytest.mark.parametrize("samples", [1, 37, 300])
+def test_reference_mis_scatter_match_oracle(ctx, cuda, samples):
+    """Against numpy_ref.mis_reference(scatter=True): its float32 replay of
+    the walk from the GPU's FP32 paths (the same bins, FP64 sums) within 1e-6,
+    and its independent FP64 walk within 1e-2 (walks whose ends land within an
+    FP32 rounding of a bin edge differ by a bin)."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE_SCATTER
+    from oracle import numpy_ref
+
+    cap, info = _scatter_case(seed=13)
+    cube = torch.from_numpy(cap.cube).to(cuda)
+    lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+    cdf, alias, prob = ctx.mis_reference_tables(info, cube)
+    V = 24 * 20 * 28
+    noise = torch.rand(V + 3, generator=torch.Generator().manual_seed(9)).to(cuda)
+    got = ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE_SCATTER, samples, noise=noise).cpu().numpy()
+    paths, consts = ctx.debug_confocal_paths(info, lx, torch.arange(V, device=cuda))
+    ctx.check_device_status()
+    nz = noise.cpu().numpy()
+    want = numpy_ref.mis_reference(info, cap.cube, cap.laser_xyz, cdf, alias, prob, nz, samples, scatter=True,
+                                   paths=paths.cpu().numpy(), consts=consts)
+    assert float(np.abs(want).max()) > 0
+    assert rel_l2(got, want) < 1e-6
+    want64 = numpy_ref.mis_reference(info, cap.cube, cap.laser_xyz, cdf, alias, prob, nz, samples, scatter=True)
+    assert rel_l2(got, want64) < 1e-2
+
+
 @pytest.mark.parametrize("proposal", ["uniform", "spatial", "clusters", "clusters_cv"])
 def test_unbiased_estimators_converge_to_full_backprojection(ctx, cuda, proposal):
     import torch

@@ -59,6 +59,16 @@ def test_lct_grid_modes_differ_only_in_radiometry(golden):
     assert a.shape == b.shape and not np.allclose(a, b)
 
 
+@pytest.mark.parametrize("U,V,slope", [(4, 8, 0.3), (8, 16, 0.1), (16, 32, 0.05)])
+def test_lct2_psf_centre_cancels_under_l2_normalisation(U, V, slope):
+    """python/lct_2.py normalises the PSF by its column at (U, U) where lct.py
+    uses (U - 1, U - 1); the L2 normalisation that follows removes any scalar,
+    so both give the same PSF (which is why fbp_lct needs no option for it)."""
+    a = numpy_ref.define_psf(U, V, slope)
+    b = numpy_ref.define_psf(U, V, slope, center=U)
+    np.testing.assert_allclose(a, b, rtol=1e-14, atol=1e-16)
+
+
 def test_resampling_operator_rejects_non_power_of_two():
     with pytest.raises(ValueError):
         numpy_ref.resampling_operator(48)
@@ -245,6 +255,42 @@ def test_scatter_oracle_known_answer_and_walk_end():
     o.num_time_bins = 10
     assert cpu.confocal_scatter_voxel(o, np.ascontiguousarray(cube[:, :10]), lx)[0, 0, 0] == pytest.approx(2.0,
                                                                                                           rel=1e-6)
+
+
+def test_scatter_float32_replay_agrees_with_fp64_walk():
+    """numpy_ref.confocal_scatter_given_paths (the float32 replay of the walk
+    from given FP32 paths, used with the GPU's paths in the GPU tests) against
+    the FP64 oracle walk, with paths and constants rounded to float32 here:
+    the known answer exactly, and a random case within the bin-edge flips."""
+    o = _info(1, 32, 0.1, (1, 1, 1), (-0.05, -0.55, -0.05), (0.1, 0.1, 0.1))
+    cube = np.zeros((1, 32), np.float32)
+    cube[0, 9], cube[0, 10], cube[0, 11] = 2.0, 3.0, 7.0
+    ext = float(np.float32(0.5 * math.sqrt(0.03)))
+    got = numpy_ref.confocal_scatter_given_paths(cube, np.array([[1.0]], np.float32), float(np.float32(10.0)), ext, 0.1)
+    assert got[0] == pytest.approx(5.0, rel=1e-6)
+    # The walk stops at the first bin outside [0, T).
+    got = numpy_ref.confocal_scatter_given_paths(np.ascontiguousarray(cube[:, :10]), np.array([[1.0]], np.float32),
+                                                 float(np.float32(10.0)), ext, 0.1)
+    assert got[0] == pytest.approx(2.0, rel=1e-6)
+
+    rng = np.random.default_rng(19)
+    L, T = 9, 64
+    lxyz = np.stack([rng.uniform(-1, 1, L), np.zeros(L), rng.uniform(-1, 1, L)], 1).astype(np.float32)
+    o = _info(L, T, 0.05, (3, 4, 5), (-0.5, -1.2, -0.4), (0.3, 0.2, 0.25))
+    cube = rng.uniform(0, 2, (T, L)).astype(np.float32)
+    cube[cube < 0.3] = 0
+    want = cpu.confocal_scatter_voxel(o, np.ascontiguousarray(cube.T), lxyz).ravel()
+    Vx, Vy, Vz = o.voxel_res
+    vs = np.array(o.voxel_size[:], dtype=np.float64)
+    paths = np.empty((Vx * Vy * Vz, L), np.float32)
+    for v in range(Vx * Vy * Vz):
+        vz, vy, vx = v // (Vx * Vy), (v // Vx) % Vy, v % Vx
+        p = np.array(o.hidden_min[:]) + np.array([vx, vz, vy]) * vs + 0.5 * vs
+        paths[v] = (2.0 * np.linalg.norm(lxyz.astype(np.float64) - p, axis=1)).astype(np.float32)
+    got = numpy_ref.confocal_scatter_given_paths(np.ascontiguousarray(cube.T), paths,
+                                                 float(np.float32(1.0 / o.time_step)),
+                                                 float(np.float32(0.5 * math.sqrt(vs @ vs))), o.time_step)
+    assert rel_l2(got, want) < 2e-2
 
 
 def test_confocal_subset_matches_full():
