@@ -58,6 +58,8 @@ def parse():
                     help="multi-GPU: weak = one capture per rank; slabs = the same capture split into depth slabs "
                          "(strong scaling; each rank uploads only its slab's bin window in the e2e leg)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--only", choices=["exhaustive", "filters", "lct", "scatter_forms", "batched", "reference_kernels"],
+                    help="run one extra leg alone on the benchmark capture and print its JSON (profiling runs)")
     a = ap.parse_args()
     a.small = a.size != "full"
     return a
@@ -629,6 +631,37 @@ def scatter_forms_leg(ctx, dev, info, cube, lx):
     except Exception as ex:  # pragma: no cover
         e["reference_8_slices"] = {"unavailable": f"harness: {ex}"}
     out["voxel_scattering"] = e
+    # The reference-mode MIS kernel of the same build (transient_reconstruction.cuh:
+    # 235-250): 64 samples per voxel, each walking its voxel's bin range.
+    from fasterbackprojection_gb300 import FBP_MIS_REFERENCE_SCATTER
+
+    noise = torch.rand(V, generator=torch.Generator().manual_seed(5)).to(dev)
+    mvol = torch.empty(V, dtype=torch.float32, device=dev)
+    _, m_ms = timed_ms(lambda: ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE_SCATTER, 64, noise=noise,
+                                                   out=mvol), reps=2)
+    m = {"workload": "64 samples per voxel, 256^2 x 1024 FP32 -> 256^3, walks of about 3 bins", "ms": m_ms,
+         "samples_per_s": V * 64 / (m_ms / 1e3)}
+    try:
+        from oracle import harness
+
+        if harness.scatter_available():
+            harness.load()
+            cdf, alias, prob = ctx.mis_reference_tables(info, cube)
+            cube_tm = cube.t().contiguous()
+            args = (torch.from_numpy(cdf).to(dev), noise, torch.from_numpy(alias.astype("int32")).to(dev),
+                    torch.from_numpy(prob).to(dev))
+            r, r_ms = timed_ms(lambda: harness.confocal_voxel_mis_scatter(info, cube_tm, lx, args[0], args[1], args[2],
+                                                                          args[3], 64), reps=2)
+            del cube_tm
+            m.update({"reference_ms": r_ms, "speedup": r_ms / m_ms,
+                      "rel_l2_vs_reference": float(torch.linalg.vector_norm((mvol.view_as(r) - r).double()) /
+                                                   max(float(torch.linalg.vector_norm(r.double())), 1e-30))})
+        else:
+            m["reference"] = {"unavailable": "reference scatter build not present"}
+    except Exception as ex:  # pragma: no cover
+        m["reference"] = {"unavailable": f"harness: {ex}"}
+    out["mis_voxel_scattering"] = m
+    del mvol, noise
     svol = torch.empty(V, dtype=torch.float32, device=dev)
     _, ms = timed_ms(lambda: ctx.splat_backproject(info, cube, lx, max_bins=700, grid=(256, 256), out=svol), reps=2)
     nz = int((cube[:, :700] > 1.1920929e-7).sum())
@@ -939,10 +972,13 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
             ref_c.copy_(torch.fft.ifft(torch.fft.fft(Hs, dim=1) * Kf[None], dim=1, norm="forward")[:, pad:pad + T].real)
 
         _, rf_ms = timed_ms(cufft_filter_h)
+        once = cube.clone()  # one application (the timed loop above filters c in place repeatedly)
+        ctx.filter_h_(once, time_step)
         res["filter_h"]["reference_cufft_c2c_ms"] = rf_ms
         res["filter_h"]["speedup_vs_cufft_pipeline"] = rf_ms / fh_ms
         res["filter_h"]["rel_l2_vs_cufft_pipeline"] = float(
-            torch.linalg.vector_norm((c.reshape(Ls, T) - ref_c).double()) / torch.linalg.vector_norm(ref_c.double()))
+            torch.linalg.vector_norm((once.reshape(Ls, T) - ref_c).double()) / torch.linalg.vector_norm(ref_c.double()))
+        del once
         del Hs
     except RuntimeError as e:  # pragma: no cover
         res["filter_h"]["reference_cufft_unavailable"] = str(e)
@@ -1115,10 +1151,40 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_only(args):
+    """One extra leg alone (for profiling command lines)."""
+    import torch
+
+    from fasterbackprojection_gb300 import Context
+
+    dev = torch.device("cuda", 0)
+    cap, info = make_workload(dev, 2, args.size)
+    ctx = Context(0)
+    cube, lx = cap.cube.contiguous(), cap.laser_xyz.contiguous()
+    vx, vy, vz = info.voxel_res
+    vol = torch.empty((vz, vy, vx), device=dev)
+    ctx.backproject_confocal(info, cube, lx, out=vol)
+    pk = measured_peaks()[0]
+    legs = {
+        "exhaustive": lambda: exhaustive_leg(ctx, dev),
+        "filters": lambda: filters_leg(ctx, dev, vol, cube, info.time_step, pk),
+        "lct": lambda: lct_leg(ctx, dev, pk),
+        "scatter_forms": lambda: scatter_forms_leg(ctx, dev, info, cube, lx),
+        "batched": lambda: batched_leg(ctx, dev, max(1, args.steps)),
+        "reference_kernels": lambda: reference_kernels_leg(ctx, dev, info, cube, lx, vol),
+    }
+    res = legs[args.only]()
+    ctx.check_device_status()
+    print(json.dumps({"only": args.only, args.only: res}), flush=True)
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only:
+        run_only(args)
     else:
         run_ours(args)
 

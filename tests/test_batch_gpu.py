@@ -130,7 +130,7 @@ def test_batch_autotune_picks_a_valid_shape(ctx, cuda):
     caps = _captures(cuda)
     b = _batch(ctx, caps)
     chosen = b.autotune()
-    assert chosen in (0, 1, 2)
+    assert chosen in (0, 1, 2, 3)
     b.run()
     torch.cuda.synchronize()
     for c in caps:
