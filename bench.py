@@ -694,7 +694,10 @@ def fp64_error(ctx, info, cube, lx, vol, nvox=512, seed=5):
 
     V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
     rng = np.random.default_rng(seed)
-    idx = np.sort(rng.choice(V, size=min(nvox, V), replace=False)).astype(np.int64)
+    rnd = rng.choice(V, size=min(nvox, V), replace=False)
+    # plus the 128 largest voxels: the longest sums of the largest weights
+    top = torch.topk(vol.reshape(-1), min(128, V)).indices.cpu().numpy()
+    idx = np.unique(np.concatenate([rnd, top])).astype(np.int64)
     idx_t = torch.from_numpy(idx).to(lx.device)
     bins = ctx.debug_confocal_bins(info, lx, idx_t).cpu().numpy()
     host = cube.float().cpu().numpy()
@@ -707,8 +710,10 @@ def fp64_error(ctx, info, cube, lx, vol, nvox=512, seed=5):
         nb = float(np.linalg.norm(b))
         return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
 
+    is_top = np.isin(idx, top)
     return {"rel_l2_vs_fp64": rel(got, want64), "rel_l2_vs_fp64_same_bins": rel(got, want_same),
-            "voxels": int(idx.shape[0])}
+            "rel_l2_vs_fp64_same_bins_largest_128": rel(got[is_top], want_same[is_top]),
+            "voxels": int(idx.shape[0]), "sample": f"{nvox} random voxels and the 128 largest"}
 
 
 def batched_leg(ctx, dev, steps):
@@ -876,7 +881,9 @@ def exhaustive_leg(ctx, dev):
     del cap.cube
     vol, ms = timed_ms(lambda: ctx.backproject_exhaustive(info, cube16, cap.laser_xyz, cap.sensor_xyz), reps=3)
     triples = 128 ** 3 * L * S
-    idx = np.sort(np.random.default_rng(3).choice(128 ** 3, 128, replace=False)).astype(np.int64)
+    rnd = np.random.default_rng(3).choice(128 ** 3, 128, replace=False)
+    top = torch.topk(vol.reshape(-1), 64).indices.cpu().numpy()  # the longest sums of the largest weights
+    idx = np.unique(np.concatenate([rnd, top])).astype(np.int64)
     cube_np = cube16.float().cpu().numpy().reshape(L * S, 1024)
     lx_np, sx_np = cap.laser_xyz.cpu().numpy(), cap.sensor_xyz.cpu().numpy()
     want = cpu.exhaustive_voxel_subset(info, cube_np, lx_np, sx_np, idx)
@@ -902,8 +909,10 @@ def exhaustive_leg(ctx, dev):
         "workload": "exhaustive 16^2 x 32^2 x 1024 (16 ps) FP16 -> 128^3, 500 points",
         "ms": ms, "value": triples / (ms / 1e3), "unit": "voxel-samples/s (voxel, laser, SPAD)",
         "achieved_gbs_2B_per_sample": triples * 2 / (ms / 1e3) / 1e9,
-        "rel_l2_vs_fp64": rel(got, want), "error_voxels": 128,
+        "rel_l2_vs_fp64": rel(got, want), "error_voxels": int(len(idx)),
+        "error_sample": "128 random voxels and the 64 largest",
         "rel_l2_vs_fp64_same_bins": rel(got, want_same),
+        "rel_l2_vs_fp64_same_bins_largest_64": rel(got[np.isin(idx, top)], want_same[np.isin(idx, top)]),
         "bin_flips": {"triples": int(flipped.size), "flipped": int(flipped.sum()),
                       "flipped_on_nonzero_samples": int((flipped & nz).sum()),
                       "rel_l2_fp64_gpu_bins_vs_fp64_bins": rel(want_same, want),

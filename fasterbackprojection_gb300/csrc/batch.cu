@@ -111,7 +111,7 @@ fbp_status rows_any(fbp_context* ctx, int dtype, const fbp_capture_desc& c, uint
 fbp_status plan_config(fbp_batch* b, int cfg, cudaStream_t s) {
     const TileCfg tc = kTileCfgs[cfg];
     const int align = (int)(16 / kRowBytes);
-    const size_t meta = ConfocalGatherParams::meta_bytes(32);
+    const size_t meta = ConfocalGatherParams::meta_bytes(32) + kahan_smem_bytes(tc.kv, 32 * tc.wy * tc.wz) + 16;
     const uint32_t n = (uint32_t)b->caps.size();
     b->params.assign(n, ConfocalGatherParams{});
     b->groups.clear();

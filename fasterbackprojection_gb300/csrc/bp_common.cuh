@@ -89,6 +89,13 @@ struct ConfocalGatherParams {
     }
 };
 
+// Shared memory holding the compensated (Kahan) sums of a CTA's voxels when a
+// thread owns 16 of them (sum and compensation per voxel, [2 KV][threads]):
+// kept there instead of in 64 registers, so three CTAs fit per SM.
+__host__ __device__ constexpr size_t kahan_smem_bytes(int kv, int threads) {
+    return kv >= 16 ? (size_t)2 * kv * threads * sizeof(float) : 0;
+}
+
 // Window geometry shared by the gathers: the widest bin span a tile of the
 // given world extents can need, capped at the whole row (T bins plus one
 // alignment step), the padded row pitch, and the stage size that fits the

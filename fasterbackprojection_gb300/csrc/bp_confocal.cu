@@ -207,8 +207,9 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
                                    (double)in.voxel_size[2] * in.voxel_size[2]);
     const double extra = scatter ? 1.02 * vdiag + 2.0 * std::fabs((double)in.time_step) : 0.0;
     FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(float),
-                        ConfocalGatherParams::meta_bytes(32) + (smp ? kSampledStaticSmem : 0), &wp,
-                        "fbp_backproject_confocal", extra));
+                        ConfocalGatherParams::meta_bytes(32) + (smp ? kSampledStaticSmem : 0) +
+                            kahan_smem_bytes((int)kv, 32 * kWY * kWZ) + 16,
+                        &wp, "fbp_backproject_confocal", extra));
     if (smp) wp.smem -= kSampledStaticSmem;
 
     float* rows = nullptr;

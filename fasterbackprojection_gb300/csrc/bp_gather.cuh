@@ -569,9 +569,22 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
         cp_async_commit();
     };
 
-    float acc[KV], ksum[KV], kcomp[KV];
+    // Compensated sums: in registers, or (16 voxels per thread) in shared
+    // memory behind the zero slot, [2 KV][NT] so a warp's accesses are
+    // consecutive words.
+    constexpr bool KSMEM = kahan_smem_bytes(KV, NT) > 0;
+    float* s_kahan = reinterpret_cast<float*>(
+        smem_raw + ((slots_off + (size_t)(zero_slot + slot_stride) * sizeof(S) + 15) & ~size_t(15)));
+    float acc[KV], ksum[KSMEM ? 1 : KV], kcomp[KSMEM ? 1 : KV];
 #pragma unroll
-    for (int k = 0; k < KV; ++k) acc[k] = ksum[k] = kcomp[k] = 0.f;
+    for (int k = 0; k < KV; ++k) acc[k] = 0.f;
+    if constexpr (KSMEM) {
+#pragma unroll
+        for (int k = 0; k < 2 * KV; ++k) s_kahan[k * NT + tid] = 0.f;
+    } else {
+#pragma unroll
+        for (int k = 0; k < KV; ++k) ksum[k] = kcomp[k] = 0.f;
+    }
 
     if (nchunks > 0) {
         plan_chunk(0, 0);
@@ -611,10 +624,18 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
         // Compensated (Kahan) fold of this stage's partial sums.
 #pragma unroll
         for (int k = 0; k < KV; ++k) {
-            const float y = sub_rn(mul_rn(acc[k], scale), kcomp[k]);
-            const float t = add_rn(ksum[k], y);
-            kcomp[k] = sub_rn(sub_rn(t, ksum[k]), y);
-            ksum[k] = t;
+            const float sk = KSMEM ? s_kahan[(2 * k) * NT + tid] : ksum[k];
+            const float ck = KSMEM ? s_kahan[(2 * k + 1) * NT + tid] : kcomp[k];
+            const float y = sub_rn(mul_rn(acc[k], scale), ck);
+            const float t = add_rn(sk, y);
+            const float c = sub_rn(sub_rn(t, sk), y);
+            if constexpr (KSMEM) {
+                s_kahan[(2 * k) * NT + tid] = t;
+                s_kahan[(2 * k + 1) * NT + tid] = c;
+            } else {
+                kcomp[k] = c;
+                ksum[k] = t;
+            }
             acc[k] = 0.f;
         }
     }
@@ -623,7 +644,7 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
         float* out = p.volume + ((size_t)vz * p.Vy + vy) * p.Vx + tx0;
 #pragma unroll
         for (int k = 0; k < KV; ++k)
-            if (tx0 + k < p.Vx) out[k] = ksum[k];
+            if (tx0 + k < p.Vx) out[k] = KSMEM ? s_kahan[(2 * k) * NT + tid] : ksum[k];
     }
 }
 

@@ -11,6 +11,7 @@
 #include "fbp_internal.cuh"
 
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 namespace fbp {
@@ -241,6 +242,83 @@ __global__ void __launch_bounds__(128) log_filter_zblock_kernel(const float* __r
     }
 }
 
+// log_filter_zblock_kernel with each thread owning two columns, x and x + 16,
+// as the halves of packed FP32 pairs: the tile holds (v[x], v[x + 16]) pairs,
+// the taps (w, w), and one fma.rn.f32x2 applies a tap to both outputs with
+// the scalar rounding on each half.  Each output still takes its terms in the
+// reference's order, so the result is bitwise that of log_filter_kernel; a
+// tap now costs half an issue slot per output.  Tile 32 x 8 x 16 outputs,
+// 128 threads, 38 KB of shared memory.
+template <int H>
+struct LogTaps2 {
+    unsigned long long w2[(2 * H + 1) * (2 * H + 1) * (2 * H + 1)];
+};
+
+template <int H>
+__global__ void __launch_bounds__(128) log_filter_zpair_kernel(const float* __restrict__ in, float* __restrict__ out,
+                                                               uint32_t nx, uint32_t ny, uint32_t nz,
+                                                               const __grid_constant__ LogTaps2<H> taps) {
+    constexpr int K = 2 * H + 1, TX = 32, HX = 16, TY = 8, TZ = 16;
+    constexpr int EX = HX + 2 * H, EY = TY + 2 * H, EZ = TZ + 2 * H;
+    __shared__ f32x2_t tile[EZ][EY][EX];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    const int tid = threadIdx.x + HX * threadIdx.y;
+    constexpr int NT = HX * TY, NE = EX * EY * EZ, B = 8;
+    for (int i0 = tid; i0 < NE; i0 += B * NT) {
+        float va[B], vb[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int i = i0 + u * NT;
+            if (i < NE) {
+                const int lx = i % EX, ly = (i / EX) % EY, lz = i / (EX * EY);
+                const int ga = min(max(x0 + lx - H, 0), (int)nx - 1);
+                const int gb = min(max(x0 + lx + HX - H, 0), (int)nx - 1);
+                const int gy = min(max(y0 + ly - H, 0), (int)ny - 1);
+                const int gz = min(max(z0 + lz - H, 0), (int)nz - 1);
+                const size_t row = ((size_t)gz * ny + gy) * nx;
+                va[u] = in[row + ga];
+                vb[u] = in[row + gb];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (i0 + u * NT < NE) (&tile[0][0][0])[i0 + u * NT] = pack2(va[u], vb[u]);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int xa = x0 + tx, xb = xa + HX, y = y0 + ty;
+    const bool ok_a = xa < (int)nx && y < (int)ny, ok_b = xb < (int)nx && y < (int)ny;
+    f32x2_t acc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] = 0ull;
+#pragma unroll 1
+    for (int pl = 0; pl < EZ; ++pl) {
+#pragma unroll
+        for (int ky = 0; ky < K; ++ky) {
+            f32x2_t r[K];
+#pragma unroll
+            for (int kx = 0; kx < K; ++kx) r[kx] = tile[pl][ty + ky][tx + kx];
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int kz = 2 * H - k;
+#pragma unroll
+                for (int kx = 0; kx < K; ++kx) acc[k] = fma_rn2(r[kx], taps.w2[(kz * K + ky) * K + kx], acc[k]);
+            }
+        }
+        const int zo = pl - 2 * H;  // acc[0] is complete
+        if (zo >= 0 && z0 + zo < (int)nz) {
+            float a, b;
+            unpack2(acc[0], a, b);
+            const size_t row = ((size_t)(z0 + zo) * ny + y) * nx;
+            if (ok_a) out[row + xa] = a;
+            if (ok_b) out[row + xb] = b;
+        }
+#pragma unroll
+        for (int k = 0; k < K - 1; ++k) acc[k] = acc[k + 1];
+        acc[K - 1] = 0ull;
+    }
+}
+
 // ------------------------------------------------------- Laplacian filter --
 
 // laplacianFilter (transient_postprocessing.cuh:21-50): k^3 * v - (sum of the
@@ -331,6 +409,71 @@ __global__ void __launch_bounds__(128) laplacian_zblock_kernel(const float* __re
         if (z0 + z < (int)nz) out[((size_t)(z0 + z) * ny + y) * nx + x] = fma_rn(k3, tile[z + H][ty + H][tx + H], -lap[z]);
 }
 
+// laplacian_zblock_kernel with the column's outputs z and z + 16 as the halves
+// of packed FP32 pairs: the tile holds (v[z], v[z + 16]) pairs along z, and one
+// add.rn.f32x2 adds a neighbour to both sums, each in the reference's order
+// (dx, dy, dz), so the result is bitwise that of the scalar kernel at half the
+// add instructions.
+template <int H>
+__global__ void __launch_bounds__(128) laplacian_zpair_kernel(const float* __restrict__ in, float* __restrict__ out,
+                                                              uint32_t nx, uint32_t ny, uint32_t nz, float k3) {
+    constexpr int K = 2 * H + 1, TX = 32, TY = 4, TZ = 32, HZ = 16;
+    constexpr int EX = TX + 2 * H, EY = TY + 2 * H, EZ2 = HZ + 2 * H;  // pairs (z, z + 16), z < EZ2
+    __shared__ f32x2_t tile[EZ2][EY][EX];
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
+    const int tid = threadIdx.x + TX * threadIdx.y;
+    constexpr int NT = TX * TY, NE = EX * EY * EZ2, B = 8;
+    for (int i0 = tid; i0 < NE; i0 += B * NT) {
+        float va[B], vb[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int i = i0 + u * NT;
+            va[u] = vb[u] = 0.f;  // zero outside the volume
+            if (i < NE) {
+                const int lx = i % EX, ly = (i / EX) % EY, lz = i / (EX * EY);
+                const int gx = x0 + lx - H, gy = y0 + ly - H, ga = z0 + lz - H, gb = ga + HZ;
+                if (gx >= 0 && gx < (int)nx && gy >= 0 && gy < (int)ny) {
+                    const size_t col = (size_t)gy * nx + gx, plane = (size_t)nx * ny;
+                    if (ga >= 0 && ga < (int)nz) va[u] = in[ga * plane + col];
+                    if (gb >= 0 && gb < (int)nz) vb[u] = in[gb * plane + col];
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (i0 + u * NT < NE) (&tile[0][0][0])[i0 + u * NT] = pack2(va[u], vb[u]);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = x0 + tx, y = y0 + ty;
+    if (x >= (int)nx || y >= (int)ny) return;
+    f32x2_t lap[HZ];  // (sum of output z, sum of output z + 16)
+#pragma unroll
+    for (int z = 0; z < HZ; ++z) lap[z] = 0ull;
+#pragma unroll 1
+    for (int dx = 0; dx < K; ++dx) {
+#pragma unroll 1
+        for (int dy = 0; dy < K; ++dy) {
+            f32x2_t c[EZ2];
+#pragma unroll
+            for (int z = 0; z < EZ2; ++z) c[z] = tile[z][ty + dy][tx + dx];
+#pragma unroll
+            for (int z = 0; z < HZ; ++z)
+#pragma unroll
+                for (int dz = 0; dz < K; ++dz) lap[z] = add_rn2(lap[z], c[z + dz]);
+        }
+    }
+#pragma unroll
+    for (int z = 0; z < HZ; ++z) {
+        float la, lb, ca, cb;
+        unpack2(lap[z], la, lb);
+        unpack2(tile[z + H][ty + H][tx + H], ca, cb);  // (v[z + H], v[z + 16 + H]) of this column
+        const size_t col = (size_t)y * nx + x, plane = (size_t)nx * ny;
+        if (z0 + z < (int)nz) out[(z0 + z) * plane + col] = fma_rn(k3, ca, -la);
+        if (z0 + z + HZ < (int)nz) out[(z0 + z + HZ) * plane + col] = fma_rn(k3, cb, -lb);
+    }
+}
+
 fbp_status launch_log(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz, int ksize,
                       float sigma, cudaStream_t stream);
 fbp_status launch_laplacian(fbp_context* ctx, const float* in, float* out, uint32_t nx, uint32_t ny, uint32_t nz,
@@ -380,9 +523,15 @@ static fbp_status log_h(fbp_context* ctx, const float* in, float* out, uint32_t 
     for (int i = 0; i < ksize * ksize * ksize; ++i) taps.w[i] = w[i];
     if constexpr (H >= 1 && H <= 2) {
         if (ksize == 2 * H + 1) {
-            dim3 grid(cdiv(nx, 32), cdiv(ny, 4), cdiv(nz, 32));
-            log_filter_zblock_kernel<H><<<grid, dim3(32, 4), 0, stream>>>(in, out, nx, ny, nz, taps);
-            FBP_CHECK_LAUNCH(ctx, "log_filter_zblock_kernel");
+            LogTaps2<H> taps2{};
+            for (int i = 0; i < ksize * ksize * ksize; ++i) {
+                uint32_t b;
+                std::memcpy(&b, &w[i], 4);
+                taps2.w2[i] = ((unsigned long long)b << 32) | b;  // (w, w)
+            }
+            dim3 grid(cdiv(nx, 32), cdiv(ny, 8), cdiv(nz, 16));
+            log_filter_zpair_kernel<H><<<grid, dim3(16, 8), 0, stream>>>(in, out, nx, ny, nz, taps2);
+            FBP_CHECK_LAUNCH(ctx, "log_filter_zpair_kernel");
             return FBP_OK;
         }
     }
@@ -400,8 +549,8 @@ static fbp_status lap_h(fbp_context* ctx, const float* in, float* out, uint32_t 
                         cudaStream_t stream) {
     if constexpr (H <= 2) {
         const dim3 grid(cdiv(nx, 32), cdiv(ny, 4), cdiv(nz, 32));
-        laplacian_zblock_kernel<H><<<grid, dim3(32, 4), 0, stream>>>(in, out, nx, ny, nz, k3);
-        FBP_CHECK_LAUNCH(ctx, "laplacian_zblock_kernel");
+        laplacian_zpair_kernel<H><<<grid, dim3(32, 4), 0, stream>>>(in, out, nx, ny, nz, k3);
+        FBP_CHECK_LAUNCH(ctx, "laplacian_zpair_kernel");
         return FBP_OK;
     }
     constexpr int E = 8 + 2 * H;
