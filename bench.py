@@ -58,7 +58,8 @@ def parse():
                     help="multi-GPU: weak = one capture per rank; slabs = the same capture split into depth slabs "
                          "(strong scaling; each rank uploads only its slab's bin window in the e2e leg)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
-    ap.add_argument("--only", choices=["exhaustive", "filters", "lct", "scatter_forms", "batched", "reference_kernels"],
+    ap.add_argument("--only", choices=["exhaustive", "filters", "lct", "scatter_forms", "batched", "reference_kernels",
+                                       "learned"],
                     help="run one extra leg alone on the benchmark capture and print its JSON (profiling runs)")
     a = ap.parse_args()
     a.small = a.size != "full"
@@ -1181,6 +1182,7 @@ def run_only(args):
         "scatter_forms": lambda: scatter_forms_leg(ctx, dev, info, cube, lx),
         "batched": lambda: batched_leg(ctx, dev, max(1, args.steps)),
         "reference_kernels": lambda: reference_kernels_leg(ctx, dev, info, cube, lx, vol),
+        "learned": lambda: learned_mis_leg(ctx, dev, info, cube, lx),
     }
     res = legs[args.only]()
     ctx.check_device_status()

@@ -177,78 +177,19 @@ __global__ void __launch_bounds__(512) log_filter_kernel(const float* __restrict
     out[((size_t)z * ny + y) * nx + x] = sum;
 }
 
-// The same filter for odd ksize = 2H+1 with H <= 2, register-blocked along
-// z: a thread owns one (x, y) column of TZ outputs and walks the input planes
-// once.  It keeps the K = 2H+1 outputs a plane reaches in a rotating window
-// of accumulators: output zo = pl - 2H + k sits in acc[k] and takes tap
-// kz = 2H - k of plane pl; after the plane acc[0] is complete and the window
-// shifts.  Every output still receives its terms in the reference's order
-// (plane = kz ascending, then ky, then kx), so the result is bitwise that of
-// log_filter_kernel.  Tile 32 x 4 x 32 outputs, 128 threads.
-template <int H>
-__global__ void __launch_bounds__(128) log_filter_zblock_kernel(const float* __restrict__ in, float* __restrict__ out,
-                                                                uint32_t nx, uint32_t ny, uint32_t nz,
-                                                                const __grid_constant__ LogTaps<H> taps) {
-    constexpr int K = 2 * H + 1, TX = 32, TY = 4, TZ = 32;
-    constexpr int EX = TX + 2 * H, EY = TY + 2 * H, EZ = TZ + 2 * H;
-    __shared__ float tile[EZ][EY][EX];
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-    const int tid = threadIdx.x + TX * threadIdx.y;
-    // Fill in batches: a thread's loads of a batch are in flight together.
-    constexpr int NT = TX * TY, NE = EX * EY * EZ, B = 8;
-    for (int i0 = tid; i0 < NE; i0 += B * NT) {
-        float v[B];
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int i = i0 + u * NT;
-            if (i < NE) {
-                const int lx = i % EX, ly = (i / EX) % EY, lz = i / (EX * EY);
-                const int gx = min(max(x0 + lx - H, 0), (int)nx - 1);
-                const int gy = min(max(y0 + ly - H, 0), (int)ny - 1);
-                const int gz = min(max(z0 + lz - H, 0), (int)nz - 1);
-                v[u] = in[((size_t)gz * ny + gy) * nx + gx];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < B; ++u)
-            if (i0 + u * NT < NE) (&tile[0][0][0])[i0 + u * NT] = v[u];
-    }
-    __syncthreads();
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int x = x0 + tx, y = y0 + ty;
-    const bool col_ok = x < (int)nx && y < (int)ny;
-    float acc[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) acc[k] = 0.f;
-#pragma unroll 1
-    for (int pl = 0; pl < EZ; ++pl) {
-#pragma unroll
-        for (int ky = 0; ky < K; ++ky) {
-            float r[K];
-#pragma unroll
-            for (int kx = 0; kx < K; ++kx) r[kx] = tile[pl][ty + ky][tx + kx];
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const int kz = 2 * H - k;
-#pragma unroll
-                for (int kx = 0; kx < K; ++kx) acc[k] = fma_rn(r[kx], taps.w[(kz * K + ky) * K + kx], acc[k]);
-            }
-        }
-        const int zo = pl - 2 * H;  // acc[0] is complete
-        if (zo >= 0 && col_ok && z0 + zo < (int)nz) out[((size_t)(z0 + zo) * ny + y) * nx + x] = acc[0];
-#pragma unroll
-        for (int k = 0; k < K - 1; ++k) acc[k] = acc[k + 1];
-        acc[K - 1] = 0.f;
-    }
-}
 
-// log_filter_zblock_kernel with each thread owning two columns, x and x + 16,
-// as the halves of packed FP32 pairs: the tile holds (v[x], v[x + 16]) pairs,
-// the taps (w, w), and one fma.rn.f32x2 applies a tap to both outputs with
-// the scalar rounding on each half.  Each output still takes its terms in the
-// reference's order, so the result is bitwise that of log_filter_kernel; a
-// tap now costs half an issue slot per output.  Tile 32 x 8 x 16 outputs,
-// 128 threads, 38 KB of shared memory.
+// The same filter for odd ksize = 2H+1 with H <= 2, register-blocked along
+// z: a thread walks the input planes of its columns once, keeping the K = 2H+1
+// outputs a plane reaches in a rotating window of accumulators (output
+// zo = pl - 2H + k sits in acc[k] and takes tap kz = 2H - k of plane pl;
+// after the plane acc[0] is complete and the window shifts).  Each thread
+// owns two columns, x and x + 16, as the halves of packed FP32 pairs: the
+// tile holds (v[x], v[x + 16]) pairs, the taps (w, w), and one fma.rn.f32x2
+// applies a tap to both outputs with the scalar rounding on each half.
+// Every output still receives its terms in the reference's order (plane =
+// kz ascending, then ky, then kx), so the result is bitwise that of
+// log_filter_kernel at half an issue slot per tap and output.  Tile
+// 32 x 8 x 16 outputs, 128 threads, 38 KB of shared memory.
 template <int H>
 struct LogTaps2 {
     unsigned long long w2[(2 * H + 1) * (2 * H + 1) * (2 * H + 1)];
@@ -351,69 +292,14 @@ __global__ void __launch_bounds__(512) laplacian_filter_kernel(const float* __re
     out[((size_t)z * ny + y) * nx + x] = fma_rn(k3, c, -lap);
 }
 
-// The same filter for H <= 2, register-blocked along z: a thread owns one
-// (x, y) column of TZ outputs.  For each (dx, dy) in the reference's order it
-// loads the input column (TZ + 2H values) once and adds its 2H + 1 z terms
-// into every output, dz ascending, so each output still receives the terms
-// in the order x outermost, z innermost: bitwise equal to
-// laplacian_filter_kernel, with one shared-memory load per 2H + 1 adds
-// instead of one per add, and TZ independent sums.  Tile 32 x 4 x 32 outputs.
-template <int H>
-__global__ void __launch_bounds__(128) laplacian_zblock_kernel(const float* __restrict__ in, float* __restrict__ out,
-                                                               uint32_t nx, uint32_t ny, uint32_t nz, float k3) {
-    constexpr int K = 2 * H + 1, TX = 32, TY = 4, TZ = 32;
-    constexpr int EX = TX + 2 * H, EY = TY + 2 * H, EZ = TZ + 2 * H;
-    __shared__ float tile[EZ][EY][EX];
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-    const int tid = threadIdx.x + TX * threadIdx.y;
-    constexpr int NT = TX * TY, NE = EX * EY * EZ, B = 8;
-    for (int i0 = tid; i0 < NE; i0 += B * NT) {
-        float v[B];
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-            const int i = i0 + u * NT;
-            v[u] = 0.f;  // zero outside the volume
-            if (i < NE) {
-                const int lx = i % EX, ly = (i / EX) % EY, lz = i / (EX * EY);
-                const int gx = x0 + lx - H, gy = y0 + ly - H, gz = z0 + lz - H;
-                if (gx >= 0 && gx < (int)nx && gy >= 0 && gy < (int)ny && gz >= 0 && gz < (int)nz)
-                    v[u] = in[((size_t)gz * ny + gy) * nx + gx];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < B; ++u)
-            if (i0 + u * NT < NE) (&tile[0][0][0])[i0 + u * NT] = v[u];
-    }
-    __syncthreads();
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int x = x0 + tx, y = y0 + ty;
-    if (x >= (int)nx || y >= (int)ny) return;
-    float lap[TZ];
-#pragma unroll
-    for (int z = 0; z < TZ; ++z) lap[z] = 0.f;
-#pragma unroll 1
-    for (int dx = 0; dx < K; ++dx) {
-#pragma unroll 1
-        for (int dy = 0; dy < K; ++dy) {
-            float c[EZ];
-#pragma unroll
-            for (int z = 0; z < EZ; ++z) c[z] = tile[z][ty + dy][tx + dx];
-#pragma unroll
-            for (int z = 0; z < TZ; ++z)
-#pragma unroll
-                for (int dz = 0; dz < K; ++dz) lap[z] = add_rn(lap[z], c[z + dz]);
-        }
-    }
-#pragma unroll
-    for (int z = 0; z < TZ; ++z)
-        if (z0 + z < (int)nz) out[((size_t)(z0 + z) * ny + y) * nx + x] = fma_rn(k3, tile[z + H][ty + H][tx + H], -lap[z]);
-}
 
-// laplacian_zblock_kernel with the column's outputs z and z + 16 as the halves
-// of packed FP32 pairs: the tile holds (v[z], v[z + 16]) pairs along z, and one
-// add.rn.f32x2 adds a neighbour to both sums, each in the reference's order
-// (dx, dy, dz), so the result is bitwise that of the scalar kernel at half the
-// add instructions.
+// laplacianFilter (transient_postprocessing.cuh:21-50) register-blocked along
+// z: a thread owns one (x, y) column of 32 outputs and adds the K^3
+// neighbours of each in the reference's order (dx, dy, dz; zero outside the
+// volume), then centre * K^3 - sum.  The outputs z and z + 16 are the halves
+// of packed FP32 pairs: the tile holds (v[z], v[z + 16]) pairs along z, and
+// one add.rn.f32x2 adds a neighbour to both sums, so the result is bitwise
+// that of the scalar sum at half the add instructions.
 template <int H>
 __global__ void __launch_bounds__(128) laplacian_zpair_kernel(const float* __restrict__ in, float* __restrict__ out,
                                                               uint32_t nx, uint32_t ny, uint32_t nz, float k3) {
