@@ -368,37 +368,37 @@ fbp_status launch_log_fft(fbp_context* ctx, const float* in, float* out, uint32_
                           float sigma, cudaStream_t stream);
 
 // Host-side LoG weights: PostprocessingFilters.cu:102-175 in float, same step order.
-fbp_status log_weights_host(int size, float std1, float* w_final) {
-    if (size <= 0 || !w_final) return set_error(FBP_ERR_INVALID_ARG, "LoG weights: size must be > 0");
-    const int lim = (size - 1) / 2;
-    const float std2 = std1 * std1;
+fbp_status log_weights_host(int size, float sigma, float* taps) {
+    if (size <= 0 || !taps) return set_error(FBP_ERR_INVALID_ARG, "LoG weights: size must be > 0");
+    const int half = (size - 1) / 2;
+    const float var = sigma * sigma;
     const int n = size * size * size;
-    std::vector<float> w(n), r2(n);
-    float maxw = 0.0f;
+    std::vector<float> g(n), rr(n);
+    float gmax = 0.0f;
     for (int kz = 0; kz < size; ++kz)
         for (int ky = 0; ky < size; ++ky)
             for (int kx = 0; kx < size; ++kx) {
-                const float x = (float)(kx - lim), y = (float)(ky - lim), z = (float)(kz - lim);
+                const float x = (float)(kx - half), y = (float)(ky - half), z = (float)(kz - half);
                 const int i = kz * size * size + ky * size + kx;
-                r2[i] = x * x + y * y + z * z;
-                w[i] = std::exp(-(x * x + y * y + z * z) / (2.0f * std2));
-                maxw = std::max(w[i], maxw);
+                rr[i] = x * x + y * y + z * z;
+                g[i] = std::exp(-(x * x + y * y + z * z) / (2.0f * var));
+                gmax = std::max(g[i], gmax);
             }
-    const float threshold = 1.19209290e-07f * maxw;  // FLT_EPSILON * max
-    float sum_w = 0.0f;
-    for (float& v : w) {
-        if (v < threshold) v = 0.0f;
-        sum_w += v;
+    const float cutoff = 1.19209290e-07f * gmax;  // FLT_EPSILON * max
+    float gsum = 0.0f;
+    for (float& v : g) {
+        if (v < cutoff) v = 0.0f;
+        gsum += v;
     }
-    if (sum_w != 0.0f)
-        for (float& v : w) v /= sum_w;
-    float sum_w1 = 0.0f;
+    if (gsum != 0.0f)
+        for (float& v : g) v /= gsum;
+    float lsum = 0.0f;
     for (int i = 0; i < n; ++i) {
-        w[i] = w[i] * (r2[i] - 3.0f * std2) / (std2 * std2);
-        sum_w1 += w[i];
+        g[i] = g[i] * (rr[i] - 3.0f * var) / (var * var);
+        lsum += g[i];
     }
-    const float adjustment = sum_w1 / (float)n;
-    for (int i = 0; i < n; ++i) w_final[i] = w[i] - adjustment;
+    const float mean = lsum / (float)n;  // subtracted so the taps sum to zero
+    for (int i = 0; i < n; ++i) taps[i] = g[i] - mean;
     return FBP_OK;
 }
 
