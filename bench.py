@@ -336,15 +336,29 @@ def run_ours(args):
 
         for _ in range(max(1, args.warmup)):
             e2e_step()
-        barrier(ws)
-        t0 = time.perf_counter()
+        # The capture's H2D copy alone, for the spread of the host-memory DMA.
+        h2d_ms = []
         for _ in range(args.steps):
-            e2e_step()
-        e2e_s = max_over_ranks(time.perf_counter() - t0, ws, dev)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            cube.copy_(host_cube, non_blocking=True)
+            b.record(stream)
+            torch.cuda.synchronize()
+            h2d_ms.append(round(a.elapsed_time(b), 3))
+        barrier(ws)
+        call_ms = []
+        with ClockSampler(local) as clk_e2e:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                t1 = time.perf_counter()
+                e2e_step()
+                call_ms.append(round((time.perf_counter() - t1) * 1e3, 2))
+            e2e_s = max_over_ranks(time.perf_counter() - t0, ws, dev)
         e2e = {"value": ws * samples * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(hc.nbytes + hl.nbytes),
-               "d2h_bytes_per_step": int(hv.nbytes),
+               "d2h_bytes_per_step": int(hv.nbytes), "ms_per_step": e2e_s * 1e3 / args.steps,
                # same kernels, same inputs as the device-resident step
-               "matches_device_path": bool(torch.equal(host_vol.to(dev), vol2))}
+               "matches_device_path": bool(torch.equal(host_vol.to(dev), vol2)),
+               "ms_per_call": call_ms, "h2d_alone_ms": h2d_ms, "clocks": clk_e2e.summary()}
 
     extras = {}
     # The extra legs and the CPU baseline run with one GPU only: at N > 1 the
@@ -818,6 +832,19 @@ def timed_ms(fn, reps=5, stream=None):
     return out, a.elapsed_time(b) / reps
 
 
+def lct_moved_bytes(N, M):
+    """Bytes the fused LCT passes read and write once each: capture in and
+    volume out (4 B), the z spectra of planes kz <= M (complex64; written by
+    the z pass, read and written by the plane pass, read by the inverse z
+    pass) and their Wiener planes; N > 64 adds the row-transformed planes
+    (N x 2N, written, read and written by the column pass, read back)."""
+    P = M + 1
+    b = 8 * M * N * N + 4 * 8 * P * N * N + 8 * P * (2 * N) ** 2
+    if N > 64:
+        b += 4 * 8 * P * N * (2 * N)
+    return b
+
+
 def lct_leg(ctx, dev, peak):
     """LCT of the 64^2 x 512 x 32 ps point capture (200 points) into 64x64x512,
     against the oracle's FP64 restatement of python/lct.py, which is also
@@ -850,11 +877,29 @@ def lct_leg(ctx, dev, peak):
     want = numpy_ref.lct(data.astype(np.float64), 1.0, cap.time_step, 0.8, True, psf=psf, mtx=mtx, mtxi=mtxi)
     t_steps = time.perf_counter() - t0
     got = vol.cpu().numpy()
+    # The row/column-pass form (N >= 128): timed only, its parity is tested.
+    N2, M2 = 128, 1024
+    cap2 = scenes.confocal_points(N2, M2, 16e-12, n_points=200, seed=2)
+    d2 = torch.from_numpy(cap2.cube.reshape(N2, N2, M2).transpose(2, 0, 1).copy()).to(dev)
+    _, ms2 = timed_ms(lambda: ctx.lct(d2, 1.0, cap2.time_step, 0.8, True))
+    bytes2 = 4 * M2 * N2 * N2 * 2 + 2 * 2 * 8 * (2 * M2) * (2 * N2) ** 2
+    moved2 = lct_moved_bytes(N2, M2)
+    del d2
     return {
         "workload": "LCT, 64^2 scan x 512 bins of 32 ps, 200 points -> 64x64x512 (diffuse, snr 0.8)",
+        "rows_cols_form": {"workload": "LCT, 128^2 scan x 1024 bins of 16 ps, 200 points -> 128x128x1024",
+                           "gpu_ms": ms2, "bytes_per_run": bytes2, "achieved_gbs": bytes2 / (ms2 / 1e3) / 1e9,
+                           "frac": bytes2 / (ms2 / 1e3) / 1e9 / peak, "moved_bytes_per_run": moved2,
+                           "moved_frac": moved2 / (ms2 / 1e3) / 1e9 / peak},
         "gpu_ms": ms, "gpu_first_call_s": first_s,
         "roofline": {"bound": "hbm", "bytes_per_run": bytes_run, "achieved_gbs": bytes_run / (ms / 1e3) / 1e9,
-                     "peak_gbs": peak, "frac": bytes_run / (ms / 1e3) / 1e9 / peak},
+                     "peak_gbs": peak, "frac": bytes_run / (ms / 1e3) / 1e9 / peak,
+                     "bytes_note": "4 B per capture and volume element plus one read and write of the padded "
+                                   "complex64 volume per forward and inverse 3-D transform",
+                     "moved_bytes_per_run": lct_moved_bytes(N, M),
+                     "moved_frac": lct_moved_bytes(N, M) / (ms / 1e3) / 1e9 / peak,
+                     "moved_note": "the passes' own buffers, each read or written once: the spectra of planes "
+                                   "kz <= M only (Hermitian z-lines), the Wiener planes kz <= M"},
         "rel_l2_vs_fp64": float(np.linalg.norm(got - want) / np.linalg.norm(want)),
         "cpu": {"kind": "port", "cores": os.cpu_count(), "define_psf_s": t_psf, "resampling_operator_s": t_res,
                 "steps_1_4_s": t_steps, "total_s": t_psf + t_res + t_steps,
@@ -1062,7 +1107,9 @@ def learned_mis_leg(ctx, dev, info, cube, lx, n_train=2000, ks=(4, 8, 16, 32, 64
         return float(np.linalg.norm(d - full_np) / np.linalg.norm(full_np))
 
     cv = cs // 4  # control variate: 4 x 4-point blocks (1/16 of the scan points)
-    arms = (("learned_cv", cdf, cv), ("uniform_cv", None, cv), ("learned", cdf, 0), ("uniform", None, 0))
+    cv8 = cs // 2  # coarser control variate: 8 x 8-point blocks (1/64 of the scan points)
+    arms = (("learned_cv", cdf, cv), ("uniform_cv", None, cv), ("learned_cv8", cdf, cv8), ("uniform_cv8", None, cv8),
+            ("learned", cdf, 0), ("uniform", None, 0))
     rows = []
     for K in ks:
         r = {"K": K}
@@ -1085,7 +1132,10 @@ def learned_mis_leg(ctx, dev, info, cube, lx, n_train=2000, ks=(4, 8, 16, 32, 64
         return None
 
     t_l, t_u = ttt("learned_cv", prop_ms), ttt("uniform_cv", 0.0)
+    t_l8, t_u8 = ttt("learned_cv8", prop_ms), ttt("uniform_cv8", 0.0)
     t_lp, t_up = ttt("learned", prop_ms), ttt("uniform", 0.0)
+    best = min((t, n) for t, n in ((t_l, "learned_cv"), (t_l8, "learned_cv8"), (t_lp, "learned")) if t) \
+        if any((t_l, t_l8, t_lp)) else (None, None)
     mlp.close()
     data_s = data.seconds
     del data
@@ -1095,11 +1145,12 @@ def learned_mis_leg(ctx, dev, info, cube, lx, n_train=2000, ks=(4, 8, 16, 32, 64
         "training": {"scenes": n_train, "tiles": int(n_train * 64), "epochs": 4, "losses": losses,
                      "data_s": data_s, "train_s": train_s},
         "full_bp_ms": full_ms, "proposal_ms": prop_ms, "per_k": rows,
-        "time_to_1pct_ms": {"learned_cv": t_l, "uniform_cv": t_u, "learned": t_lp, "uniform": t_up,
-                            "full_bp": full_ms},
-        "learned_vs_full_time": (t_l / full_ms) if t_l else None,
+        "time_to_1pct_ms": {"learned_cv": t_l, "uniform_cv": t_u, "learned_cv8": t_l8, "uniform_cv8": t_u8,
+                            "learned": t_lp, "uniform": t_up, "full_bp": full_ms},
+        "learned_vs_full_time": (best[0] / full_ms) if best[0] else None, "best_learned_arm": best[1],
         "estimators": "learned_cv / uniform_cv: block-summed control variate (4x4 scan points) + sampled "
-                      "clusters' residuals; learned / uniform: plain cluster sampling; all unbiased",
+                      "clusters' residuals; *_cv8: the same with 8x8-point blocks; learned / uniform: plain "
+                      "cluster sampling; all unbiased",
         "note": "rel-L2 vs the full backprojection of the same BF16 cube; mean over MIS seeds " + str(list(seeds)),
     }
 

@@ -6,19 +6,23 @@
 // (2M, 2N, 2N), takes a 3-D FFT, multiplies by the PSF's Wiener filter and
 // inverse-transforms.  The 3-D transform is separable, so here the axes run
 // in the order z, (y, x) forward, filter, (y, x), z inverse, and only what is
-// not padding is ever stored:
+// not padding is ever stored.  The capture and the PSF are real, so every
+// z-line's spectrum is Hermitian (X[2M - kz] = conj(X[kz])) before and after
+// the (y, x) filtering: only the planes kz = 0..M are computed and stored.
 //   1. lct_zfwd_kernel: per scan point (y, x), radiometric scale, resample
 //      the time axis with mtx, 2M-point FFT along z (the upper M inputs are
-//      zero padding); stores buf[kz][y][x] (an N x N plane per frequency kz).
-//   2. lct_plane_kernel: per kz, the 2N x 2N plane in shared memory (rows and
+//      zero padding), two real lines per complex transform; stores
+//      buf[kz][y][x] for kz <= M (an N x N plane per frequency kz).
+//   2. lct_plane_kernel: per kz <= M, the 2N x 2N plane in shared memory (rows and
 //      columns >= N are zero padding, never materialised: the first pass of
 //      each forward transform skips them, the last pass of each inverse
 //      transform skips outputs that are cut), forward row and column FFTs, times the Wiener
 //      filter, inverse column and row FFTs; stores the N x N corner back.
-//   3. lct_zinv_kernel: per (y, x), inverse 2M-point FFT along z, then rows
-//      z < M of mtx^T (the inverse resample), the 1/(2M 2N 2N) normalisation
-//      and max(real, 0) (lct.py) or the magnitude (lct_2.py); stores
-//      vol[z][y][x].
+//   3. lct_zinv_kernel: per (y, x), the whole z spectrum from the stored half,
+//      inverse 2M-point FFT along z (two lines per complex transform: the
+//      results are real), then rows z < M of mtx^T (the inverse resample), the
+//      1/(2M 2N 2N) normalisation and max(real, 0) (lct.py) or the magnitude
+//      (lct_2.py); stores vol[z][y][x].
 // The FFTs are Stockham passes (radix 16 or 8, then 4 or 2) with compile-time
 // sizes; each pass reads its twiddles from a per-stage table
 // exp(-2 pi i r jm / (Ns R)) built in double precision on the host.
@@ -43,9 +47,9 @@ struct LctFusedParams {
     int power, tiled;
     const float2* tw_z;           // stage tables, n = 2M and n = 2N
     const float2* tw_x;
-    const float2* wiener;         // [2M][2N][2N]
-    float2* buf;                  // [2M][N][N]
-    float2* pad;                  // [2M][N][2N]: rows of the padded planes (N > 64 only)
+    const float2* wiener;         // [2M][2N][2N], planes kz <= M read
+    float2* buf;                  // [M + 1][N][N]
+    float2* pad;                  // [M + 1][N][2N]: rows of the padded planes (N > 64 only)
     float* vol;                   // [M][N][N]
     float scale;                  // 1 / (2M * 2N * 2N)
     int magnitude;                // 1: |vol| (lct_2.py), 0: max(real(vol), 0) (lct.py)
@@ -53,13 +57,15 @@ struct LctFusedParams {
 
 constexpr int kZThreads = 512;
 
-// Lines per CTA of the z kernels: 64 KiB of line buffers at most, at most 8.
+// Real lines per CTA of the z kernels (even: lines j and j + C/2 share one
+// complex transform): 64 KiB of line buffers at most, at most 8.
 constexpr int z_lines(int log2z) { return log2z <= 10 ? 8 : (log2z == 11 ? 4 : 2); }
 
 template <int LOG2Z>
 constexpr size_t zfwd_smem() {
     constexpr int Z = 1 << LOG2Z, C = z_lines(LOG2Z);
-    return ((size_t)C * line_stride(Z) + stage_table_size(LOG2Z)) * sizeof(float2) + (size_t)C * (Z / 2) * sizeof(float);
+    return ((size_t)(C / 2) * line_stride(Z) + stage_table_size(LOG2Z)) * sizeof(float2) +
+           (size_t)C * (Z / 2) * sizeof(float);
 }
 template <int LOG2Z>
 constexpr size_t zinv_smem() {
@@ -76,10 +82,11 @@ constexpr int plane_threads() { return LOG2X >= 7 ? 512 : 256; }
 
 template <int LOG2Z>
 __global__ void __launch_bounds__(kZThreads, 2) lct_zfwd_kernel(LctFusedParams p) {
-    constexpr int Z = 1 << LOG2Z, M = Z / 2, C = z_lines(LOG2Z), LS = line_stride(Z), TWN = stage_table_size(LOG2Z);
+    constexpr int Z = 1 << LOG2Z, M = Z / 2, C = z_lines(LOG2Z), H = C / 2, LS = line_stride(Z),
+                  TWN = stage_table_size(LOG2Z);
     extern __shared__ __align__(16) float2 sm[];
-    float2* lines = sm;
-    float2* tw = lines + C * LS;
+    float2* lines = sm;  // [H] complex lines: line j in the real part, line j + H in the imaginary part
+    float2* tw = lines + H * LS;
     float* raw = reinterpret_cast<float*>(tw + TWN);  // [C][M], scaled capture
     for (int i = threadIdx.x; i < TWN; i += kZThreads) tw[i] = p.tw_z[i];
     const int N = p.N, y = blockIdx.y, x0 = blockIdx.x * C;
@@ -111,13 +118,19 @@ __global__ void __launch_bounds__(kZThreads, 2) lct_zfwd_kernel(LctFusedParams p
         const int i = e / M, zp = e % M;
         float acc = 0.f;
         for (int k = p.rp[zp]; k < p.rp[zp + 1]; ++k) acc = fmaf(p.v[k], raw[i * M + p.ci[k]], acc);
-        lines[i * LS + pidx(zp)] = make_float2(acc, 0.f);
+        reinterpret_cast<float*>(lines + (i % H) * LS + pidx(zp))[i / H] = acc;
     }
     __syncthreads();
-    lean_fft<LOG2Z, 0, C, kZThreads, false, false, true, false>(lines, tw, LS);  // inputs z' >= M are zero
-    for (int e = threadIdx.x; e < C * Z; e += kZThreads) {
+    lean_fft<LOG2Z, 0, H, kZThreads, false, false, true, false>(lines, tw, LS);  // inputs z' >= M are zero
+    // P = FFT(a + i b) of two real lines: A[k] = (P[k] + conj(P[Z - k])) / 2,
+    // B[k] = (P[k] - conj(P[Z - k])) / 2i; kz = 0..M stored.
+    for (int e = threadIdx.x; e < C * (M + 1); e += kZThreads) {
         const int i = e % C, kz = e / C;
-        if (x0 + i < N) p.buf[((size_t)kz * N + y) * N + x0 + i] = lines[i * LS + pidx(kz)];
+        if (x0 + i >= N) continue;
+        const float2* l = lines + (i % H) * LS;
+        const float2 pk = l[pidx(kz)], pm = l[pidx((Z - kz) & (Z - 1))];
+        p.buf[((size_t)kz * N + y) * N + x0 + i] = i < H ? make_float2(0.5f * (pk.x + pm.x), 0.5f * (pk.y - pm.y))
+                                                          : make_float2(0.5f * (pk.y + pm.y), 0.5f * (pm.x - pk.x));
     }
 }
 
@@ -184,40 +197,51 @@ __global__ void __launch_bounds__(plane_threads<LOG2X>()) lct_plane_kernel(LctFu
 
 template <int LOG2Z>
 __global__ void __launch_bounds__(kZThreads, 2) lct_zinv_kernel(LctFusedParams p) {
-    constexpr int Z = 1 << LOG2Z, M = Z / 2, C = z_lines(LOG2Z), LS = line_stride(Z), TWN = stage_table_size(LOG2Z);
+    constexpr int Z = 1 << LOG2Z, M = Z / 2, C = z_lines(LOG2Z), H = C / 2, LS = line_stride(Z),
+                  TWN = stage_table_size(LOG2Z);
     extern __shared__ __align__(16) float2 sm[];
     float2* lines = sm;
     float2* tw = lines + C * LS;
     for (int i = threadIdx.x; i < TWN; i += kZThreads) tw[i] = p.tw_z[i];
     const int N = p.N, y = blockIdx.y, x0 = blockIdx.x * C;
     {
-        constexpr int PL = (C * Z + kZThreads - 1) / kZThreads;
+        constexpr int PL = (C * (M + 1) + kZThreads - 1) / kZThreads;
         float2 t[PL];
 #pragma unroll
         for (int u = 0; u < PL; ++u) {
             const int e = threadIdx.x + u * kZThreads;
             const int i = e % C, kz = e / C;
-            t[u] = (e < C * Z && x0 + i < N) ? p.buf[((size_t)kz * N + y) * N + x0 + i] : make_float2(0.f, 0.f);
+            t[u] = (e < C * (M + 1) && x0 + i < N) ? p.buf[((size_t)kz * N + y) * N + x0 + i] : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < PL; ++u) {
             const int e = threadIdx.x + u * kZThreads;
-            if (e < C * Z) lines[(e % C) * LS + pidx(e / C)] = t[u];
+            if (e < C * (M + 1)) lines[(e % C) * LS + pidx(e / C)] = t[u];
         }
     }
     __syncthreads();
-    lean_fft<LOG2Z, 0, C, kZThreads, true, false, false, true>(lines, tw, LS);  // z < M kept
+    // Q = A + i B over the whole period for the line pair (j, j + H), with
+    // A[Z - k] = conj(A[k]) and B[Z - k] = conj(B[k]) (and the real parts at
+    // k = 0 and M): IFFT(Q) = Re IFFT(A) + i Re IFFT(B).
+    for (int e = threadIdx.x; e < H * (M + 1); e += kZThreads) {
+        const int j = e / (M + 1), k = e % (M + 1);
+        const float2 a = lines[j * LS + pidx(k)], b = lines[(j + H) * LS + pidx(k)];
+        if (k == 0 || k == M) {
+            lines[j * LS + pidx(k)] = make_float2(a.x, b.x);
+        } else {
+            lines[j * LS + pidx(k)] = make_float2(a.x - b.y, a.y + b.x);
+            lines[j * LS + pidx(Z - k)] = make_float2(a.x + b.y, b.x - a.y);
+        }
+    }
+    __syncthreads();
+    lean_fft<LOG2Z, 0, H, kZThreads, true, false, false, true>(lines, tw, LS);  // z < M kept
     for (int e = threadIdx.x; e < C * M; e += kZThreads) {
         const int i = e % C, z = e / C;
         if (x0 + i >= N) continue;
-        float re = 0.f, im = 0.f;
-        for (int k = p.rpt[z]; k < p.rpt[z + 1]; ++k) {
-            const float2 b = lines[i * LS + pidx(p.cit[k])];
-            re = fmaf(p.vt[k], b.x, re);
-            im = fmaf(p.vt[k], b.y, im);
-        }
-        p.vol[((size_t)z * N + y) * N + x0 + i] =
-            p.magnitude ? sqrtf(re * re + im * im) * p.scale : fmaxf(re * p.scale, 0.f);
+        const float* l = reinterpret_cast<const float*>(lines + (i % H) * LS) + i / H;  // a: real, b: imaginary
+        float re = 0.f;
+        for (int k = p.rpt[z]; k < p.rpt[z + 1]; ++k) re = fmaf(p.vt[k], l[2 * pidx(p.cit[k])], re);
+        p.vol[((size_t)z * N + y) * N + x0 + i] = p.magnitude ? fabsf(re) * p.scale : fmaxf(re * p.scale, 0.f);
     }
 }
 
@@ -458,15 +482,15 @@ fbp_status lct_fused_run(fbp_context* ctx, const LctFusedInputs& in, cudaStream_
     FBP_TRY(stage_twiddles(ctx, log2z, s, &p.tw_z));
     FBP_TRY(stage_twiddles(ctx, log2x, s, &p.tw_x));
     void* b = nullptr;
-    FBP_TRY(workspace(ctx, WS_FFT_A, (size_t)2 * M * N * N * sizeof(float2), s, &b));
+    FBP_TRY(workspace(ctx, WS_FFT_A, (size_t)(M + 1) * N * N * sizeof(float2), s, &b));
     p.buf = static_cast<float2*>(b);
     if (N > 64) {
         void* pd = nullptr;
-        FBP_TRY(workspace(ctx, WS_FFT_C, (size_t)2 * M * N * (2 * N) * sizeof(float2), s, &pd));
+        FBP_TRY(workspace(ctx, WS_FFT_C, (size_t)(M + 1) * N * (2 * N) * sizeof(float2), s, &pd));
         p.pad = static_cast<float2*>(pd);
     }
     FBP_TRY(dispatch_z(ctx, log2z, p, true, s));
-    FBP_TRY(dispatch_plane(ctx, log2x, p, 2 * M, s));
+    FBP_TRY(dispatch_plane(ctx, log2x, p, M + 1, s));  // planes kz > M are conjugates
     FBP_TRY(dispatch_z(ctx, log2z, p, false, s));
     return FBP_OK;
 }
