@@ -159,6 +159,157 @@ __global__ void __launch_bounds__(kLogNT) log_x_c2r_kernel(LogFftParams p) {
     }
 }
 
+// ---------------------------------------------- 256-point lines in registers
+// A 256-point line as 16 x 16 (the four-step factorisation, n = n1 + 16 n2,
+// k = k1 + 16 k2): the line's 16 threads each hold v[n2] = x[n1 + 16 n2], take
+// a 16-point DFT over n2 in registers, multiply by w256^(n1 k1), trade values
+// through shared memory once (a transposition), and take a 16-point DFT over
+// n1; the thread then holds v[k2] = X[n1 + 16 k2].  The same holds for the
+// inverse, so a forward and an inverse transform chain without reordering.
+// Shared-memory traffic is one write and one read per element per transform,
+// against one per element per Stockham pass plus the staging of the lines.
+constexpr int kFsRow = 17;                  // a scratch row: 16 values + 1 pad
+constexpr int kFsLine = 16 * kFsRow + 1;    // a line's scratch (odd: conflict-free across lines)
+constexpr int kFsTw = 16 + 256;             // the stage tables of n = 256 (radix 16, 16)
+
+template <bool INV>
+__device__ __forceinline__ void fs256(float2 (&v)[16], float2* s, int n1, const float2* tw) {
+    dft16<INV>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < 16; ++k1) {
+        float2 w = tw[16 + k1 * 16 + n1];  // second stage table: entry jm * 16 + k = w256^(jm k)
+        if (INV) w.y = -w.y;
+        v[k1] = cmul(v[k1], w);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) s[k1 * kFsRow + n1] = v[k1];
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = s[n1 * kFsRow + m];
+    __syncthreads();  // the scratch is free again
+    dft16<INV>(v);
+}
+
+// Pass 1 for nx = 256: thread (line i = row pair, n1); loads straight from
+// the rows, the half spectra split after one more exchange.
+__global__ void __launch_bounds__(kLogNT) log_x_r2c256_kernel(LogFftParams p) {
+    __shared__ float2 tw[kFsTw];
+    __shared__ float2 scratch[16 * kFsLine];
+    for (int e = threadIdx.x; e < kFsTw; e += kLogNT) tw[e] = p.tw[e];
+    const int n1 = threadIdx.x & 15, i = threadIdx.x >> 4;
+    const int z = blockIdx.y, pr = blockIdx.x * 16 + i;
+    const bool ok = pr < p.ny / 2;
+    const float* ra = p.in + ((size_t)z * p.ny + 2 * (size_t)pr) * 256;
+    float2 v[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2)
+        v[n2] = ok ? make_float2(ra[n1 + 16 * n2], ra[256 + n1 + 16 * n2]) : make_float2(0.f, 0.f);
+    __syncthreads();  // tw
+    float2* s = scratch + i * kFsLine;
+    fs256<false>(v, s, n1, tw);
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) s[k2 * kFsRow + n1] = v[k2];
+    __syncthreads();
+    if (!ok) return;
+    float2* sp = p.spec + ((size_t)z * p.ny + 2 * (size_t)pr) * p.hn;
+#pragma unroll
+    for (int k2 = 0; k2 <= 8; ++k2) {
+        const int k = n1 + 16 * k2, km = (256 - k) & 255;
+        if (k > 128) continue;
+        const float2 a = v[k2], b = s[(km >> 4) * kFsRow + (km & 15)];
+        // Z = A + iB with A, B the rows' spectra; conj(Z[-k]) = A - iB at k.
+        sp[k] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+        sp[p.hn + k] = make_float2(0.5f * (a.y + b.y), 0.5f * (b.x - a.x));
+    }
+}
+
+// Passes 2-4 for lines of 256: thread (kx offset i, n1), so each load and
+// store of a warp covers 16 adjacent kx of two lines.
+template <int MODE>
+__global__ void __launch_bounds__(kLogNT) log_strided256_kernel(LogFftParams p, long long es, long long outer) {
+    __shared__ float2 tw[kFsTw];
+    __shared__ float2 scratch[16 * kFsLine];
+    for (int e = threadIdx.x; e < kFsTw; e += kLogNT) tw[e] = p.tw[e];
+    const int i = threadIdx.x & 15, n1 = threadIdx.x >> 4;
+    const int kx0 = blockIdx.x * 16, o = blockIdx.y;
+    const bool ok = kx0 + i < p.hn;
+    float2* base = p.spec + (size_t)o * outer + kx0 + i;
+    float2 v[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) v[n2] = ok ? base[(n1 + 16 * n2) * es] : make_float2(0.f, 0.f);
+    __syncthreads();  // tw
+    float2* s = scratch + i * kFsLine;
+    fs256<MODE == 1>(v, s, n1, tw);
+    if (MODE == 2) {
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) {
+            const float r = log_response(kx0 + i, o, n1 + 16 * k2, p.nx, p.ny, p.nz, p.sigma);
+            v[k2] = make_float2(v[k2].x * r, v[k2].y * r);
+        }
+        fs256<true>(v, s, n1, tw);
+    }
+    if (ok) {
+#pragma unroll
+        for (int k2 = 0; k2 < 16; ++k2) base[(n1 + 16 * k2) * es] = v[k2];
+    }
+}
+
+// Pass 5 for nx = 256: each row pair's full spectrum rebuilt from the half
+// while loading (Z = X_a + i X_b, conjugate symmetry above N/2).
+__global__ void __launch_bounds__(kLogNT) log_x_c2r256_kernel(LogFftParams p) {
+    __shared__ float2 tw[kFsTw];
+    __shared__ float2 scratch[16 * kFsLine];
+    for (int e = threadIdx.x; e < kFsTw; e += kLogNT) tw[e] = p.tw[e];
+    const int n1 = threadIdx.x & 15, i = threadIdx.x >> 4;
+    const int z = blockIdx.y, pr = blockIdx.x * 16 + i;
+    const bool ok = pr < p.ny / 2;
+    const float2* sp = p.spec + ((size_t)z * p.ny + 2 * (size_t)pr) * p.hn;
+    float2 v[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 16; ++n2) {
+        const int k = n1 + 16 * n2, kk = k <= 128 ? k : 256 - k;
+        float2 zk = make_float2(0.f, 0.f);
+        if (ok) {
+            const float2 xa = sp[kk], xb = sp[p.hn + kk];
+            zk = k <= 128 ? make_float2(xa.x - xb.y, xa.y + xb.x) : make_float2(xa.x + xb.y, xb.x - xa.y);
+        }
+        v[n2] = zk;
+    }
+    __syncthreads();  // tw
+    fs256<true>(v, scratch + i * kFsLine, n1, tw);
+    if (!ok) return;
+    float* out = p.out + ((size_t)z * p.ny + 2 * (size_t)pr) * 256;
+#pragma unroll
+    for (int k2 = 0; k2 < 16; ++k2) {
+        out[n1 + 16 * k2] = v[k2].x;
+        out[256 + n1 + 16 * k2] = v[k2].y;
+    }
+}
+
+fbp_status log_pass256(fbp_context* ctx, int kind, const LogFftParams& p, cudaStream_t s) {
+    const unsigned xg = cdiv(p.ny / 2, 16), cg = cdiv(p.hn, 16);
+    switch (kind) {
+        case 0:
+            log_x_r2c256_kernel<<<dim3(xg, p.nz), kLogNT, 0, s>>>(p);
+            FBP_CHECK_LAUNCH(ctx, "log_x_r2c256_kernel");
+            return FBP_OK;
+        case 4:
+            log_x_c2r256_kernel<<<dim3(xg, p.nz), kLogNT, 0, s>>>(p);
+            FBP_CHECK_LAUNCH(ctx, "log_x_c2r256_kernel");
+            return FBP_OK;
+        case 1:
+        case 3:
+            if (kind == 1) log_strided256_kernel<0><<<dim3(cg, p.nz), kLogNT, 0, s>>>(p, p.hn, (long long)p.ny * p.hn);
+            else log_strided256_kernel<1><<<dim3(cg, p.nz), kLogNT, 0, s>>>(p, p.hn, (long long)p.ny * p.hn);
+            FBP_CHECK_LAUNCH(ctx, "log_strided256_kernel");
+            return FBP_OK;
+        default:
+            log_strided256_kernel<2><<<dim3(cg, p.ny), kLogNT, 0, s>>>(p, (long long)p.ny * p.hn, p.hn);
+            FBP_CHECK_LAUNCH(ctx, "log_strided256_kernel");
+            return FBP_OK;
+    }
+}
+
 // One pass of the given kind for axis length 2^log2n.
 // kind 0: x r2c, 1: y forward, 2: z forward * LoG * inverse, 3: y inverse, 4: x c2r.
 template <int LOG2N>
@@ -166,6 +317,11 @@ fbp_status log_pass(fbp_context* ctx, int kind, LogFftParams p, cudaStream_t s) 
     constexpr int C = log_lines(LOG2N);
     constexpr size_t smem = log_smem<LOG2N>();
     FBP_TRY(stage_twiddles(ctx, LOG2N, s, &p.tw));
+    if constexpr (LOG2N == 8) {
+        static_assert(stage_table_size(8) == kFsTw && stage_radix_bits(8, 0) == 4 && stage_radix_bits(8, 4) == 4,
+                      "the register path reads the radix-16 stage tables of n = 256");
+        return log_pass256(ctx, kind, p, s);
+    }
     const unsigned xg = cdiv(p.ny / 2, C), cg = cdiv(p.hn, C);
     switch (kind) {
         case 0: {

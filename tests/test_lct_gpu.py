@@ -134,10 +134,11 @@ def _log_response_xyz(nx, ny, nz, sigma):
     return (-4 * pi * pi * k2 * np.exp(-2 * pi * pi * sigma * sigma * k2)).astype(np.float64)
 
 
-@pytest.mark.parametrize("shape", [(64, 32, 128), (16, 16, 16), (32, 256, 64)])
+@pytest.mark.parametrize("shape", [(64, 32, 128), (16, 16, 16), (32, 256, 64), (256, 32, 256), (32, 256, 256)])
 def test_log_fft_filter_non_cubic(ctx, cuda, shape):
     """Non-cubic volumes (z, y, x): the half-spectrum path for axes in
-    [32, 1024], the full complex passes below that."""
+    [32, 1024], the full complex passes below that; axes of 256 take the
+    register (16 x 16) line transforms (x and z, x and y here)."""
     import torch
     from fasterbackprojection_gb300 import FBP_FILTER_LOG_FFT
 
