@@ -864,7 +864,7 @@ def lct_leg(ctx, dev, peak):
     first = ctx.lct(d, 1.0, cap.time_step, 0.8, True)
     torch.cuda.synchronize()
     first_s = time.perf_counter() - t0
-    vol, ms = timed_ms(lambda: ctx.lct(d, 1.0, cap.time_step, 0.8, True))
+    vol, ms = timed_ms(lambda: ctx.lct(d, 1.0, cap.time_step, 0.8, True), reps=20)
     bytes_run = 4 * M * N * N * 2 + 2 * 2 * 8 * (2 * M) * (2 * N) ** 2
     # CPU: the FP64 NumPy restatement, timed step by step on all host cores.
     t0 = time.perf_counter()
@@ -980,9 +980,9 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
 
     V = vol.numel()
     out = torch.empty_like(vol)
-    _, log_ms = timed_ms(lambda: ctx.postfilter(FBP_FILTER_LOG, vol, 5, 1.0, out=out))
+    _, log_ms = timed_ms(lambda: ctx.postfilter(FBP_FILTER_LOG, vol, 5, 1.0, out=out), reps=20)
     tmp = out.clone()
-    _, norm_ms = timed_ms(lambda: ctx.normalize_(tmp))
+    _, norm_ms = timed_ms(lambda: ctx.normalize_(tmp), reps=20)
     # The allocation-free entry point on the same volume (same result bits).
     import ctypes
 
@@ -991,7 +991,7 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
     lib = _lib.load()
     tmp2 = out.clone()
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    _, na_ms = timed_ms(lambda: lib.fbp_normalize_minmax_noalloc(ctypes.c_void_p(tmp2.data_ptr()), V, sp))
+    _, na_ms = timed_ms(lambda: lib.fbp_normalize_minmax_noalloc(ctypes.c_void_p(tmp2.data_ptr()), V, sp), reps=20)
     res = {"log": {"ms": log_ms, "bytes": 8 * V, "achieved_gbs": 8 * V / (log_ms / 1e3) / 1e9,
                    "frac": 8 * V / (log_ms / 1e3) / 1e9 / peak},
            "normalize": {"ms": norm_ms, "bytes": 12 * V, "achieved_gbs": 12 * V / (norm_ms / 1e3) / 1e9,
@@ -999,7 +999,7 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
                          "noalloc_ms": na_ms, "noalloc_bitwise_equal": bool(torch.equal(tmp, tmp2))}}
     c = cube.clone()
     nb = c.numel()
-    _, fh_ms = timed_ms(lambda: ctx.filter_h_(c, time_step))
+    _, fh_ms = timed_ms(lambda: ctx.filter_h_(c, time_step), reps=20)
     res["filter_h"] = {"ms": fh_ms, "bytes": 8 * nb, "achieved_gbs": 8 * nb / (fh_ms / 1e3) / 1e9,
                        "frac": 8 * nb / (fh_ms / 1e3) / 1e9 / peak,
                        "workload": "256^2 series x 1024 bins, wavelength 10 bins (taps over 1106 padded bins)"}
@@ -1043,7 +1043,7 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
     from fasterbackprojection_gb300 import FBP_FILTER_LOG_FFT
 
     n = vol.shape[0]
-    _, lf_ms = timed_ms(lambda: ctx.postfilter(FBP_FILTER_LOG_FFT, vol, 5, 1.0, out=out))
+    _, lf_ms = timed_ms(lambda: ctx.postfilter(FBP_FILTER_LOG_FFT, vol, 5, 1.0, out=out), reps=20)
     f = torch.fft.fftfreq(n, device=vol.device).float()
     fz, fy, fx = torch.meshgrid(f, f, f[: n // 2 + 1].abs(), indexing="ij")
     k2 = fx * fx + fy * fy + fz * fz
@@ -1055,7 +1055,7 @@ def filters_leg(ctx, dev, vol, cube, time_step, peak):
 
     cf_ms = 0.0
     try:
-        _, cf_ms = timed_ms(cufft_path)
+        _, cf_ms = timed_ms(cufft_path, reps=20)
         rel = float(torch.linalg.vector_norm((out - ref_out).double()) / torch.linalg.vector_norm(ref_out.double()))
     except RuntimeError as e:  # pragma: no cover
         rel = None
