@@ -75,6 +75,7 @@ struct ConfocalGatherParams {
     SampleParams smp;    // used by the sampled (MIS) variant only
     float vs[3];         // voxel size (the voxel-scattering variant's extent)
     int exact_weights;   // 1: every weight by its own rcp.approx (FBP_WEIGHTS_REFERENCE)
+    int scat_exact;      // voxel scattering: every walk is exactly the unrolled steps long (no tail loop)
 
     // Per scan point of a stage, in shared memory: (x, y, z, bounce), (bias,
     // slot address), the sample weight, three planning ints, and the packed

@@ -179,6 +179,28 @@ fbp_status dispatch_confocal(fbp_context* ctx, const ConfocalGatherParams& p, di
     return go_confocal<S, PATH_FAST, false, SAMPLED, false>(ctx, p, grid, smem, stream);
 }
 
+// The voxel-scattering walk with unconditional unrolled steps (prefix sp),
+// clamped window index only where the window is the whole row.
+fbp_status dispatch_scatter_free(fbp_context* ctx, const ConfocalGatherParams& p, dim3 grid, size_t smem,
+                                 cudaStream_t stream, int sp, bool bounce, bool capped) {
+    constexpr int F = PATH_SCATTER + kScatterForms;
+    switch ((sp - 2) + (bounce ? 4 : 0) + (capped ? 8 : 0)) {
+        case 0: return go_confocal<float, F, false, false, false, kKV>(ctx, p, grid, smem, stream);
+        case 1: return go_confocal<float, F + 1, false, false, false, kKV>(ctx, p, grid, smem, stream);
+        case 2: return go_confocal<float, F + 2, false, false, false, kKV>(ctx, p, grid, smem, stream);
+        case 4: return go_confocal<float, F, true, false, false, kKV>(ctx, p, grid, smem, stream);
+        case 5: return go_confocal<float, F + 1, true, false, false, kKV>(ctx, p, grid, smem, stream);
+        case 6: return go_confocal<float, F + 2, true, false, false, kKV>(ctx, p, grid, smem, stream);
+        case 8: return go_confocal<float, F, false, false, true, kKV>(ctx, p, grid, smem, stream);
+        case 9: return go_confocal<float, F + 1, false, false, true, kKV>(ctx, p, grid, smem, stream);
+        case 10: return go_confocal<float, F + 2, false, false, true, kKV>(ctx, p, grid, smem, stream);
+        case 12: return go_confocal<float, F, true, false, true, kKV>(ctx, p, grid, smem, stream);
+        case 13: return go_confocal<float, F + 1, true, false, true, kKV>(ctx, p, grid, smem, stream);
+        case 14: return go_confocal<float, F + 2, true, false, true, kKV>(ctx, p, grid, smem, stream);
+        default: return set_error(FBP_ERR_INTERNAL, "voxel scattering: no kernel for this step prefix");
+    }
+}
+
 // Depth slices [z_begin, z_end) of the volume (the whole volume by default)
 // into `volume` ([z_end - z_begin][Vy][Vx]).  The window plan and the voxel
 // tables are those of the whole volume, so with z_begin a multiple of the
@@ -201,11 +223,12 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     WindowPlan wp;
     // The sampled kernel also holds its cluster list in static shared memory.
     // The voxel-scattering variant reads every bin of dist -/+ half the voxel
-    // diagonal, one step past the end.
+    // diagonal, one step past the end (up to max(step, diagonal) from 0 where
+    // a walk is clipped at 0).
     const double vdiag = std::sqrt((double)in.voxel_size[0] * in.voxel_size[0] +
                                    (double)in.voxel_size[1] * in.voxel_size[1] +
                                    (double)in.voxel_size[2] * in.voxel_size[2]);
-    const double extra = scatter ? 1.02 * vdiag + 2.0 * std::fabs((double)in.time_step) : 0.0;
+    const double extra = scatter ? 1.52 * vdiag + 2.0 * std::fabs((double)in.time_step) : 0.0;
     FBP_TRY(plan_window(ctx, ex, ey, ez, in.time_step, T, ALIGN, sizeof(float),
                         ConfocalGatherParams::meta_bytes(32) + (smp ? kSampledStaticSmem : 0) +
                             kahan_smem_bytes((int)kv, 32 * kWY * kWZ) + 16,
@@ -235,19 +258,26 @@ fbp_status launch_confocal(fbp_context* ctx, const fbp_recon_info& in, const voi
     if (scatter) {
         // Steps per (voxel, scan point): at most ceil(diagonal / (dt + EPS)),
         // one more where rounding lands on the end; the kernel unrolls 2..4
-        // of them and loops over the rest.
-        const double steps = std::ceil(vdiag / ((double)in.time_step + (double)FBP_EPS));
+        // of them and loops over the rest.  Where even the shortest walk
+        // takes all the unrolled steps (a 1e-4 m margin over the rounding of
+        // the path arithmetic below 64 m) they need no end test, and the
+        // unclamped window index of the other paths applies.
+        const double step = (double)in.time_step + (double)FBP_EPS;
+        const double steps = std::ceil(vdiag / step);
         const int sp = (int)std::min(std::max(steps, 2.0), (double)kScatterMaxPrefix);
-        if (sp == 2) {
-            if (bounce) return go_confocal<float, PATH_SCATTER, true, false, true, kKV>(ctx, p, grid, wp.smem, stream);
-            return go_confocal<float, PATH_SCATTER, false, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+        const bool free_walk = (sp - 1) * step + 1e-4 < vdiag;
+        // ... and where none takes more (sp steps already pass the far end).
+        p.scat_exact = free_walk && sp * step > vdiag + 1e-4;
+        switch ((sp - 2) + (free_walk ? kScatterForms : 0) + (bounce ? 8 : 0)) {
+            case 0: return go_confocal<float, PATH_SCATTER, false, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+            case 1: return go_confocal<float, PATH_SCATTER + 1, false, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+            case 2: return go_confocal<float, PATH_SCATTER + 2, false, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+            case 8: return go_confocal<float, PATH_SCATTER, true, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+            case 9: return go_confocal<float, PATH_SCATTER + 1, true, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+            case 10: return go_confocal<float, PATH_SCATTER + 2, true, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+            default: break;
         }
-        if (sp == 3) {
-            if (bounce) return go_confocal<float, PATH_SCATTER + 1, true, false, true, kKV>(ctx, p, grid, wp.smem, stream);
-            return go_confocal<float, PATH_SCATTER + 1, false, false, true, kKV>(ctx, p, grid, wp.smem, stream);
-        }
-        if (bounce) return go_confocal<float, PATH_SCATTER + 2, true, false, true, kKV>(ctx, p, grid, wp.smem, stream);
-        return go_confocal<float, PATH_SCATTER + 2, false, false, true, kKV>(ctx, p, grid, wp.smem, stream);
+        return dispatch_scatter_free(ctx, p, grid, wp.smem, stream, sp, bounce, wp.capped);
     }
     if (smp) return dispatch_confocal<float, true>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);
     return dispatch_confocal<float, false>(ctx, p, grid, wp.smem, stream, bounce, in.time_offset, wp.capped);

@@ -22,10 +22,18 @@ namespace fbp {
 //               steps run unrolled and predicated (the voxels' walks
 //               interleave), any further ones in a loop; bins by the same
 //               round-toward-zero add (the path is never negative).
+//   PATH_SCATTER + 3 + j  the same where every walk takes at least 2 + j
+//               steps: the host checks (1 + j) (dt + EPS) + 1e-4 m < the
+//               voxel diagonal, and stages with a path under 3.5 mm past
+//               the half diagonal or of 64 m or more take the predicated
+//               reference loop, so the unrolled steps add unconditionally
+//               (the rounding of dd over four steps stays below 2e-5 m).
 enum { PATH_2D = 0, PATH_FAST = 1, PATH_EXACT = 2, PATH_SCATTER = 3 };
 constexpr int kScatterMaxPrefix = 4;
+constexpr int kScatterForms = kScatterMaxPrefix - 1;  // prefixes 2, 3, 4
 __host__ __device__ constexpr bool is_scatter(int path) { return path >= PATH_SCATTER; }
-__host__ __device__ constexpr int scatter_prefix(int path) { return path - PATH_SCATTER + 2; }
+__host__ __device__ constexpr int scatter_prefix(int path) { return (path - PATH_SCATTER) % kScatterForms + 2; }
+__host__ __device__ constexpr bool scatter_free(int path) { return path - PATH_SCATTER >= kScatterForms; }
 
 template <typename S>
 __device__ __forceinline__ float lds_elem(uint32_t addr);
@@ -59,7 +67,8 @@ template <typename S, int KV, int PATH, bool BOUNCE, bool CLAMP, bool SAFE, bool
 __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, const ulonglong2* __restrict__ geo2,
                                                const int2* __restrict__ meta, const float* __restrict__ wts, int nl, const float (&px)[KV], float py,
                                                float pz, float neg_t0, float rcp_dt, uint32_t slot_w,
-                                               float (&acc)[KV], float ext = 0.f, float step = 0.f) {
+                                               float (&acc)[KV], float ext = 0.f, float step = 0.f,
+                                               bool tail = true) {
     constexpr int SH = ElemShift<S>::value;
     const float rcp2 = 2.f * rcp_dt;  // exact
     if constexpr (is_scatter(PATH)) {
@@ -81,7 +90,8 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
             const float dy2 = mul_rn(dy, dy);
             auto bin_at = [&](float dd) -> uint32_t {
                 const uint32_t bits = __float_as_uint(add_rz(ref_bin_ratio(dd, rcp_dt), bias));
-                return (uint32_t)m.y + (min(bits - 0x4B000000u, slot_w) << SH);
+                if (CLAMP) return (uint32_t)m.y + (min(bits - 0x4B000000u, slot_w) << SH);
+                return (uint32_t)m.y + (bits << SH);  // every read inside the planned window; bias folded into m.y
             };
             // Steps SP.. of one walk (rare: a diagonal longer than the planned steps).
             auto walk_rest = [&](float a, float dd, float dmax, float w) -> float {
@@ -117,15 +127,26 @@ __device__ __forceinline__ void confocal_stage(const float4* __restrict__ geo, c
                         float d0, d1, b0, b1, p0, p1;
                         unpack2(dd, d0, d1);
                         unpack2(add_rz2(mul_rn2(dd, rdp), biasp), b0, b1);
-                        const uint32_t i0 = min(__float_as_uint(b0) - 0x4B000000u, slot_w);
-                        const uint32_t i1 = min(__float_as_uint(b1) - 0x4B000000u, slot_w);
+                        const uint32_t i0 = CLAMP ? min(__float_as_uint(b0) - 0x4B000000u, slot_w) : __float_as_uint(b0);
+                        const uint32_t i1 = CLAMP ? min(__float_as_uint(b1) - 0x4B000000u, slot_w) : __float_as_uint(b1);
                         f32x2_t I = pack2(lds_elem<S>((uint32_t)m.y + (i0 << SH)),
                                           lds_elem<S>((uint32_t)m.y + (i1 << SH)));
                         if (WEIGHTED) I = mul_rn2(I, wlp);
                         unpack2(mul_rn2(I, w), p0, p1);
-                        a0 = add_rn_if_lt(a0, p0, d0, h0);
-                        a1 = add_rn_if_lt(a1, p1, d1, h1);
+                        if constexpr (scatter_free(PATH)) {
+                            a0 = add_rn(a0, p0);  // dd < dmax holds for every unrolled step
+                            a1 = add_rn(a1, p1);
+                        } else {
+                            a0 = add_rn_if_lt(a0, p0, d0, h0);
+                            a1 = add_rn_if_lt(a1, p1, d1, h1);
+                        }
                         dd = add_rn2(dd, stepp);
+                    }
+                    if (scatter_free(PATH) && !tail) {
+                        // Every walk is exactly the unrolled steps long.
+                        acc[2 * j] = a0;
+                        acc[2 * j + 1] = a1;
+                        continue;
                     }
                     float d0, d1, w0, w1;
                     unpack2(dd, d0, d1);
@@ -479,14 +500,18 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
                 const float dmax = sqrtf(fx * fx + fy * fy + fz * fz);
                 const float bnc = BOUNCE ? g.w : 0.f;
                 float pmin = 2.f * dmin + neg_t0 + bnc, pmax = 2.f * dmax + neg_t0 + bnc;
-                if (is_scatter(PATH)) {  // the bins of dist -/+ ext, stepped past dist + ext
+                if (is_scatter(PATH)) {
+                    // The bins of dist -/+ ext, read one step past dist + ext;
+                    // a walk clipped at 0 reads up to max(step, 2 ext).
                     pmin = fmaxf(0.f, pmin - 1.01f * scat_ext);
-                    pmax = pmax + 1.01f * scat_ext + scat_step;
+                    pmax = fmaxf(pmax + 1.01f * scat_ext, 2.02f * scat_ext) + scat_step;
                 }
                 // Paths this short make dist^2 <= EPS possible: use safeRCP's
                 // branch.  Paths this long (or NaN) could take the batched
                 // reciprocal's products out of the FP32 range: also per voxel.
-                near = pmin < 0.0035f || !(pmax < 1.0e4f);
+                // The unconditional scattering walk also wants paths under
+                // 64 m (its rounding bound) and dist - ext > 0 (pmin above).
+                near = pmin < 0.0035f || !(pmax < (scatter_free(PATH) ? 64.f : 1.0e4f));
                 // Conservative bin range with a 2-bin margin for rounding.
                 const int blo = (int)fmaxf(fminf(floorf(pmin * rcp_dt), 1.0e9f), -1.0e9f) - 2;
                 const int bhi = (int)fmaxf(fminf(floorf(pmax * rcp_dt), 1.0e9f), -1.0e9f) + 2;
@@ -614,7 +639,8 @@ __device__ __forceinline__ void confocal_tile(const ConfocalGatherParams& p, uin
         float scale = 1.f;
         if (!safe) {
             confocal_stage<S, KV, PATH, BOUNCE, CLAMP, false, SAMPLED>(geo, geo2, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
-                                                                        p.slot_w, acc, scat_ext, scat_step);
+                                                                        p.slot_w, acc, scat_ext, scat_step,
+                                                                        !p.scat_exact);
             if (PATH == PATH_2D) scale = 0.25f;  // w was rcp(d^2) = 4 rcp(dist^2)
         } else {
             confocal_stage<S, KV, PATH, BOUNCE, CLAMP, true, SAMPLED>(geo, geo2, meta, wts, nl, px, py, pz, neg_t0, rcp_dt,
