@@ -622,9 +622,14 @@ def scatter_forms_leg(ctx, dev, info, cube, lx):
     out = {}
     V = info.voxel_res[0] * info.voxel_res[1] * info.voxel_res[2]
     pairs = V * info.num_laser_targets
+    n = int(round(info.num_laser_targets ** 0.5))
+    vdiag = sum(float(v) ** 2 for v in info.voxel_size) ** 0.5
+    bin_m = info.time_step
+    shape = f"{n}^2 x {info.num_time_bins} FP32 -> {info.voxel_res[0]}^3"
     vol = torch.empty(V, dtype=torch.float32, device=dev)
     _, ms = timed_ms(lambda: ctx.backproject_confocal_scatter(info, cube, lx, out=vol), reps=2)
-    e = {"workload": "256^2 x 1024 FP32 -> 256^3, voxel extent sqrt(3) * 7.8 mm / 2 = 6.8 mm, bins of 4.8 mm",
+    e = {"workload": f"{shape}, voxel extent (diagonal) {vdiag * 1e3:.1f} mm, bins of {bin_m * 1e3:.1f} mm "
+                     f"(about {vdiag / bin_m:.1f} bins per walk)",
          "ms": ms, "value": pairs / (ms / 1e3), "unit": UNIT}
     try:
         from oracle import harness
@@ -654,7 +659,7 @@ def scatter_forms_leg(ctx, dev, info, cube, lx):
     mvol = torch.empty(V, dtype=torch.float32, device=dev)
     _, m_ms = timed_ms(lambda: ctx.mis_backproject(info, cube, lx, FBP_MIS_REFERENCE_SCATTER, 64, noise=noise,
                                                    out=mvol), reps=2)
-    m = {"workload": "64 samples per voxel, 256^2 x 1024 FP32 -> 256^3, walks of about 3 bins", "ms": m_ms,
+    m = {"workload": f"64 samples per voxel, {shape}, walks of about {vdiag / bin_m:.1f} bins", "ms": m_ms,
          "samples_per_s": V * 64 / (m_ms / 1e3)}
     try:
         from oracle import harness
@@ -680,7 +685,7 @@ def scatter_forms_leg(ctx, dev, info, cube, lx):
     svol = torch.empty(V, dtype=torch.float32, device=dev)
     _, ms = timed_ms(lambda: ctx.splat_backproject(info, cube, lx, max_bins=700, grid=(256, 256), out=svol), reps=2)
     nz = int((cube[:, :700] > 1.1920929e-7).sum())
-    out["splat"] = {"workload": "256^2 x 1024 FP32, bins < 700, 256 x 256 pixel grid -> 256^3", "ms": ms,
+    out["splat"] = {"workload": f"{shape}, bins < 700, 256 x 256 pixel grid", "ms": ms,
                     "instances": nz, "instances_per_s": nz / (ms / 1e3),
                     "gl_timing": "unavailable on this box (no graphics stack)"}
     del svol
