@@ -195,6 +195,115 @@ __global__ void __launch_bounds__(plane_threads<LOG2X>()) lct_plane_kernel(LctFu
     }
 }
 
+// The plane pass for 2N = 128 with the 128-point transforms in registers
+// (8 x 16, the four-step factorisation): a line's 8 threads hold 16 values
+// each (n = n1 + 8 n2), take a 16-point DFT, multiply by w128^(n1 k1) (the
+// second stage table of n = 128), trade values once through shared memory,
+// and take two 8-point DFTs (k1 = n1 and n1 + 8); the thread then holds
+// X[n1 + 8 j], the same distribution as its input.  Rows (y < 64) go to a
+// 64 x 130 plane in shared memory; the columns run in rounds (forward, times
+// the Wiener filter, whose loads are issued before the forward transform,
+// inverse, rows y < 64 kept) and go back to the plane; the inverse rows keep
+// x < 64 and store to global memory.  Rows: 8 adjacent threads per row;
+// columns: a warp holds one n1 of 32 adjacent columns, so the Wiener and
+// plane accesses of a warp are 256 contiguous bytes.  256 threads (32 lines
+// at a time) keep a CTA near 105 KB, so two share an SM.
+constexpr int kP128Threads = 256;
+constexpr int kP128Lines = kP128Threads / 8;
+constexpr int kP128Ps = 136;                  // plane row stride (8 mod 16: conflict-free row pairs)
+constexpr int kP128RowLine = 16 * 9 + 8;      // a row's exchange scratch (8 mod 16 between the rows of a half-warp)
+constexpr int kP128ColLine = 16 * 9 + 9;      // a column's (odd: the 16 columns of a half-warp)
+constexpr int kP128Tw = 16 + 128;             // the stage tables of n = 128 (radix 16, 8)
+constexpr size_t kP128Smem = ((size_t)64 * kP128Ps + (size_t)kP128Lines * kP128ColLine + kP128Tw) * sizeof(float2);
+
+template <bool INV>
+__device__ __forceinline__ void fs128(float2 (&v)[16], float2* s, int n1, const float2* tw) {
+    dft16<INV>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < 16; ++k1) {
+        float2 w = tw[16 + k1 * 8 + n1];  // second stage table: entry jm * 8 + k = w128^(jm k)
+        if (INV) w.y = -w.y;
+        v[k1] = cmul(v[k1], w);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 16; ++k1) s[k1 * 9 + n1] = v[k1];
+    __syncthreads();
+    float2 a[8], b[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        a[m] = s[n1 * 9 + m];
+        b[m] = s[(n1 + 8) * 9 + m];
+    }
+    __syncthreads();  // the scratch is free again
+    dft8<INV>(a);     // X[n1 + 16 k2]
+    dft8<INV>(b);     // X[n1 + 8 + 16 k2]
+#pragma unroll
+    for (int k2 = 0; k2 < 8; ++k2) {
+        v[2 * k2] = a[k2];
+        v[2 * k2 + 1] = b[k2];
+    }
+}
+
+__global__ void __launch_bounds__(kP128Threads, 2) lct_plane128_kernel(LctFusedParams p) {
+    constexpr int X = 128, N = 64;
+    extern __shared__ __align__(16) float2 sm[];
+    float2* plane = sm;                              // [64][kP128Ps]
+    float2* scratch = plane + 64 * kP128Ps;          // [kP128Lines][kP128ColLine]
+    float2* tw = scratch + kP128Lines * kP128ColLine;
+    for (int i = threadIdx.x; i < kP128Tw; i += kP128Threads) tw[i] = p.tw_x[i];
+    const size_t kz = blockIdx.x;
+    float2* g = p.buf + kz * N * N;
+    const int line = threadIdx.x >> 3, n1 = threadIdx.x & 7;
+    float2* s = scratch + line * kP128RowLine;
+    float2 v[16];
+    __syncthreads();  // tw
+    // Forward rows y < 64 (inputs x >= 64 are zero).
+#pragma unroll 1
+    for (int r0 = 0; r0 < N; r0 += kP128Lines) {
+        const int y = r0 + line;
+#pragma unroll
+        for (int n2 = 0; n2 < 8; ++n2) v[n2] = g[y * N + n1 + 8 * n2];
+#pragma unroll
+        for (int n2 = 8; n2 < 16; ++n2) v[n2] = make_float2(0.f, 0.f);
+        fs128<false>(v, s, n1, tw);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) plane[y * kP128Ps + n1 + 8 * j] = v[j];
+    }
+    __syncthreads();
+    // Columns: forward (rows y >= 64 are zero), the Wiener filter, inverse keeping y < 64.
+    const float2* wz = p.wiener + kz * X * X;
+    const int cl = threadIdx.x & 31, u = threadIdx.x >> 5;  // column of the round, its n1
+    float2* sc = scratch + cl * kP128ColLine;
+#pragma unroll 1
+    for (int c0 = 0; c0 < X; c0 += kP128Lines) {
+        const int kx = c0 + cl;
+        float2 wf[16];  // the column's Wiener values, in flight during the forward transform
+#pragma unroll
+        for (int j = 0; j < 16; ++j) wf[j] = wz[(u + 8 * j) * X + kx];
+#pragma unroll
+        for (int m2 = 0; m2 < 8; ++m2) v[m2] = plane[(u + 8 * m2) * kP128Ps + kx];
+#pragma unroll
+        for (int m2 = 8; m2 < 16; ++m2) v[m2] = make_float2(0.f, 0.f);
+        fs128<false>(v, sc, u, tw);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = cmul(v[j], wf[j]);
+        fs128<true>(v, sc, u, tw);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) plane[(u + 8 * j) * kP128Ps + kx] = v[j];
+    }
+    __syncthreads();
+    // Inverse rows y < 64, x < 64 kept.
+#pragma unroll 1
+    for (int r0 = 0; r0 < N; r0 += kP128Lines) {
+        const int y = r0 + line;
+#pragma unroll
+        for (int n2 = 0; n2 < 16; ++n2) v[n2] = plane[y * kP128Ps + n1 + 8 * n2];
+        fs128<true>(v, s, n1, tw);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) g[y * N + n1 + 8 * j] = v[j];
+    }
+}
+
 template <int LOG2Z>
 __global__ void __launch_bounds__(kZThreads, 2) lct_zinv_kernel(LctFusedParams p) {
     constexpr int Z = 1 << LOG2Z, M = Z / 2, C = z_lines(LOG2Z), H = C / 2, LS = line_stride(Z),
@@ -417,12 +526,21 @@ fbp_status dispatch_z(fbp_context* ctx, int log2z, const LctFusedParams& p, bool
     }
 }
 
+fbp_status launch_plane128(fbp_context* ctx, const LctFusedParams& p, unsigned planes, cudaStream_t s) {
+    static_assert(stage_table_size(7) == kP128Tw && stage_radix_bits(7, 0) == 4 && stage_radix_bits(7, 4) == 3,
+                  "the register path reads the radix-16, radix-8 stage tables of n = 128");
+    FBP_TRY_CUDA(cudaFuncSetAttribute(lct_plane128_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP128Smem));
+    lct_plane128_kernel<<<planes, kP128Threads, kP128Smem, s>>>(p);
+    FBP_CHECK_LAUNCH(ctx, "lct_plane128_kernel");
+    return FBP_OK;
+}
+
 fbp_status dispatch_plane(fbp_context* ctx, int log2x, const LctFusedParams& p, unsigned planes, cudaStream_t s) {
     switch (log2x) {
         case 4: return launch_plane<4>(ctx, p, planes, s);
         case 5: return launch_plane<5>(ctx, p, planes, s);
         case 6: return launch_plane<6>(ctx, p, planes, s);
-        case 7: return launch_plane<7>(ctx, p, planes, s);
+        case 7: return launch_plane128(ctx, p, planes, s);
         case 8: return launch_rows_cols<8>(ctx, p, planes, s);
         case 9: return launch_rows_cols<9>(ctx, p, planes, s);
         case 10: return launch_rows_cols<10>(ctx, p, planes, s);
