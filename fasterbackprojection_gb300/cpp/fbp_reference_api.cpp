@@ -96,7 +96,7 @@ NLosData::NLosData(const std::string& filename, bool saveBinary, bool useBinary)
     if (useBinary && loadBinaryFile(binary)) return;
     if (filename.size() >= 5 && filename.substr(filename.size() - 5) == ".nlos" && loadBinaryFile(filename)) return;
     (void)saveBinary;
-    throw std::runtime_error("NLosData: HDF5/MAT captures are not readable in this build; provide the .nlos cache: " +
+    throw std::runtime_error("NLosData: HDF5/MAT captures are not readable by this library (no HDF5 reader); provide the .nlos cache: " +
                              binary);
 }
 

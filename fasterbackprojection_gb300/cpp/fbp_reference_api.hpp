@@ -105,7 +105,7 @@ public:
 
     NLosData() = default;
     // NLosData.cpp:15-127: filename's ".nlos" twin is read when present (useBinary);
-    // HDF5/MAT parsing is not available in this build and throws.
+    // this library has no HDF5/MAT reader: other files throw.
     explicit NLosData(const std::string& filename, bool saveBinary = true, bool useBinary = true);
     virtual ~NLosData() = default;
 
