@@ -45,7 +45,7 @@ def test_confocal_random_geometries_bitwise(ctx, harness, cuda, mode):
     discard, t0 = {"plain": (1, 0.0), "bounces": (0, 0.0), "t0": (1, 0.6), "bounces_t0": (0, 0.6)}[mode]
     rng = np.random.default_rng(5000 + len(mode))
     cube = _cube(cuda)
-    bad = total = 0
+    bad = total = nonzero = 0
     with reference_weights(ctx):
         for _ in range(60):
             res = tuple(int(r) for r in rng.integers(5, 70, 3))
@@ -56,7 +56,9 @@ def test_confocal_random_geometries_bitwise(ctx, harness, cuda, mode):
             torch.cuda.synchronize()
             bad += int((ref.view(torch.int32) != got.view(torch.int32)).sum())
             total += ref.numel()
+            nonzero += int((ref != 0).sum())
     ctx.check_device_status()
+    assert nonzero > total // 5, f"{nonzero} of {total} voxels non-zero"
     assert bad == 0, f"{bad} of {total} voxels differ from the reference kernel"
 
 
@@ -72,7 +74,7 @@ def test_voxel_scattering_random_geometries_bitwise(ctx, harness, cuda, mode):
         pytest.skip("voxel-scattering build of the reference kernels not present")
     rng = np.random.default_rng(6000 + len(mode) * 7)
     cube = _cube(cuda)
-    bad = total = 0
+    bad = total = nonzero = 0
     for _ in range(40):
         res = tuple(int(r) for r in rng.integers(5, 48, 3))
         info = _rand_geometry(rng, 32, T, 0 if mode == "bounces" else 1, 0.6 if mode == "t0" else 0.0, res=res)
@@ -86,7 +88,9 @@ def test_voxel_scattering_random_geometries_bitwise(ctx, harness, cuda, mode):
         torch.cuda.synchronize()
         bad += int((ref.view(torch.int32) != got.view(torch.int32)).sum())
         total += ref.numel()
+        nonzero += int((ref != 0).sum())
     ctx.check_device_status()
+    assert nonzero > total // 5, f"{nonzero} of {total} voxels non-zero"
     assert bad == 0, f"{bad} of {total} voxels differ from the reference scattering kernel"
 
 
@@ -132,3 +136,41 @@ def test_log_fft_256_axes_vs_fp64(ctx, cuda, shape):
     want = np.real(np.fft.ifftn(np.fft.fftn(vol.astype(np.float64)) * _log_response(nx, ny, nz, 1.3)))
     want *= nx * ny * nz
     assert rel_l2(got, want) < 5e-6
+
+
+def test_exhaustive_random_grids_vs_fp64(ctx, cuda):
+    """backprojectExhaustiveVoxel (transient_reconstruction.cuh:138-166) over
+    random laser / SPAD grids (4-36 lasers and SPADs: stages of up to 64 pairs
+    with ragged last stages, laser blocks of 4 and single lasers), ragged
+    volumes and random time offsets and bounce modes, against the FP64 oracle
+    with the GPU's bins."""
+    import torch
+    from fasterbackprojection_gb300 import FBP_EXHAUSTIVE, make_info, scenes
+    from oracle import cpu
+
+    rng = np.random.default_rng(7100)
+    worst, compared = 0.0, 0
+    for trial in range(12):
+        nl, ns = int(rng.integers(2, 7)), int(rng.integers(2, 7))
+        Tb = int(rng.choice([256, 512, 1024]))  # 64 bins of 32 ps end before the scene's paths
+        cap = scenes.exhaustive_points(nl, ns, Tb, 32e-12, n_points=20, seed=7100 + trial)
+        L, S, Tb = cap.cube.shape
+        vres = tuple(int(r) for r in rng.integers(6, 26, 3))
+        hmin, vs = scenes.volume_geometry(vres, depth_range=(0.0, float(rng.uniform(1.2, 2.4))))
+        info = make_info(num_laser_targets=L, num_sensor_targets=S, num_time_bins=Tb, time_step=cap.time_step,
+                         voxel_res=vres, hidden_min=hmin, voxel_size=vs, capture_system=FBP_EXHAUSTIVE,
+                         discard_first_last_bounces=int(rng.integers(0, 2)), laser_position=(0.0, -0.2, 0.1),
+                         sensor_position=(0.1, -0.3, 0.0), time_offset=float(rng.choice([0.0, -0.05, 0.2])))
+        cube = torch.from_numpy(cap.cube).to(cuda)
+        lx = torch.from_numpy(cap.laser_xyz).to(cuda)
+        sx = torch.from_numpy(cap.sensor_xyz).to(cuda)
+        got = ctx.backproject_exhaustive(info, cube, lx, sx).cpu().numpy()
+        V = vres[0] * vres[1] * vres[2]
+        bins = ctx.debug_exhaustive_bins(info, lx, sx, torch.arange(V, device=cuda)).cpu().numpy()
+        want = cpu.exhaustive_voxel(info, cap.cube, cap.laser_xyz, cap.sensor_xyz, bins=bins)
+        if float(np.abs(want).max()) > 0:
+            worst = max(worst, rel_l2(got, want))
+            compared += 1
+    ctx.check_device_status()
+    assert compared >= 10, compared
+    assert worst < 1e-6, worst
